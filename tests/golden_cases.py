@@ -1,0 +1,69 @@
+"""Loading of the golden fixtures written by tests/golden/make_golden.py."""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+
+from fcfc_gb300 import pcfile
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def case_names():
+    return sorted(d for d in os.listdir(GOLDEN)
+                  if os.path.isfile(os.path.join(GOLDEN, d, "meta.json")))
+
+
+class Case:
+    def __init__(self, name):
+        self.name = name
+        self.dir = os.path.join(GOLDEN, name)
+        with open(os.path.join(self.dir, "meta.json")) as f:
+            self.meta = json.load(f)
+        self.cats = {l: np.load(os.path.join(self.dir, l + ".npy"))
+                     for l in self.meta["labels"]}
+        self.box = self.meta.get("geometry") == "box"
+        self.sedges = None
+        if self.meta.get("sfile"):
+            t = np.loadtxt(os.path.join(self.dir, self.meta["sfile"]), ndmin=2)
+            # read_bins: lower edges, with the midpoint of a discontinuity
+            e = np.empty(len(t) + 1)
+            e[0] = t[0, 0]
+            for i in range(1, len(t)):
+                e[i] = t[i, 0] if t[i, 0] == t[i - 1, 1] else 0.5 * (t[i, 0] + t[i - 1, 1])
+            e[-1] = t[-1, 1]
+            self.sedges = e
+
+    def pcfile(self, pair):
+        return pcfile.read_binary(os.path.join(self.dir, pair + ".bin"))
+
+    def bins_kwargs(self):
+        m = self.meta
+        kw = dict(bintype=m["bintype"])
+        if self.sedges is not None:
+            kw.update(ns=len(self.sedges) - 1, sedges=self.sedges)
+        else:
+            s = m["sbin"]
+            n, v = 0, s["smin"]
+            while v < s["smax"] - 1e-10:
+                v += s["ds"]
+                n += 1
+            kw.update(ns=n, smin=s["smin"], ds=s["ds"])
+        if m["bintype"] == 1:
+            kw["nmu"] = m.get("nmu", 10)
+        if m["bintype"] == 2:
+            p = m["pbin"]
+            n, v = 0, p["pmin"]
+            while v < p["pmax"] - 1e-10:
+                v += p["dpi"]
+                n += 1
+            kw.update(np_=n, pmin=p["pmin"], dpi=p["dpi"])
+        if self.box:
+            kw["box"] = (m["box"] * 3)[:3] if len(m["box"]) == 1 else m["box"]
+        return kw
+
+    def xyzw(self, label):
+        a = self.cats[label]
+        return a[:, :3], (a[:, 3] if a.shape[1] > 3 else None)
