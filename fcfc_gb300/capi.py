@@ -1,0 +1,158 @@
+"""ctypes binding of libfcfcg.so (include/fcfcg.h).
+
+The shared library is the product: every count runs on the GPU through it.
+Importing this module does not need a GPU; creating a device context does,
+and fails with FCFCGError(FCFCG_ERR_CUDA) when there is none.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libfcfcg.so")
+
+OK = 0
+ERR_MEMORY, ERR_ARG, ERR_FILE, ERR_CFG = -1, -2, -3, -4
+ERR_DATA, ERR_CNVT, ERR_CF, ERR_SAVE, ERR_UNKNOWN = -21, -22, -24, -25, -99
+ERR_CUDA, ERR_TIMEOUT, ERR_UNSUPPORTED = -100, -101, -102
+BIN_ISO, BIN_SMU, BIN_SPI = 0, 1, 2
+GEOM_BOX, GEOM_SURVEY = 0, 1
+PREC_FP32_RECHECK, PREC_FP64 = 0, 1
+TAB_INT, TAB_HYBRID = 0, 1
+
+_dp = C.POINTER(C.c_double)
+
+
+class Binning(C.Structure):
+    _fields_ = [("geometry", C.c_int), ("bintype", C.c_int),
+                ("box", C.c_double * 3), ("ns", C.c_int), ("smin", C.c_double),
+                ("ds", C.c_double), ("sedges", _dp), ("nmu", C.c_int),
+                ("np", C.c_int), ("pmin", C.c_double), ("dpi", C.c_double),
+                ("pedges", _dp)]
+
+
+class BinsInfo(C.Structure):
+    _fields_ = [("ns", C.c_int), ("nmu", C.c_int), ("np", C.c_int),
+                ("ntot", C.c_int64), ("tabtype", C.c_int),
+                ("rescale", C.c_double), ("box_rescaled", C.c_double * 3),
+                ("nstab", C.c_int64), ("nptab", C.c_int64)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("candidates", C.c_uint64), ("in_range", C.c_uint64),
+                ("rechecked", C.c_uint64), ("recheck_inline", C.c_uint64),
+                ("ms_grid", C.c_double), ("ms_count", C.c_double),
+                ("ms_recheck", C.c_double), ("ms_total", C.c_double),
+                ("cells_per_smax", C.c_int), ("ncell", C.c_int * 3),
+                ("nstencil", C.c_int), ("nchunks", C.c_uint64),
+                ("precision_used", C.c_int)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["ncell"] = list(self.ncell)
+        return d
+
+
+class FCFCGError(RuntimeError):
+    def __init__(self, code, msg=""):
+        super().__init__("%s (%d)%s" % (strerror(code), code,
+                                         (": " + msg) if msg else ""))
+        self.code = code
+
+
+# Every exported entry point with its prototype: (restype, argtypes).
+P = C.c_void_p
+PROTOTYPES = {
+    "fcfcg_strerror": (C.c_char_p, [C.c_int]),
+    "fcfcg_last_error": (C.c_char_p, [P]),
+    "fcfcg_linear_nbin": (C.c_int, [C.c_double, C.c_double, C.c_double]),
+    "fcfcg_create": (C.c_int, [C.POINTER(Binning), C.c_int, C.POINTER(P)]),
+    "fcfcg_create_host": (C.c_int, [C.POINTER(Binning), C.POINTER(P)]),
+    "fcfcg_destroy": (None, [P]),
+    "fcfcg_bins_info_get": (C.c_int, [P, C.POINTER(BinsInfo)]),
+    "fcfcg_bins_edges": (C.c_int, [P, P, P]),
+    "fcfcg_bins_tables": (C.c_int, [P, P, P, P, P]),
+    "fcfcg_load_catalog": (C.c_int, [P, C.c_int, C.c_size_t, P, P, P, P]),
+    "fcfcg_load_catalog_device": (C.c_int, [P, C.c_int, C.c_size_t, P, P, P, P]),
+    "fcfcg_catalog_info": (C.c_int, [P, C.c_int, C.POINTER(C.c_size_t),
+                                     C.POINTER(C.c_double)]),
+    "fcfcg_count": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                              P, P]),
+    "fcfcg_stats_get": (C.c_int, [P, C.POINTER(Stats)]),
+    "fcfcg_set_cells_per_smax": (C.c_int, [P, C.c_int]),
+    "fcfcg_norm": (C.c_double, [C.c_int, C.c_int, C.c_double, C.c_double]),
+    "fcfcg_analytic_rr": (C.c_int, [P, P]),
+    "fcfcg_multipoles": (C.c_int, [P, P, C.c_int, P, P]),
+    "fcfcg_wp": (C.c_int, [P, P, P]),
+    "fcfcg_write_paircount": (C.c_int, [P, C.c_char_p, C.c_int, C.c_int,
+                                        C.c_int, P, P, C.c_double, P, P, P]),
+    "fcfcg_read_paircount": (C.c_int, [P, C.c_char_p, P, P, P, P, P, P, P,
+                                       P]),
+    "fcfcg_write_cf": (C.c_int, [P, C.c_char_p, P]),
+    "fcfcg_write_multipoles": (C.c_int, [P, C.c_char_p, C.c_int, P, P]),
+    "fcfcg_write_wp": (C.c_int, [P, C.c_char_p, P]),
+}
+
+_lib = None
+
+
+def load_library(path: str | None = None):
+    """Load libfcfcg.so (building it first if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        from . import build
+        build.build()
+    lib = C.CDLL(path)
+    for name, (res, args) in PROTOTYPES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def strerror(code: int) -> str:
+    return load_library().fcfcg_strerror(code).decode()
+
+
+def ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def make_binning(geometry, bintype, box=None, ns=None, smin=0.0, ds=1.0,
+                 sedges=None, nmu=1, np_=0, pmin=0.0, dpi=1.0, pedges=None,
+                 smax=None, pmax=None):
+    """Binning struct plus the arrays it points to (keep both alive)."""
+    lib = load_library()
+    keep = []
+    b = Binning()
+    b.geometry, b.bintype = int(geometry), int(bintype)
+    bx = [0.0, 0.0, 0.0] if box is None else list(
+        np.broadcast_to(np.asarray(box, float), (3,)))
+    b.box = (C.c_double * 3)(*bx)
+    if sedges is not None:
+        se = np.ascontiguousarray(sedges, np.float64)
+        keep.append(se)
+        b.sedges = se.ctypes.data_as(_dp)
+        b.ns = len(se) - 1
+    else:
+        if ns is None:
+            ns = lib.fcfcg_linear_nbin(smin, smax, ds)
+        b.ns, b.smin, b.ds = int(ns), float(smin), float(ds)
+    b.nmu = int(nmu)
+    if pedges is not None:
+        pe = np.ascontiguousarray(pedges, np.float64)
+        keep.append(pe)
+        b.pedges = pe.ctypes.data_as(_dp)
+        b.np = len(pe) - 1
+    else:
+        if bintype == BIN_SPI and not np_:
+            np_ = lib.fcfcg_linear_nbin(pmin, pmax, dpi)
+        b.np, b.pmin, b.dpi = int(np_), float(pmin), float(dpi)
+    return b, keep

@@ -1,0 +1,939 @@
+/*
+ * ctx.c -- host side of the engine: contexts, catalogues, the cell grid and
+ * its stencil, the FP32 rounding bounds, and the count driver that replaces
+ * FCFC's count_pairs (src/fcfc/2pt_box/count_func.c:4847-7725 and the survey
+ * twin src/fcfc/2pt/count_func.c:4846).  C99 on the CUDA runtime C API.
+ */
+#include <cuda_runtime_api.h>
+#include <float.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "fcfcg_internal.h"
+
+typedef struct {
+  size_t n, cap;
+  int has_w;
+  double sumw, wmax;
+  int wexp;
+  double *x, *y, *z, *s, *w;       /* rescaled FP64 (device) */
+  double xabs, s2abs;              /* max |coordinate|, max |x|^2 (host) */
+  double bmin[3], bmax[3];         /* bounding box (rescaled) */
+  /* sorted copy for the current grid */
+  size_t scap;
+  float *l4, *wlo;
+  double *sx, *sy, *sz, *ss, *sw;
+  uint32_t *sid, *cell_of;
+  uint32_t *cstart;
+  size_t ccap;
+  int grid_valid;
+  int gsig_n[3];
+  double gsig_cw[3], gsig_lo[3];
+} slot_t;
+
+struct fcfcg_ctx {
+  fcfcg_bins bins;
+  int host_only;
+  int device, nsm;
+  cudaStream_t stream;
+  char err[512];
+  int kcell;
+  slot_t slot[FCFCG_MAX_SLOT];
+  /* shared scratch */
+  uint32_t *cfill, *scan_tmp, *cchunk, *chunks;
+  size_t cfill_cap, scan_cap, cchunk_cap, chunk_cap;
+  uint16_t *d_fs, *d_fp, *d_rs, *d_rp;
+  double *d_s2edge, *d_pedge;
+  int *d_sten;
+  float *d_stenD;
+  unsigned long long *d_cnt, *d_wt, *d_stats, *d_bbox;
+  double *d_wd;
+  uint32_t *d_head, *d_qcount, *d_queue;
+  size_t qcap;
+  void *h_pinned;
+  size_t h_pinned_cap;
+  fcfcg_stats stats;
+  cudaEvent_t ev[5];
+  int sten[4 * FCFCG_MAX_STENCIL];
+  float stD[4 * FCFCG_MAX_STENCIL];
+};
+
+static void set_err(fcfcg_ctx *c, const char *fmt, ...) {
+  if (!c) return;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(c->err, sizeof c->err, fmt, ap);
+  va_end(ap);
+}
+
+#define CK(call)                                                          \
+  do {                                                                    \
+    cudaError_t e_ = (call);                                              \
+    if (e_ != cudaSuccess) {                                              \
+      set_err(c, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+              __LINE__);                                                  \
+      return FCFCG_ERR_CUDA;                                              \
+    }                                                                     \
+  } while (0)
+
+#define CKK(call)                                                         \
+  do {                                                                    \
+    int e_ = (call);                                                      \
+    if (e_) {                                                             \
+      set_err(c, "%s: %s", #call, fcfcg_cuda_errstr(e_));                 \
+      return FCFCG_ERR_CUDA;                                              \
+    }                                                                     \
+  } while (0)
+
+const char *fcfcg_strerror(int err) {
+  switch (err) {
+    case FCFCG_OK: return "success";
+    case FCFCG_ERR_MEMORY: return "memory allocation failed";
+    case FCFCG_ERR_ARG: return "invalid argument";
+    case FCFCG_ERR_FILE: return "file error";
+    case FCFCG_ERR_CFG: return "invalid configuration";
+    case FCFCG_ERR_DATA: return "invalid catalogue data";
+    case FCFCG_ERR_CNVT: return "coordinate conversion failed";
+    case FCFCG_ERR_CF: return "correlation function set-up failed";
+    case FCFCG_ERR_SAVE: return "failed to save results";
+    case FCFCG_ERR_CUDA: return "CUDA error";
+    case FCFCG_ERR_TIMEOUT: return "device wait timed out";
+    case FCFCG_ERR_UNSUPPORTED: return "configuration not supported";
+    default: return "unknown error";
+  }
+}
+
+const char *fcfcg_last_error(const fcfcg_ctx *ctx) {
+  return ctx ? ctx->err : "no context";
+}
+
+/* Grow a device buffer to at least `need` bytes. */
+static int grow(fcfcg_ctx *c, void **p, size_t *cap, size_t need) {
+  if (*cap >= need && *p) return FCFCG_OK;
+  if (*p) cudaFree(*p);
+  *p = NULL;
+  *cap = 0;
+  size_t alloc = need ? need : 16;
+  CK(cudaMalloc(p, alloc));
+  *cap = alloc;
+  return FCFCG_OK;
+}
+
+#define GROW(ptr, capv, bytes)                                              \
+  do {                                                                      \
+    size_t cap_ = (capv);                                                   \
+    int r_ = grow(c, (void **) &(ptr), &cap_, (bytes));                     \
+    if (r_) return r_;                                                      \
+    (capv) = cap_;                                                          \
+  } while (0)
+
+static int upload(fcfcg_ctx *c, void **dst, const void *src, size_t bytes) {
+  if (*dst) cudaFree(*dst);
+  *dst = NULL;
+  CK(cudaMalloc(dst, bytes ? bytes : 16));
+  if (bytes) CK(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice,
+                                c->stream));
+  return FCFCG_OK;
+}
+
+static void slot_free(slot_t *s) {
+  void *p[] = {s->x, s->y, s->z, s->s, s->w, s->l4, s->wlo, s->sx, s->sy,
+               s->sz, s->ss, s->sw, s->sid, s->cell_of, s->cstart};
+  for (size_t i = 0; i < sizeof p / sizeof p[0]; i++)
+    if (p[i]) cudaFree(p[i]);
+  memset(s, 0, sizeof *s);
+}
+
+void fcfcg_destroy(fcfcg_ctx *c) {
+  if (!c) return;
+  if (!c->host_only) {
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (int i = 0; i < FCFCG_MAX_SLOT; i++) slot_free(c->slot + i);
+    void *p[] = {c->cfill, c->scan_tmp, c->cchunk, c->chunks, c->d_fs,
+                 c->d_fp, c->d_rs, c->d_rp, c->d_s2edge, c->d_pedge,
+                 c->d_sten, c->d_stenD, c->d_cnt, c->d_wt, c->d_stats,
+                 c->d_bbox, c->d_wd, c->d_head, c->d_queue};
+    for (size_t i = 0; i < sizeof p / sizeof p[0]; i++)
+      if (p[i]) cudaFree(p[i]);
+    if (c->h_pinned) cudaFreeHost(c->h_pinned);
+    for (int i = 0; i < 5; i++)
+      if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    if (c->stream) cudaStreamDestroy(c->stream);
+  }
+  fcfcg_bins_release(&c->bins);
+  free(c);
+}
+
+int fcfcg_create_host(const fcfcg_binning *cfg, fcfcg_ctx **out) {
+  if (!out) return FCFCG_ERR_ARG;
+  *out = NULL;
+  fcfcg_ctx *c = calloc(1, sizeof *c);
+  if (!c) return FCFCG_ERR_MEMORY;
+  c->host_only = 1;
+  int rc = fcfcg_bins_setup(cfg, &c->bins, c->err, sizeof c->err);
+  if (rc) {
+    /* keep the message: hand the context back so the caller can read it */
+    *out = c;
+    return rc;
+  }
+  *out = c;
+  return FCFCG_OK;
+}
+
+int fcfcg_create(const fcfcg_binning *cfg, int device, fcfcg_ctx **out) {
+  int rc = fcfcg_create_host(cfg, out);
+  if (rc) return rc;
+  fcfcg_ctx *c = *out;
+  c->host_only = 0;
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev < 1) {
+    set_err(c, "no CUDA device available (%s)",
+            e ? cudaGetErrorString(e) : "0 devices");
+    c->host_only = 1;
+    return FCFCG_ERR_CUDA;
+  }
+  if (device < 0) CK(cudaGetDevice(&device));
+  c->device = device;
+  CK(cudaSetDevice(device));
+  CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device));
+  CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  for (int i = 0; i < 5; i++) CK(cudaEventCreate(&c->ev[i]));
+  const fcfcg_bins *b = &c->bins;
+  /* reference tables and FP32 window tables */
+  rc = upload(c, (void **) &c->d_rs, b->s.rtab, sizeof(uint16_t) * b->s.nrtab);
+  if (rc) return rc;
+  rc = upload(c, (void **) &c->d_s2edge, b->s.edge,
+              sizeof(double) * (b->s.nbin + 1));
+  if (rc) return rc;
+  if (b->s.ftab) {
+    rc = upload(c, (void **) &c->d_fs, b->s.ftab, sizeof(uint16_t) * b->s.nftab);
+    if (rc) return rc;
+  }
+  if (b->bintype == FCFCG_BIN_SPI) {
+    rc = upload(c, (void **) &c->d_rp, b->p.rtab, sizeof(uint16_t) * b->p.nrtab);
+    if (rc) return rc;
+    rc = upload(c, (void **) &c->d_pedge, b->p.edge,
+                sizeof(double) * (b->p.nbin + 1));
+    if (rc) return rc;
+    if (b->p.ftab) {
+      rc = upload(c, (void **) &c->d_fp, b->p.ftab,
+                  sizeof(uint16_t) * b->p.nftab);
+      if (rc) return rc;
+    }
+  }
+  CK(cudaMalloc((void **) &c->d_cnt, sizeof(unsigned long long) * b->ntot));
+  CK(cudaMalloc((void **) &c->d_wt, sizeof(unsigned long long) * 2 * b->ntot));
+  CK(cudaMalloc((void **) &c->d_wd, sizeof(double) * b->ntot));
+  CK(cudaMalloc((void **) &c->d_stats, sizeof(unsigned long long) * 8));
+  CK(cudaMalloc((void **) &c->d_bbox, sizeof(unsigned long long) * 6));
+  CK(cudaMalloc((void **) &c->d_head, sizeof(uint32_t) * 4));
+  c->d_qcount = c->d_head + 1;
+  c->qcap = (size_t) 1 << 22;
+  CK(cudaMalloc((void **) &c->d_queue, sizeof(uint32_t) * 4 * c->qcap));
+  CK(cudaStreamSynchronize(c->stream));
+  return FCFCG_OK;
+}
+
+int fcfcg_bins_info_get(const fcfcg_ctx *c, fcfcg_bins_info *o) {
+  if (!c || !o) return FCFCG_ERR_ARG;
+  const fcfcg_bins *b = &c->bins;
+  if (!b->sbin_raw) return FCFCG_ERR_CF;
+  o->ns = b->ns;
+  o->nmu = b->nmu;
+  o->np = b->np;
+  o->ntot = b->ntot;
+  o->tabtype = b->s.tabtype;
+  o->rescale = b->rescale;
+  for (int k = 0; k < 3; k++) o->box_rescaled[k] = b->box[k];
+  o->nstab = b->s.nrtab;
+  o->nptab = (b->bintype == FCFCG_BIN_SPI) ? b->p.nrtab : 0;
+  return FCFCG_OK;
+}
+
+int fcfcg_bins_edges(const fcfcg_ctx *c, double *sbin, double *pbin) {
+  if (!c || !c->bins.sbin_raw) return FCFCG_ERR_ARG;
+  if (sbin) memcpy(sbin, c->bins.sbin_raw, sizeof(double) * (c->bins.ns + 1));
+  if (pbin && c->bins.pbin_raw)
+    memcpy(pbin, c->bins.pbin_raw, sizeof(double) * (c->bins.np + 1));
+  return FCFCG_OK;
+}
+
+int fcfcg_bins_tables(const fcfcg_ctx *c, uint16_t *stab, uint16_t *ptab,
+    double *s2bin, double *pbin) {
+  if (!c || !c->bins.sbin_raw) return FCFCG_ERR_ARG;
+  const fcfcg_bins *b = &c->bins;
+  if (stab) memcpy(stab, b->s.rtab, sizeof(uint16_t) * b->s.nrtab);
+  if (s2bin) memcpy(s2bin, b->s.edge, sizeof(double) * (b->s.nbin + 1));
+  if (b->bintype == FCFCG_BIN_SPI) {
+    if (ptab) memcpy(ptab, b->p.rtab, sizeof(uint16_t) * b->p.nrtab);
+    if (pbin) memcpy(pbin, b->p.edge, sizeof(double) * (b->p.nbin + 1));
+  }
+  return FCFCG_OK;
+}
+
+int fcfcg_set_cells_per_smax(fcfcg_ctx *c, int k) {
+  if (!c || k < 0 || k > 8) return FCFCG_ERR_ARG;
+  c->kcell = k;
+  for (int i = 0; i < FCFCG_MAX_SLOT; i++) c->slot[i].grid_valid = 0;
+  return FCFCG_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Catalogues.                                                               */
+
+static int load_common(fcfcg_ctx *c, int slot, size_t n, const double *x,
+    const double *y, const double *z, const double *w, int on_device) {
+  if (!c || c->host_only) return FCFCG_ERR_ARG;
+  if (slot < 0 || slot >= FCFCG_MAX_SLOT) {
+    set_err(c, "slot %d out of range", slot);
+    return FCFCG_ERR_ARG;
+  }
+  if (n > 0xFFFFFFF0u) {
+    set_err(c, "catalogue too large (%zu objects)", n);
+    return FCFCG_ERR_ARG;
+  }
+  if (n && (!x || !y || !z)) return FCFCG_ERR_ARG;
+  CK(cudaSetDevice(c->device));
+  slot_t *s = c->slot + slot;
+  const int survey = (c->bins.geometry == FCFCG_GEOM_SURVEY);
+  if (s->cap < n || !s->x) {
+    slot_free(s);
+    size_t m = n ? n : 1;
+    CK(cudaMalloc((void **) &s->x, sizeof(double) * m));
+    CK(cudaMalloc((void **) &s->y, sizeof(double) * m));
+    CK(cudaMalloc((void **) &s->z, sizeof(double) * m));
+    CK(cudaMalloc((void **) &s->s, sizeof(double) * m));
+    CK(cudaMalloc((void **) &s->w, sizeof(double) * m));
+    s->cap = m;
+  }
+  s->n = n;
+  s->has_w = (w != NULL);
+  s->grid_valid = 0;
+  double *tx = NULL, *ty = NULL, *tz = NULL, *tw = NULL;
+  const double *ix = x, *iy = y, *iz = z, *iw = w;
+  if (!on_device && n) {
+    /* stage raw input in the output arrays, then rescale in place */
+    CK(cudaMemcpyAsync(s->x, x, sizeof(double) * n, cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaMemcpyAsync(s->y, y, sizeof(double) * n, cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaMemcpyAsync(s->z, z, sizeof(double) * n, cudaMemcpyHostToDevice,
+                       c->stream));
+    if (w)
+      CK(cudaMemcpyAsync(s->w, w, sizeof(double) * n, cudaMemcpyHostToDevice,
+                         c->stream));
+    ix = tx = s->x;
+    iy = ty = s->y;
+    iz = tz = s->z;
+    iw = w ? (tw = s->w) : NULL;
+  }
+  (void) tx; (void) ty; (void) tz; (void) tw;
+  unsigned long long *wbits = c->d_stats + 7;
+  CK(cudaMemsetAsync(wbits, 0, sizeof(unsigned long long), c->stream));
+  CKK(fcfcg_k_prep(c->stream, n, ix, iy, iz, iw, c->bins.rescale, survey,
+                   s->x, s->y, s->z, s->s, s->w, wbits));
+  /* bounding box of the rescaled catalogue and max |w| */
+  unsigned long long init[6] = {~0ull, ~0ull, ~0ull, 0, 0, 0};
+  CK(cudaMemcpyAsync(c->d_bbox, init, sizeof init, cudaMemcpyHostToDevice,
+                     c->stream));
+  CKK(fcfcg_k_bbox(c->stream, n, s->x, s->y, s->z, c->d_bbox));
+  unsigned long long hb[7];
+  CK(cudaMemcpyAsync(hb, c->d_bbox, sizeof(unsigned long long) * 6,
+                     cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(hb + 6, wbits, sizeof(unsigned long long),
+                     cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  double mn[3], mx[3];
+  for (int k = 0; k < 3; k++) {
+    unsigned long long a = hb[k], bb = hb[3 + k];
+    a = (a >> 63) ? (a & 0x7FFFFFFFFFFFFFFFull) : ~a;
+    bb = (bb >> 63) ? (bb & 0x7FFFFFFFFFFFFFFFull) : ~bb;
+    memcpy(mn + k, &a, 8);
+    memcpy(mx + k, &bb, 8);
+  }
+  s->xabs = 0;
+  s->s2abs = 0;
+  if (n) {
+    for (int k = 0; k < 3; k++) {
+      if (!isfinite(mn[k]) || !isfinite(mx[k])) {
+        set_err(c, "catalogue in slot %d holds non-finite coordinates", slot);
+        return FCFCG_ERR_DATA;
+      }
+      double a = fmax(fabs(mn[k]), fabs(mx[k]));
+      s->xabs = fmax(s->xabs, a);
+      s->s2abs += a * a;
+      if (c->bins.geometry == FCFCG_GEOM_BOX) {
+        const double L = c->bins.box[k];
+        const double tol = L * 1e-9;
+        if (mn[k] < -tol || mx[k] > L + tol) {
+          set_err(c, "catalogue in slot %d leaves the box along axis %d "
+                  "([%g, %g] after rescaling, box %g)", slot, k, mn[k],
+                  mx[k], L);
+          return FCFCG_ERR_DATA;
+        }
+      }
+      s->bmin[k] = mn[k];
+      s->bmax[k] = mx[k];
+    }
+  }
+  memcpy(&s->wmax, hb + 6, 8);
+  if (!w) s->wmax = 1;
+  if (w && !isfinite(s->wmax)) {
+    set_err(c, "catalogue in slot %d holds non-finite weights", slot);
+    return FCFCG_ERR_DATA;
+  }
+  s->wexp = (s->wmax > 0) ? (int) ceil(log2(s->wmax)) : 0;
+  if (ldexp(1.0, s->wexp) < s->wmax) s->wexp++;
+  /* sum of weights on the host, in input order (the reference sums with an
+   * OpenMP reduction whose order varies) */
+  if (w) {
+    double sum = 0;
+    if (on_device) {
+      double *hw = malloc(sizeof(double) * (n ? n : 1));
+      if (!hw) return FCFCG_ERR_MEMORY;
+      cudaError_t e = cudaMemcpy(hw, s->w, sizeof(double) * n,
+                                 cudaMemcpyDeviceToHost);
+      if (e) {
+        free(hw);
+        CK(e);
+      }
+      for (size_t i = 0; i < n; i++) sum += hw[i];
+      free(hw);
+    } else {
+      for (size_t i = 0; i < n; i++) sum += w[i];
+    }
+    s->sumw = sum;
+  } else {
+    s->sumw = (double) n;
+  }
+  return FCFCG_OK;
+}
+
+int fcfcg_load_catalog(fcfcg_ctx *c, int slot, size_t n, const double *x,
+    const double *y, const double *z, const double *w) {
+  return load_common(c, slot, n, x, y, z, w, 0);
+}
+
+int fcfcg_load_catalog_device(fcfcg_ctx *c, int slot, size_t n,
+    const double *x, const double *y, const double *z, const double *w) {
+  return load_common(c, slot, n, x, y, z, w, 1);
+}
+
+int fcfcg_catalog_info(const fcfcg_ctx *c, int slot, size_t *n,
+    double *sumw) {
+  if (!c || slot < 0 || slot >= FCFCG_MAX_SLOT) return FCFCG_ERR_ARG;
+  if (n) *n = c->slot[slot].n;
+  if (sumw) *sumw = c->slot[slot].sumw;
+  return FCFCG_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Grid, stencil and bounds.                                                 */
+
+typedef struct {
+  int n[3];
+  double cw[3], lo[3];
+  double reach[3];     /* largest separation along each axis that counts */
+  double reach3;       /* largest 3D separation that counts */
+  int k;
+} grid_t;
+
+static double box_volume(const double v[3]) { return v[0] * v[1] * v[2]; }
+
+static int pick_k(double density, double reach) {
+  /* cells of at least ~48 points where possible, between 1 and 4 cells per
+   * maximum separation */
+  int k = 1;
+  for (int t = 4; t >= 1; t--) {
+    double cw = reach / t;
+    if (density * cw * cw * cw >= 48.0) {
+      k = t;
+      break;
+    }
+  }
+  return k;
+}
+
+static int grid_setup(fcfcg_ctx *c, grid_t *g, const slot_t *A,
+    const slot_t *B) {
+  const fcfcg_bins *b = &c->bins;
+  const int box = (b->geometry == FCFCG_GEOM_BOX);
+  double r3;
+  if (b->bintype == FCFCG_BIN_SPI) {
+    double smax = sqrt(b->s.vmax);
+    double pmax = box ? b->p.vmax : sqrt(b->p.vmax);
+    r3 = sqrt(b->s.vmax + pmax * pmax);
+    if (box) {
+      g->reach[0] = g->reach[1] = smax;
+      g->reach[2] = pmax;
+    } else {
+      g->reach[0] = g->reach[1] = g->reach[2] = r3;
+    }
+  } else {
+    r3 = sqrt(b->s.vmax);
+    g->reach[0] = g->reach[1] = g->reach[2] = r3;
+  }
+  g->reach3 = r3;
+  double lo[3], hi[3];
+  if (box) {
+    for (int k = 0; k < 3; k++) {
+      lo[k] = 0;
+      hi[k] = b->box[k];
+    }
+  } else {
+    for (int k = 0; k < 3; k++) {
+      lo[k] = fmin(A->bmin[k], B->bmin[k]);
+      hi[k] = fmax(A->bmax[k], B->bmax[k]);
+      if (!(hi[k] > lo[k])) hi[k] = lo[k] + 1;
+    }
+  }
+  double ext[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
+  double vol = box_volume(ext);
+  double density = (double) B->n / (vol > 0 ? vol : 1);
+  int k = c->kcell ? c->kcell : pick_k(density, r3);
+  g->k = k;
+  const double maxcells = 16.0 * 1024 * 1024;
+  double scale = 1;
+  for (;;) {
+    double tot = 1;
+    for (int d = 0; d < 3; d++) {
+      double cwt = g->reach[d] / k * scale;
+      int n = (int) floor(ext[d] / cwt);
+      if (n < 1) n = 1;
+      if (n > 4096) n = 4096;
+      g->n[d] = n;
+      tot *= n;
+    }
+    if (tot <= maxcells) break;
+    scale *= 1.25;
+  }
+  for (int d = 0; d < 3; d++) {
+    g->lo[d] = lo[d];
+    g->cw[d] = box ? b->box[d] / g->n[d] : ext[d] / g->n[d] * (1 + 1e-12);
+  }
+  return FCFCG_OK;
+}
+
+/* Cell offsets whose cell pairs can hold a counted pair; half of them (with
+ * the zero offset) for auto counts.  D = -offset * cell width. */
+static int stencil_build(fcfcg_ctx *c, const grid_t *g, int isauto, int *sten,
+    float *stD, int *nsten, double *dmax) {
+  const fcfcg_bins *b = &c->bins;
+  const int box = (b->geometry == FCFCG_GEOM_BOX);
+  const double margin = 1 + 1e-6;
+  int r[3];
+  for (int d = 0; d < 3; d++) {
+    r[d] = (int) ceil(g->reach[d] * margin / g->cw[d]);
+    if (!box && r[d] > g->n[d] - 1) r[d] = g->n[d] - 1;
+    if (r[d] < 0) r[d] = 0;
+  }
+  int cnt = 0;
+  *dmax = 0;
+  for (int oz = -r[2]; oz <= r[2]; oz++)
+    for (int oy = -r[1]; oy <= r[1]; oy++)
+      for (int ox = -r[0]; ox <= r[0]; ox++) {
+        if (isauto) {
+          int sgn = oz ? oz : (oy ? oy : ox);
+          if (sgn < 0) continue;
+        }
+        const int o[3] = {ox, oy, oz};
+        double gap[3], far[3];
+        for (int d = 0; d < 3; d++) {
+          int a = abs(o[d]);
+          gap[d] = (a > 0 ? a - 1 : 0) * g->cw[d];
+          far[d] = (a + 1) * g->cw[d];
+        }
+        if (b->bintype == FCFCG_BIN_SPI && box) {
+          if (gap[2] > b->p.vmax * margin) continue;
+          if (gap[0] * gap[0] + gap[1] * gap[1] > b->s.vmax * margin) continue;
+          if (!b->s.min0 &&
+              far[0] * far[0] + far[1] * far[1] < b->s.vmin / margin)
+            continue;
+          if (!b->p.min0 && far[2] < b->p.vmin / margin) continue;
+        } else {
+          double g2 = gap[0] * gap[0] + gap[1] * gap[1] + gap[2] * gap[2];
+          if (g2 > g->reach3 * g->reach3 * margin) continue;
+          if (b->bintype != FCFCG_BIN_SPI && !b->s.min0) {
+            double f2 = far[0] * far[0] + far[1] * far[1] + far[2] * far[2];
+            if (f2 < b->s.vmin / margin) continue;
+          }
+        }
+        if (cnt >= FCFCG_MAX_STENCIL) {
+          set_err(c, "cell stencil too large");
+          return FCFCG_ERR_UNSUPPORTED;
+        }
+        sten[4 * cnt + 0] = ox;
+        sten[4 * cnt + 1] = oy;
+        sten[4 * cnt + 2] = oz;
+        sten[4 * cnt + 3] = 0;
+        for (int d = 0; d < 3; d++) {
+          double D = -o[d] * g->cw[d];
+          stD[4 * cnt + d] = (float) D;
+          if (fabs(D) > *dmax) *dmax = fabs(D);
+        }
+        stD[4 * cnt + 3] = 0;
+        cnt++;
+      }
+  *nsten = cnt;
+  return FCFCG_OK;
+}
+
+/* Sort a slot into the grid (skipped when already sorted for it). */
+static int slot_grid(fcfcg_ctx *c, slot_t *s, const grid_t *g) {
+  const size_t nc = (size_t) g->n[0] * g->n[1] * g->n[2];
+  if (s->grid_valid && s->ccap >= nc + 1 &&
+      !memcmp(s->gsig_n, g->n, sizeof g->n) &&
+      !memcmp(s->gsig_cw, g->cw, sizeof g->cw) &&
+      !memcmp(s->gsig_lo, g->lo, sizeof g->lo))
+    return FCFCG_OK;
+  const size_t n = s->n, m = n ? n : 1;
+  if (s->scap < m) {
+    void *p[] = {s->l4, s->wlo, s->sx, s->sy, s->sz, s->ss, s->sw, s->sid,
+                 s->cell_of};
+    for (size_t i = 0; i < sizeof p / sizeof p[0]; i++)
+      if (p[i]) cudaFree(p[i]);
+    CK(cudaMalloc((void **) &s->l4, sizeof(float) * 4 * m));
+    CK(cudaMalloc((void **) &s->wlo, sizeof(float) * m));
+    CK(cudaMalloc((void **) &s->sx, sizeof(double) * m));
+    CK(cudaMalloc((void **) &s->sy, sizeof(double) * m));
+    CK(cudaMalloc((void **) &s->sz, sizeof(double) * m));
+    CK(cudaMalloc((void **) &s->ss, sizeof(double) * m));
+    CK(cudaMalloc((void **) &s->sw, sizeof(double) * m));
+    CK(cudaMalloc((void **) &s->sid, sizeof(uint32_t) * m));
+    CK(cudaMalloc((void **) &s->cell_of, sizeof(uint32_t) * m));
+    s->scap = m;
+  }
+  if (s->ccap < nc + 1) {
+    if (s->cstart) cudaFree(s->cstart);
+    s->cstart = NULL;
+    CK(cudaMalloc((void **) &s->cstart, sizeof(uint32_t) * (nc + 1)));
+    s->ccap = nc + 1;
+  }
+  GROW(c->cfill, c->cfill_cap, sizeof(uint32_t) * (nc + 1));
+  size_t st = fcfcg_scan_tmp_len(nc + 1) + 16;
+  GROW(c->scan_tmp, c->scan_cap, sizeof(uint32_t) * st);
+  const int survey = (c->bins.geometry == FCFCG_GEOM_SURVEY);
+  CKK(fcfcg_k_grid(c->stream, n, s->x, s->y, s->z, survey ? s->s : NULL,
+                   s->w, s->has_w, s->wexp, g->n, g->cw, g->lo, s->cell_of,
+                   s->cstart, c->cfill, c->scan_tmp, st, s->l4, s->wlo,
+                   s->sx, s->sy, s->sz, survey ? s->ss : NULL, s->sw,
+                   s->sid));
+  memcpy(s->gsig_n, g->n, sizeof g->n);
+  memcpy(s->gsig_cw, g->cw, sizeof g->cw);
+  memcpy(s->gsig_lo, g->lo, sizeof g->lo);
+  s->grid_valid = 1;
+  return FCFCG_OK;
+}
+
+/* Rounding bounds of the FP32 path; returns 0 when the FP32 windows stay
+ * below half a table unit, i.e. the FP32 path applies. */
+static int fp32_bounds(const fcfcg_ctx *c, const grid_t *g, double dmax,
+    const slot_t *A, const slot_t *B, fcfcg_launch *L) {
+  const fcfcg_bins *b = &c->bins;
+  const int box = (b->geometry == FCFCG_GEOM_BOX);
+  const double u = ldexp(1.0, -24);
+  double hw = 0;
+  for (int d = 0; d < 3; d++) hw = fmax(hw, 0.5 * g->cw[d] * (1 + 1e-6));
+  const double R = g->reach3 * 1.01;
+  double xabs = fmax(A->xabs, B->xabs);
+  double sabs = fmax(A->s2abs, B->s2abs);
+  if (box) xabs = fmax(xabs, fmax(b->box[0], fmax(b->box[1], b->box[2])));
+  /* per-component error of an FP32 separation against the reference's FP64
+   * separation: rounding of both local coordinates, of D, of l_a + D, of the
+   * difference, and the reference's own FP64 rounding */
+  const double dc = 1.25 * u * (2 * hw + 2 * dmax + hw + R) +
+                    4 * ldexp(1.0, -53) * (2 * xabs + R) + 1e-12;
+  const double refs2 = box ? 0 : ldexp(1.0, -47) * sabs;
+  const double s3 = sqrt(3.0);
+  L->K2 = (float) ldexp(1.0, -20);
+  L->K1 = (float) (1.1 * 2 * s3 * dc);
+  if (b->bintype == FCFCG_BIN_SPI && box) L->K1 = (float) (1.1 * 2 * sqrt(2.0) * dc);
+  L->K0 = (float) (4 * dc * dc + refs2 + 1e-30);
+  double nmu = b->nmu;
+  L->fnmu = (float) nmu;
+  if (box) {
+    L->Q1 = (float) (1.25 * nmu * (dc + 0.5 * L->K1));
+    L->Q2 = (float) (1.25 * (0.5 * L->K2 + ldexp(1.0, -21)));
+    L->Q0 = 1e-6f;
+  } else {
+    L->Q1 = (float) (1.25 * nmu * (s3 * dc + 0.5 * L->K1));
+    L->Q2 = (float) (1.25 * (0.5 * L->K2 + ldexp(1.0, -20)));
+    L->Q0 = (float) (1.25 * nmu * ldexp(1.0, -20) + 1e-6);
+  }
+  double tiny = 1e6 * L->K0 * (nmu > 1 ? nmu : 1);
+  if (tiny < 1e-20) tiny = 1e-20;
+  L->tiny = (float) tiny;
+  /* worst windows at the top of the ranges */
+  double smax2 = b->s.vmax;
+  double Es = L->K2 * smax2 + L->K1 * sqrt(smax2) + L->K0;
+  double Ep = 0;
+  if (b->bintype == FCFCG_BIN_SPI) {
+    if (box) {
+      L->P0 = (float) (1.25 * dc);
+      L->P1 = L->P2 = 0;
+      Ep = L->P0;
+      L->p_lim = (float) (b->p.vmax + Ep + 1e-6 * (1 + b->p.vmax));
+      L->s_lim = (float) (smax2 + Es + 1e-6 * (1 + smax2));
+    } else {
+      double r2 = b->s.vmax + b->p.vmax;
+      L->P0 = (float) (refs2 + 1e-12);
+      L->P1 = (float) (1.25 * 2 * s3 * dc);
+      L->P2 = (float) (1.25 * (ldexp(1.0, -19) + ldexp(1.0, -21)));
+      Ep = L->P2 * r2 + L->P1 * sqrt(r2) + L->P0;
+      Es = L->K2 * r2 + L->K1 * sqrt(r2) + L->K0 + Ep;
+      L->s_lim = (float) (r2 + Es + 1e-6 * (1 + r2));
+      L->p_lim = 0;
+    }
+  } else {
+    L->s_lim = (float) (smax2 + Es + 1e-6 * (1 + smax2));
+  }
+  if (!(Es < 0.45) || !(Ep < 0.45)) return -1;
+  if (b->s.nbin > FCFCG_FTAB_MAXBIN || !b->s.ftab) return -1;
+  if (b->bintype == FCFCG_BIN_SPI &&
+      (b->p.nbin > FCFCG_FTAB_MAXBIN || !b->p.ftab))
+    return -1;
+  /* the FP32 tables must cover every value below the limits */
+  if ((double) L->s_lim >= (double) (b->s.foff + b->s.nftab - 1)) return -1;
+  if (b->bintype == FCFCG_BIN_SPI && box &&
+      (double) L->p_lim >= (double) (b->p.foff + b->p.nftab - 1))
+    return -1;
+  return 0;
+}
+
+static int ensure_pinned(fcfcg_ctx *c, size_t bytes) {
+  if (c->h_pinned_cap >= bytes) return FCFCG_OK;
+  if (c->h_pinned) cudaFreeHost(c->h_pinned);
+  c->h_pinned = NULL;
+  c->h_pinned_cap = 0;
+  CK(cudaMallocHost(&c->h_pinned, bytes));
+  c->h_pinned_cap = bytes;
+  return FCFCG_OK;
+}
+
+int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
+    int precision, int64_t *icnt, double *wcnt) {
+  if (!c || c->host_only) return FCFCG_ERR_ARG;
+  if (sa < 0 || sa >= FCFCG_MAX_SLOT || sb < 0 || sb >= FCFCG_MAX_SLOT) {
+    set_err(c, "slot out of range");
+    return FCFCG_ERR_ARG;
+  }
+  if (isauto && sa != sb) {
+    set_err(c, "auto counts need the same slot twice");
+    return FCFCG_ERR_ARG;
+  }
+  if (precision != FCFCG_PREC_FP32_RECHECK && precision != FCFCG_PREC_FP64)
+    return FCFCG_ERR_ARG;
+  if ((withwt && !wcnt) || (!withwt && !icnt)) return FCFCG_ERR_ARG;
+  CK(cudaSetDevice(c->device));
+  const fcfcg_bins *b = &c->bins;
+  slot_t *A = c->slot + sa, *B = c->slot + sb;
+  if (!A->x || !B->x) {
+    set_err(c, "catalogue slot not loaded");
+    return FCFCG_ERR_ARG;
+  }
+  memset(&c->stats, 0, sizeof c->stats);
+  if (A->n == 0 || B->n == 0) {
+    if (icnt) memset(icnt, 0, sizeof(int64_t) * b->ntot);
+    if (wcnt) memset(wcnt, 0, sizeof(double) * b->ntot);
+    return FCFCG_OK;
+  }
+  CK(cudaEventRecord(c->ev[0], c->stream));
+  grid_t g;
+  memset(&g, 0, sizeof g);
+  int rc = grid_setup(c, &g, A, B);
+  if (rc) return rc;
+  int *sten = c->sten;
+  float *stD = c->stD;
+  int nsten = 0;
+  double dmax = 0;
+  if ((rc = stencil_build(c, &g, isauto, sten, stD, &nsten, &dmax))) return rc;
+  if ((rc = slot_grid(c, A, &g))) return rc;
+  if (B != A && (rc = slot_grid(c, B, &g))) return rc;
+  const uint32_t ncell = (uint32_t) ((size_t) g.n[0] * g.n[1] * g.n[2]);
+  GROW(c->cchunk, c->cchunk_cap, sizeof(uint32_t) * 2 * ((size_t) ncell + 1));
+  size_t st = fcfcg_scan_tmp_len(ncell + 1) + 16;
+  GROW(c->scan_tmp, c->scan_cap, sizeof(uint32_t) * st);
+  size_t maxchunk = A->n / FCFCG_CHUNK + ncell + 1;
+  GROW(c->chunks, c->chunk_cap, sizeof(uint32_t) * 4 * maxchunk);
+  rc = upload(c, (void **) &c->d_sten, sten, sizeof(int) * 4 * nsten);
+  if (rc) return rc;
+  rc = upload(c, (void **) &c->d_stenD, stD, sizeof(float) * 4 * nsten);
+  if (rc) return rc;
+  uint32_t nchunk = 0;
+  CKK(fcfcg_k_chunks(c->stream, A->cstart, ncell, c->cchunk, c->scan_tmp, st,
+                     c->chunks, &nchunk));
+  CK(cudaEventRecord(c->ev[1], c->stream));
+
+  fcfcg_launch L;
+  memset(&L, 0, sizeof L);
+  L.geometry = b->geometry;
+  L.bintype = b->bintype;
+  L.isauto = isauto;
+  L.withwt = withwt;
+  for (int d = 0; d < 3; d++) {
+    L.ncell[d] = g.n[d];
+    L.cw[d] = g.cw[d];
+    L.lo[d] = g.lo[d];
+    L.box[d] = b->box[d];
+    L.cwf[d] = (float) g.cw[d];
+    L.lof[d] = (float) g.lo[d];
+  }
+  L.nsten = nsten;
+  L.sten = c->d_sten;
+  L.stenD = c->d_stenD;
+  CK(cudaStreamSynchronize(c->stream));
+  L.nchunk = nchunk;
+  L.chunks = c->chunks;
+  L.chunk_head = c->d_head;
+  const slot_t *S[2] = {A, B};
+  fcfcg_dcat *D[2] = {&L.A, &L.B};
+  for (int q = 0; q < 2; q++) {
+    D[q]->l4 = S[q]->l4;
+    D[q]->wlo = S[q]->wlo;
+    D[q]->x = S[q]->sx;
+    D[q]->y = S[q]->sy;
+    D[q]->z = S[q]->sz;
+    D[q]->s = S[q]->ss;
+    D[q]->w = S[q]->sw;
+    D[q]->id = S[q]->sid;
+    D[q]->cstart = S[q]->cstart;
+    D[q]->wexp = S[q]->wexp;
+  }
+  L.ns = b->ns;
+  L.nmu = b->nmu;
+  L.np = b->np;
+  L.ntot = b->ntot;
+  L.rs = c->d_rs;
+  L.rp = c->d_rp;
+  L.rsoff = b->s.roff;
+  L.rpoff = b->p.roff;
+  L.nrs = b->s.nrtab;
+  L.nrp = b->p.nrtab;
+  L.tabtype = b->s.tabtype;
+  L.s2edge = c->d_s2edge;
+  L.pedge = c->d_pedge;
+  L.s2min = b->s.vmin;
+  L.s2max = b->s.vmax;
+  L.smin0 = b->s.min0;
+  if (b->bintype == FCFCG_BIN_SPI) {
+    L.pmin = b->p.vmin;
+    L.pmax = b->p.vmax;
+    L.pmin0 = b->p.min0;
+  }
+  L.fixF = 42;
+  L.gcnt = c->d_cnt;
+  L.gwt = c->d_wt;
+  L.gwd = c->d_wd;
+  L.queue = c->d_queue;
+  L.qcount = c->d_qcount;
+  L.qcap = (uint32_t) c->qcap;
+  L.stats = c->d_stats;
+  int prec = precision;
+  if (prec == FCFCG_PREC_FP32_RECHECK && fp32_bounds(c, &g, dmax, A, B, &L))
+    prec = FCFCG_PREC_FP64;
+  if (prec == FCFCG_PREC_FP32_RECHECK) {
+    L.fs = c->d_fs;
+    L.nfs = (int) b->s.nftab;
+    L.fsoff = (int) b->s.foff;
+    if (b->bintype == FCFCG_BIN_SPI) {
+      L.fp = c->d_fp;
+      L.nfp = (int) b->p.nftab;
+      L.fpoff = (int) b->p.foff;
+    }
+  }
+  size_t tabbytes = (prec == FCFCG_PREC_FP32_RECHECK)
+      ? (((size_t) (L.nfs + L.nfp) * 2 + 15) & ~(size_t) 15) : 0;
+  size_t hbytes = (size_t) b->ntot * (withwt ? 8 : 4);
+  L.hist_smem = (tabbytes + hbytes <= 160 * 1024);
+  if (tabbytes > 160 * 1024) prec = FCFCG_PREC_FP64;
+
+  CK(cudaMemsetAsync(c->d_cnt, 0, sizeof(unsigned long long) * b->ntot,
+                     c->stream));
+  CK(cudaMemsetAsync(c->d_wt, 0, sizeof(unsigned long long) * 2 * b->ntot,
+                     c->stream));
+  CK(cudaMemsetAsync(c->d_wd, 0, sizeof(double) * b->ntot, c->stream));
+  CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * 4, c->stream));
+  CK(cudaMemsetAsync(c->d_head, 0, sizeof(uint32_t) * 2, c->stream));
+  CK(cudaEventRecord(c->ev[2], c->stream));
+  size_t smem = 0;
+  CKK(fcfcg_k_count(c->stream, &L, prec, c->nsm, &smem));
+  CK(cudaEventRecord(c->ev[3], c->stream));
+  uint32_t nq = 0;
+  if (prec == FCFCG_PREC_FP32_RECHECK) {
+    CK(cudaMemcpyAsync(&nq, c->d_qcount, sizeof nq, cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (nq > c->qcap) nq = (uint32_t) c->qcap;
+    CKK(fcfcg_k_recheck(c->stream, &L, nq));
+  }
+  CK(cudaEventRecord(c->ev[4], c->stream));
+  /* results */
+  size_t rbytes = sizeof(unsigned long long) * 2 * b->ntot + 64;
+  if ((rc = ensure_pinned(c, rbytes))) return rc;
+  unsigned long long *hres = (unsigned long long *) c->h_pinned;
+  unsigned long long hstats[4];
+  if (withwt && prec == FCFCG_PREC_FP64)
+    CK(cudaMemcpyAsync(hres, c->d_wd, sizeof(double) * b->ntot,
+                       cudaMemcpyDeviceToHost, c->stream));
+  else if (withwt)
+    CK(cudaMemcpyAsync(hres, c->d_wt, sizeof(unsigned long long) * 2 * b->ntot,
+                       cudaMemcpyDeviceToHost, c->stream));
+  else
+    CK(cudaMemcpyAsync(hres, c->d_cnt, sizeof(unsigned long long) * b->ntot,
+                       cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(hstats, c->d_stats, sizeof hstats, cudaMemcpyDeviceToHost,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  if (withwt && prec == FCFCG_PREC_FP64) {
+    memcpy(wcnt, hres, sizeof(double) * b->ntot);
+  } else if (withwt) {
+    const int ex = A->wexp + B->wexp - L.fixF;
+    for (long i = 0; i < b->ntot; i++) {
+      __int128 v = (__int128) (((unsigned __int128) hres[2 * i + 1] << 64) |
+                               (unsigned __int128) hres[2 * i]);
+      wcnt[i] = ldexp((double) v, ex);
+    }
+  } else {
+    for (long i = 0; i < b->ntot; i++) icnt[i] = (int64_t) hres[i];
+  }
+  fcfcg_stats *o = &c->stats;
+  o->candidates = hstats[0];
+  o->in_range = hstats[1];
+  o->rechecked = hstats[2];
+  o->recheck_inline = hstats[3];
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+  o->ms_grid = ms;
+  cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+  o->ms_count = ms;
+  cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]);
+  o->ms_recheck = ms;
+  cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]);
+  o->ms_total = ms;
+  o->cells_per_smax = g.k;
+  for (int d = 0; d < 3; d++) o->ncell[d] = g.n[d];
+  o->nstencil = nsten;
+  o->nchunks = nchunk;
+  o->precision_used = prec;
+  (void) smem;
+  return FCFCG_OK;
+}
+
+const fcfcg_bins *fcfcg_ctx_bins(const fcfcg_ctx *c) {
+  return (c && c->bins.sbin_raw) ? &c->bins : NULL;
+}
+
+const double *fcfcg_ctx_box_raw(const fcfcg_ctx *c) {
+  return c ? c->bins.box_raw : NULL;
+}
+
+int fcfcg_stats_get(const fcfcg_ctx *c, fcfcg_stats *out) {
+  if (!c || !out) return FCFCG_ERR_ARG;
+  *out = c->stats;
+  return FCFCG_OK;
+}

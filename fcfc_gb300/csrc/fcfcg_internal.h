@@ -1,0 +1,151 @@
+/*
+ * fcfcg_internal.h -- structures shared by the C host layer and the CUDA
+ * kernels of the pair-counting engine.  Plain C, no CUDA types.
+ */
+#ifndef FCFCG_INTERNAL_H
+#define FCFCG_INTERNAL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/fcfcg.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FCFCG_MAX_SLOT 8
+#define FCFCG_CHUNK 32            /* points of one cell a warp holds */
+#define FCFCG_MAX_STENCIL 4096
+#define FCFCG_FTAB_BIN_MASK 0x1FFFu
+#define FCFCG_FTAB_LO 0x2000u     /* an edge lies in [i - 1/2, i] */
+#define FCFCG_FTAB_HI 0x4000u     /* an edge lies in [i + 1, i + 3/2] */
+#define FCFCG_FTAB_CX 0x8000u     /* an edge lies strictly inside (i, i + 1) */
+#define FCFCG_FTAB_MAXBIN 8190    /* largest bin index an FP32 table holds */
+
+/*
+ * One binned quantity (s^2, s_perp^2, pi or pi^2), as FCFC looks it up:
+ * reference table rtab over (int) v - roff with FCFC's integer / hybrid
+ * semantics, and the FP32 edge-window table ftab over (int) v - foff.
+ */
+typedef struct {
+  int nbin;
+  int tabtype;
+  double *edge;          /* nbin + 1 rescaled edges (host) */
+  uint16_t *rtab;        /* reference table (host) */
+  long nrtab, roff;
+  uint16_t *ftab;        /* FP32 window table (host) */
+  long nftab, foff;
+  double vmin, vmax;     /* edge[0], edge[nbin] */
+  int min0;              /* edge[0] == 0: no lower range check (smin0) */
+} fcfcg_axis;
+
+typedef struct {
+  int geometry, bintype;
+  int ns, nmu, np;
+  long ntot;
+  double rescale;
+  double box[3];         /* rescaled */
+  double box_raw[3];     /* as configured */
+  double *sbin_raw, *pbin_raw;
+  fcfcg_axis s;          /* s^2 (or s_perp^2) */
+  fcfcg_axis p;          /* pi (box) or pi^2 (survey) */
+} fcfcg_bins;
+
+int fcfcg_bins_setup(const fcfcg_binning *cfg, fcfcg_bins *b, char *err,
+    size_t errlen);
+void fcfcg_bins_release(fcfcg_bins *b);
+/* Build the FP32 window table of an axis (ftab / foff / nftab). */
+int fcfcg_axis_ftab(fcfcg_axis *a, int vmin_is_floor);
+/* Accessors of the opaque context used by the post-processing code. */
+const fcfcg_bins *fcfcg_ctx_bins(const fcfcg_ctx *c);
+const double *fcfcg_ctx_box_raw(const fcfcg_ctx *c);
+
+/* ------------------------------------------------------------------------ */
+/* Launch parameters of the counting kernels (passed by value).             */
+
+typedef struct {
+  /* sorted catalogue on the device */
+  const float *l4;       /* float4 per point: local x, y, z, scaled w_hi */
+  const float *wlo;      /* scaled w_lo */
+  const double *x, *y, *z, *s, *w;   /* rescaled FP64, |x|^2, weight */
+  const uint32_t *id;    /* input index */
+  const uint32_t *cstart;/* ncell + 1 */
+  int wexp;              /* weights scaled by 2^-wexp */
+} fcfcg_dcat;
+
+typedef struct {
+  int geometry, bintype, isauto, withwt;
+  int ncell[3];
+  double cw[3], lo[3], box[3];
+  float cwf[3], lof[3];
+  /* stencil: nsten entries of int4 (ox, oy, oz, 0) and float4 (-o * cw) */
+  int nsten;
+  const int *sten;
+  const float *stenD;
+  /* chunks: uint4 (cell, first sorted index, count, 0) */
+  uint32_t nchunk;
+  const uint32_t *chunks;
+  uint32_t *chunk_head;
+  fcfcg_dcat A, B;
+  /* bins */
+  int ns, nmu, np;
+  long ntot;
+  /* FP32 tables (copied to shared memory) */
+  const uint16_t *fs, *fp;
+  int nfs, nfp, fsoff, fpoff;
+  float s_lim, p_lim;          /* values at/above: out of range for sure */
+  float K0, K1, K2;            /* E(s^2) = K2 s^2 + K1 s + K0 */
+  float P0, P1, P2;            /* E(pi) (box) or E(pi^2) (survey) */
+  float Q0, Q1, Q2;            /* E(q), q = nmu mu: Q1 / s + Q2 q + Q0 */
+  float tiny;                  /* s^2 below: always recheck */
+  float fnmu;
+  /* FP64 reference binning */
+  const uint16_t *rs, *rp;
+  long rsoff, rpoff, nrs, nrp;
+  int tabtype;
+  const double *s2edge, *pedge;
+  double s2min, s2max, pmin, pmax;
+  int smin0, pmin0;
+  /* weights: fixed point with F fractional bits */
+  int fixF;
+  /* outputs */
+  unsigned long long *gcnt;    /* ntot counts */
+  unsigned long long *gwt;     /* 2 * ntot: lo, hi words of int128 */
+  double *gwd;                 /* ntot FP64 sums (FP64 path) */
+  /* recheck queue: uint4 (a, b, code, 0) */
+  uint32_t *queue;
+  uint32_t *qcount;
+  uint32_t qcap;
+  unsigned long long *stats;   /* [0] candidates [1] in-range [2] recheck
+                                  [3] inline rechecks */
+  int hist_smem;               /* histogram in shared memory */
+} fcfcg_launch;
+
+/* Launchers implemented in the .cu files; return 0 or a CUDA error code. */
+int fcfcg_k_prep(void *stream, size_t n, const double *x, const double *y,
+    const double *z, const double *w, double rescale, int survey,
+    double *ox, double *oy, double *oz, double *os, double *ow,
+    unsigned long long *wmax_bits);
+int fcfcg_k_grid(void *stream, size_t n, const double *x, const double *y,
+    const double *z, const double *s, const double *w, int has_w, int wexp,
+    const int ncell[3], const double cw[3], const double lo[3],
+    uint32_t *cell_of, uint32_t *cstart, uint32_t *cfill, uint32_t *scan_tmp,
+    size_t scan_tmp_len, float *l4, float *wlo, double *sx, double *sy,
+    double *sz, double *ss, double *sw, uint32_t *sid);
+int fcfcg_k_chunks(void *stream, const uint32_t *cstart, uint32_t ncell,
+    uint32_t *cchunk, uint32_t *scan_tmp, size_t scan_tmp_len,
+    uint32_t *chunks, uint32_t *nchunk_out);
+int fcfcg_k_bbox(void *stream, size_t n, const double *x, const double *y,
+    const double *z, unsigned long long *bits6);
+int fcfcg_k_count(void *stream, const fcfcg_launch *L, int precision,
+    int nsm, size_t *smem_used);
+int fcfcg_k_recheck(void *stream, const fcfcg_launch *L, uint32_t nq);
+int fcfcg_k_flush_count(void *stream, const fcfcg_launch *L);
+size_t fcfcg_scan_tmp_len(size_t n);
+const char *fcfcg_cuda_errstr(int code);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,359 @@
+/*
+ * prep.cu -- catalogue preparation on the device: rescaling (as FCFC's
+ * tree_create does, src/fcfc/2pt_box/build_tree.c:121-131), |x|^2 for
+ * surveys (src/fcfc/2pt/build_tree.c:35-133), weight range, bounding box,
+ * and the cell grid: a counting sort of the points into cells, stored as
+ * SoA FP64 copies plus one float4 per point (FP32 offsets from the cell
+ * centre and the scaled high part of the weight) for the FP32 kernels.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "fcfcg_internal.h"
+
+#define PREP_THREADS 256
+#define SCAN_THREADS 1024
+#define SCAN_ITEMS 4
+#define SCAN_TILE (SCAN_THREADS * SCAN_ITEMS)
+
+static int grid_for(size_t n, int threads) {
+  size_t b = (n + threads - 1) / threads;
+  if (b > 152 * 32) b = 152 * 32;
+  if (b < 1) b = 1;
+  return (int) b;
+}
+
+/* Order-preserving map of a double to an unsigned key. */
+__device__ __forceinline__ unsigned long long dkey(double v) {
+  unsigned long long b = (unsigned long long) __double_as_longlong(v);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__global__ void k_prep(size_t n, const double *__restrict__ x,
+    const double *__restrict__ y, const double *__restrict__ z,
+    const double *__restrict__ w, double rescale, int survey,
+    double *__restrict__ ox, double *__restrict__ oy, double *__restrict__ oz,
+    double *__restrict__ os, double *__restrict__ ow,
+    unsigned long long *wmax_bits) {
+  unsigned long long wm = 0;
+  for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n;
+       i += (size_t) gridDim.x * blockDim.x) {
+    double a = x[i], b = y[i], c = z[i];
+    if (rescale != 1) {
+      a = __dmul_rn(a, rescale);
+      b = __dmul_rn(b, rescale);
+      c = __dmul_rn(c, rescale);
+    }
+    ox[i] = a;
+    oy[i] = b;
+    oz[i] = c;
+    if (survey)
+      os[i] = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)),
+                        __dmul_rn(c, c));
+    if (w) {
+      double v = w[i];
+      ow[i] = v;
+      unsigned long long bits =
+          (unsigned long long) __double_as_longlong(fabs(v));
+      wm = bits > wm ? bits : wm;
+    }
+  }
+  if (w) {
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long t = __shfl_xor_sync(0xffffffffu, wm, o);
+      wm = t > wm ? t : wm;
+    }
+    if ((threadIdx.x & 31) == 0 && wm) atomicMax(wmax_bits, wm);
+  }
+}
+
+extern "C" int fcfcg_k_prep(void *stream, size_t n, const double *x,
+    const double *y, const double *z, const double *w, double rescale,
+    int survey, double *ox, double *oy, double *oz, double *os, double *ow,
+    unsigned long long *wmax_bits) {
+  if (!n) return 0;
+  k_prep<<<grid_for(n, PREP_THREADS), PREP_THREADS, 0,
+           (cudaStream_t) stream>>>(n, x, y, z, w, rescale, survey, ox, oy,
+                                    oz, os, ow, wmax_bits);
+  return (int) cudaGetLastError();
+}
+
+__global__ void k_bbox(size_t n, const double *__restrict__ x,
+    const double *__restrict__ y, const double *__restrict__ z,
+    unsigned long long *bits6) {
+  unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0, 0, 0};
+  const double *p[3] = {x, y, z};
+  for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n;
+       i += (size_t) gridDim.x * blockDim.x) {
+    for (int k = 0; k < 3; k++) {
+      unsigned long long v = dkey(p[k][i]);
+      lo[k] = v < lo[k] ? v : lo[k];
+      hi[k] = v > hi[k] ? v : hi[k];
+    }
+  }
+  for (int k = 0; k < 3; k++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long a = __shfl_xor_sync(0xffffffffu, lo[k], o);
+      unsigned long long b = __shfl_xor_sync(0xffffffffu, hi[k], o);
+      lo[k] = a < lo[k] ? a : lo[k];
+      hi[k] = b > hi[k] ? b : hi[k];
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(bits6 + k, lo[k]);
+      atomicMax(bits6 + 3 + k, hi[k]);
+    }
+  }
+}
+
+extern "C" int fcfcg_k_bbox(void *stream, size_t n, const double *x,
+    const double *y, const double *z, unsigned long long *bits6) {
+  if (!n) return 0;
+  k_bbox<<<grid_for(n, PREP_THREADS), PREP_THREADS, 0,
+           (cudaStream_t) stream>>>(n, x, y, z, bits6);
+  return (int) cudaGetLastError();
+}
+
+/* ------------------------------------------------------------------------ */
+/* Exclusive scan of uint32 (n + 1 outputs: out[n] = total).               */
+
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v,
+    uint32_t *sh_warp, uint32_t *total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  uint32_t inc = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
+  }
+  if (lane == 31) sh_warp[wid] = inc;
+  __syncthreads();
+  if (wid == 0) {
+    uint32_t s = (lane < (int) (blockDim.x >> 5)) ? sh_warp[lane] : 0;
+    uint32_t si = s;
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t t = __shfl_up_sync(0xffffffffu, si, o);
+      if (lane >= o) si += t;
+    }
+    sh_warp[lane] = si - s;
+    if (lane == 31) *total = si;
+  }
+  __syncthreads();
+  uint32_t r = sh_warp[wid] + inc - v;
+  __syncthreads();
+  return r;
+}
+
+__global__ void k_scan_tiles(const uint32_t *__restrict__ in, size_t n,
+    uint32_t *__restrict__ tile_sum) {
+  __shared__ uint32_t shw[32];
+  __shared__ uint32_t tot;
+  size_t base = (size_t) blockIdx.x * SCAN_TILE;
+  uint32_t s = 0;
+  for (int k = 0; k < SCAN_ITEMS; k++) {
+    size_t i = base + (size_t) k * SCAN_THREADS + threadIdx.x;
+    if (i < n) s += in[i];
+  }
+  block_excl_scan(s, shw, &tot);
+  if (threadIdx.x == 0) tile_sum[blockIdx.x] = tot;
+}
+
+__global__ void k_scan_sums(uint32_t *__restrict__ tile_sum, size_t ntile) {
+  __shared__ uint32_t shw[32];
+  __shared__ uint32_t tot;
+  uint32_t carry = 0;
+  for (size_t b = 0; b < ntile; b += SCAN_THREADS) {
+    size_t i = b + threadIdx.x;
+    uint32_t v = (i < ntile) ? tile_sum[i] : 0;
+    uint32_t e = block_excl_scan(v, shw, &tot);
+    if (i < ntile) tile_sum[i] = e + carry;
+    carry += tot;
+    __syncthreads();
+  }
+}
+
+__global__ void k_scan_apply(const uint32_t *__restrict__ in, size_t n,
+    const uint32_t *__restrict__ tile_sum, uint32_t *__restrict__ out) {
+  __shared__ uint32_t shw[32];
+  __shared__ uint32_t tot;
+  size_t base = (size_t) blockIdx.x * SCAN_TILE;
+  /* each thread owns SCAN_ITEMS consecutive items */
+  uint32_t v[SCAN_ITEMS];
+  uint32_t s = 0;
+  for (int k = 0; k < SCAN_ITEMS; k++) {
+    size_t i = base + (size_t) threadIdx.x * SCAN_ITEMS + k;
+    v[k] = (i < n) ? in[i] : 0;
+    s += v[k];
+  }
+  uint32_t e = block_excl_scan(s, shw, &tot) + tile_sum[blockIdx.x];
+  for (int k = 0; k < SCAN_ITEMS; k++) {
+    size_t i = base + (size_t) threadIdx.x * SCAN_ITEMS + k;
+    if (i < n) out[i] = e;
+    e += v[k];
+    if (i == n - 1) out[n] = e;
+  }
+}
+
+extern "C" size_t fcfcg_scan_tmp_len(size_t n) {
+  return (n + SCAN_TILE - 1) / SCAN_TILE + 1;
+}
+
+/* out[0..n] = exclusive scan of in[0..n-1], out[n] = total. */
+static int scan_u32(cudaStream_t s, const uint32_t *in, size_t n,
+    uint32_t *out, uint32_t *tmp) {
+  if (n == 0) {
+    return (int) cudaMemsetAsync(out, 0, sizeof(uint32_t), s);
+  }
+  size_t ntile = (n + SCAN_TILE - 1) / SCAN_TILE;
+  k_scan_tiles<<<(unsigned) ntile, SCAN_THREADS, 0, s>>>(in, n, tmp);
+  k_scan_sums<<<1, SCAN_THREADS, 0, s>>>(tmp, ntile);
+  k_scan_apply<<<(unsigned) ntile, SCAN_THREADS, 0, s>>>(in, n, tmp, out);
+  return (int) cudaGetLastError();
+}
+
+/* ------------------------------------------------------------------------ */
+/* Cell grid.                                                               */
+
+__device__ __forceinline__ int cell_axis(double v, double lo, double cw,
+    int n) {
+  double t = floor((v - lo) / cw);
+  int c = (t < 0) ? 0 : (t >= n ? n - 1 : (int) t);
+  return c;
+}
+
+__global__ void k_cell(size_t n, const double *__restrict__ x,
+    const double *__restrict__ y, const double *__restrict__ z, int nx,
+    int ny, int nz, double cwx, double cwy, double cwz, double lox,
+    double loy, double loz, uint32_t *__restrict__ cell_of,
+    uint32_t *__restrict__ count) {
+  for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n;
+       i += (size_t) gridDim.x * blockDim.x) {
+    int cx = cell_axis(x[i], lox, cwx, nx);
+    int cy = cell_axis(y[i], loy, cwy, ny);
+    int cz = cell_axis(z[i], loz, cwz, nz);
+    uint32_t c = ((uint32_t) cz * ny + cy) * nx + cx;
+    cell_of[i] = c;
+    atomicAdd(count + c, 1u);
+  }
+}
+
+__global__ void k_scatter(size_t n, const double *__restrict__ x,
+    const double *__restrict__ y, const double *__restrict__ z,
+    const double *__restrict__ s, const double *__restrict__ w, int has_w,
+    int wexp, int nx, int ny, double cwx, double cwy, double cwz, double lox,
+    double loy, double loz, const uint32_t *__restrict__ cell_of,
+    const uint32_t *__restrict__ cstart, uint32_t *__restrict__ cfill,
+    float4 *__restrict__ l4, float *__restrict__ wlo, double *__restrict__ sx,
+    double *__restrict__ sy, double *__restrict__ sz, double *__restrict__ ss,
+    double *__restrict__ sw, uint32_t *__restrict__ sid) {
+  for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n;
+       i += (size_t) gridDim.x * blockDim.x) {
+    uint32_t c = cell_of[i];
+    uint32_t pos = cstart[c] + atomicAdd(cfill + c, 1u);
+    int cx = (int) (c % (uint32_t) nx);
+    int cy = (int) ((c / (uint32_t) nx) % (uint32_t) ny);
+    int cz = (int) (c / ((uint32_t) nx * (uint32_t) ny));
+    double a = x[i], b = y[i], d = z[i];
+    double ccx = lox + (cx + 0.5) * cwx;
+    double ccy = loy + (cy + 0.5) * cwy;
+    double ccz = loz + (cz + 0.5) * cwz;
+    double wv = has_w ? w[i] : 1.0;
+    double ws = ldexp(wv, -wexp);
+    float whi = (float) ws;
+    float4 v;
+    v.x = (float) (a - ccx);
+    v.y = (float) (b - ccy);
+    v.z = (float) (d - ccz);
+    v.w = whi;
+    l4[pos] = v;
+    wlo[pos] = (float) (ws - (double) whi);
+    sx[pos] = a;
+    sy[pos] = b;
+    sz[pos] = d;
+    if (ss) ss[pos] = s[i];
+    sw[pos] = wv;
+    sid[pos] = (uint32_t) i;
+  }
+}
+
+extern "C" int fcfcg_k_grid(void *stream, size_t n, const double *x,
+    const double *y, const double *z, const double *s, const double *w,
+    int has_w, int wexp, const int ncell[3], const double cw[3],
+    const double lo[3], uint32_t *cell_of, uint32_t *cstart, uint32_t *cfill,
+    uint32_t *scan_tmp, size_t scan_tmp_len, float *l4, float *wlo,
+    double *sx, double *sy, double *sz, double *ss, double *sw,
+    uint32_t *sid) {
+  cudaStream_t st = (cudaStream_t) stream;
+  size_t nc = (size_t) ncell[0] * ncell[1] * ncell[2];
+  (void) scan_tmp_len;
+  cudaError_t e = cudaMemsetAsync(cfill, 0, sizeof(uint32_t) * nc, st);
+  if (e) return (int) e;
+  if (n) {
+    k_cell<<<grid_for(n, PREP_THREADS), PREP_THREADS, 0, st>>>(
+        n, x, y, z, ncell[0], ncell[1], ncell[2], cw[0], cw[1], cw[2], lo[0],
+        lo[1], lo[2], cell_of, cfill);
+    if ((e = cudaGetLastError())) return (int) e;
+  }
+  int r = scan_u32(st, cfill, nc, cstart, scan_tmp);
+  if (r) return r;
+  if ((e = cudaMemsetAsync(cfill, 0, sizeof(uint32_t) * nc, st))) return (int) e;
+  if (n) {
+    k_scatter<<<grid_for(n, PREP_THREADS), PREP_THREADS, 0, st>>>(
+        n, x, y, z, s, w, has_w, wexp, ncell[0], ncell[1], cw[0], cw[1],
+        cw[2], lo[0], lo[1], lo[2], cell_of, cstart, cfill, (float4 *) l4,
+        wlo, sx, sy, sz, ss, sw, sid);
+    if ((e = cudaGetLastError())) return (int) e;
+  }
+  return 0;
+}
+
+/* Work chunks: every cell is cut into pieces of at most FCFCG_CHUNK points. */
+__global__ void k_chunk_count(const uint32_t *__restrict__ cstart,
+    uint32_t ncell, uint32_t *__restrict__ cchunk) {
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
+       c += gridDim.x * blockDim.x) {
+    uint32_t m = cstart[c + 1] - cstart[c];
+    cchunk[c] = (m + FCFCG_CHUNK - 1) / FCFCG_CHUNK;
+  }
+}
+
+__global__ void k_chunk_emit(const uint32_t *__restrict__ cstart,
+    uint32_t ncell, const uint32_t *__restrict__ coff,
+    uint4 *__restrict__ chunks) {
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
+       c += gridDim.x * blockDim.x) {
+    uint32_t a = cstart[c], m = cstart[c + 1] - a;
+    uint32_t k = coff[c];
+    for (uint32_t q = 0; q < m; q += FCFCG_CHUNK) {
+      uint32_t len = (m - q < FCFCG_CHUNK) ? m - q : FCFCG_CHUNK;
+      chunks[k++] = make_uint4(c, a + q, len, 0);
+    }
+  }
+}
+
+extern "C" int fcfcg_k_chunks(void *stream, const uint32_t *cstart,
+    uint32_t ncell, uint32_t *cchunk, uint32_t *scan_tmp,
+    size_t scan_tmp_len, uint32_t *chunks, uint32_t *nchunk_out) {
+  cudaStream_t st = (cudaStream_t) stream;
+  (void) scan_tmp_len;
+  k_chunk_count<<<grid_for(ncell, PREP_THREADS), PREP_THREADS, 0, st>>>(
+      cstart, ncell, cchunk);
+  cudaError_t e = cudaGetLastError();
+  if (e) return (int) e;
+  /* cchunk holds ncell + 1 slots: scan in place via the offset array */
+  uint32_t *coff = cchunk + ncell + 1;
+  int r = scan_u32(st, cchunk, ncell, coff, scan_tmp);
+  if (r) return r;
+  if (chunks) {
+    k_chunk_emit<<<grid_for(ncell, PREP_THREADS), PREP_THREADS, 0, st>>>(
+        cstart, ncell, coff, (uint4 *) chunks);
+    if ((e = cudaGetLastError())) return (int) e;
+  }
+  if (nchunk_out)
+    if ((e = cudaMemcpyAsync(nchunk_out, coff + ncell, sizeof(uint32_t),
+                             cudaMemcpyDeviceToHost, st)))
+      return (int) e;
+  return 0;
+}
+
+extern "C" const char *fcfcg_cuda_errstr(int code) {
+  return cudaGetErrorString((cudaError_t) code);
+}

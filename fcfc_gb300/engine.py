@@ -1,0 +1,230 @@
+"""Python front end of the GB300 pair-counting engine.
+
+``PairCounter`` holds one binning set-up (what FCFC's cf_setup builds,
+src/fcfc/2pt_box/setup_cf.c:547-848) on one GPU, takes catalogues, and counts
+pairs through the C ABI exactly where FCFC calls
+``count_pairs(tree1, tree2, cf, cnt, isauto, withwt)``
+(src/fcfc/2pt_box/count_func.h:54-59): auto counts come back undoubled, as
+count_pairs leaves them, and ``normalise`` applies eval_pairs' doubling and
+norms (src/fcfc/2pt_box/eval_cf.c:117-167).
+
+There is no CPU path: every count runs in libfcfcg.so on the device, and a
+missing GPU or library raises FCFCGError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import (BIN_ISO, BIN_SMU, BIN_SPI, GEOM_BOX, GEOM_SURVEY,
+                   PREC_FP32_RECHECK, PREC_FP64, FCFCGError)
+
+
+class PairCounter:
+    """One binning set-up on one GPU.
+
+    geometry: "box" (FCFC_2PT_BOX, periodic) or "survey" (FCFC_2PT).
+    bintype: BINNING_SCHEME (0 iso, 1 (s,mu), 2 (s_perp,pi)).
+    Separation bins: linear (smin, smax, ds) or ``sedges`` (ns+1 edges as
+    read_bins gives them); pi bins likewise; ``nmu`` for (s, mu).
+    """
+
+    def __init__(self, geometry="box", bintype=BIN_SMU, box=None, smin=0.0,
+                 smax=None, ds=None, sedges=None, nmu=1, pmin=0.0, pmax=None,
+                 dpi=None, pedges=None, device=-1, host_only=False):
+        lib = capi.load_library()
+        self.lib = lib
+        geom = GEOM_BOX if geometry in ("box", GEOM_BOX) else GEOM_SURVEY
+        self.geometry = geom
+        self.bintype = int(bintype)
+        self._b, self._keep = capi.make_binning(
+            geom, bintype, box=box, smin=smin, ds=ds if ds is not None else 1.0,
+            smax=smax, sedges=sedges, nmu=nmu, pmin=pmin, pmax=pmax,
+            dpi=dpi if dpi is not None else 1.0, pedges=pedges)
+        h = C.c_void_p()
+        if host_only:
+            rc = lib.fcfcg_create_host(C.byref(self._b), C.byref(h))
+        else:
+            rc = lib.fcfcg_create(C.byref(self._b), int(device), C.byref(h))
+        self.h = h
+        if rc:
+            msg = lib.fcfcg_last_error(h).decode() if h else ""
+            lib.fcfcg_destroy(h)
+            self.h = None
+            raise FCFCGError(rc, msg)
+        info = capi.BinsInfo()
+        self._check(lib.fcfcg_bins_info_get(self.h, C.byref(info)))
+        self.info = info
+        self.ns, self.nmu, self.np, self.ntot = info.ns, info.nmu, info.np, info.ntot
+        self.rescale = info.rescale
+        self.box_raw = None if box is None else np.broadcast_to(
+            np.asarray(box, float), (3,)).copy()
+        self.sbin = np.zeros(self.ns + 1)
+        self.pbin = np.zeros(self.np + 1) if self.bintype == BIN_SPI else None
+        self._check(lib.fcfcg_bins_edges(self.h, capi.ptr(self.sbin),
+                                         capi.ptr(self.pbin)))
+        self._n = {}
+
+    # -- plumbing -----------------------------------------------------------
+    def _check(self, rc):
+        if rc:
+            msg = self.lib.fcfcg_last_error(self.h).decode() if self.h else ""
+            raise FCFCGError(rc, msg)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fcfcg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- tables -------------------------------------------------------------
+    def tables(self):
+        st = np.zeros(self.info.nstab, np.uint16)
+        pt = np.zeros(self.info.nptab, np.uint16)
+        s2 = np.zeros(self.ns + 1)
+        pb = np.zeros(self.np + 1) if self.bintype == BIN_SPI else None
+        self._check(self.lib.fcfcg_bins_tables(self.h, capi.ptr(st),
+                                               capi.ptr(pt), capi.ptr(s2),
+                                               capi.ptr(pb)))
+        return st, pt, s2, pb
+
+    # -- catalogues ---------------------------------------------------------
+    def load(self, slot: int, xyz, w=None):
+        """Copy a catalogue (N x 3 FP64 host array, coordinates as read, and
+        optional weights) to the device slot."""
+        xyz = np.asarray(xyz, np.float64)
+        cols = [np.ascontiguousarray(xyz[:, k]) for k in range(3)]
+        ww = None if w is None else np.ascontiguousarray(w, np.float64)
+        self._check(self.lib.fcfcg_load_catalog(
+            self.h, int(slot), len(xyz), *[capi.ptr(c) for c in cols],
+            capi.ptr(ww)))
+        self._n[slot] = (len(xyz), w is not None)
+
+    def load_device(self, slot: int, x_ptr: int, y_ptr: int, z_ptr: int,
+                    n: int, w_ptr: int | None = None):
+        """Catalogue already on the device (FP64 pointers, e.g. from torch)."""
+        self._check(self.lib.fcfcg_load_catalog_device(
+            self.h, int(slot), int(n), C.c_void_p(x_ptr), C.c_void_p(y_ptr),
+            C.c_void_p(z_ptr), C.c_void_p(w_ptr) if w_ptr else None))
+        self._n[slot] = (int(n), w_ptr is not None)
+
+    def catalog_info(self, slot: int):
+        n = C.c_size_t()
+        sw = C.c_double()
+        self._check(self.lib.fcfcg_catalog_info(self.h, int(slot), C.byref(n),
+                                                C.byref(sw)))
+        return n.value, sw.value
+
+    def set_cells_per_smax(self, k: int):
+        self._check(self.lib.fcfcg_set_cells_per_smax(self.h, int(k)))
+
+    # -- counting -----------------------------------------------------------
+    def count_pairs(self, a: int, b: int | None = None, weighted=False,
+                    precision=PREC_FP32_RECHECK, out=None):
+        """count_pairs: unordered pairs once for auto (b None or == a)."""
+        isauto = b is None or b == a
+        b = a if b is None else b
+        if weighted:
+            res = out if out is not None else np.zeros(self.ntot, np.float64)
+            self._check(self.lib.fcfcg_count(self.h, a, b, int(isauto), 1,
+                                             int(precision), None,
+                                             capi.ptr(res)))
+        else:
+            res = out if out is not None else np.zeros(self.ntot, np.int64)
+            self._check(self.lib.fcfcg_count(self.h, a, b, int(isauto), 0,
+                                             int(precision), capi.ptr(res),
+                                             None))
+        return res
+
+    def stats(self) -> dict:
+        s = capi.Stats()
+        self._check(self.lib.fcfcg_stats_get(self.h, C.byref(s)))
+        return s.as_dict()
+
+    # -- post-processing (eval_cf.c) ---------------------------------------
+    def normalise(self, cnt, isauto, weighted, n1, n2=None):
+        """eval_pairs: auto counts doubled; returns (cnt, norm, ncnt)."""
+        cnt = np.asarray(cnt)
+        if isauto:
+            cnt = cnt * 2
+        norm = self.lib.fcfcg_norm(int(isauto), int(weighted), float(n1),
+                                   float(n2 if n2 is not None else 0.0))
+        return cnt, norm, cnt / norm
+
+    def analytic_rr(self):
+        rr = np.zeros(self.ntot)
+        self._check(self.lib.fcfcg_analytic_rr(self.h, capi.ptr(rr)))
+        return rr
+
+    def multipoles(self, xi, poles):
+        xi = np.ascontiguousarray(xi, np.float64)
+        pl = np.ascontiguousarray(poles, np.int32)
+        mp = np.zeros(len(pl) * self.ns)
+        self._check(self.lib.fcfcg_multipoles(self.h, capi.ptr(xi), len(pl),
+                                              capi.ptr(pl), capi.ptr(mp)))
+        return mp.reshape(len(pl), self.ns)
+
+    def wp(self, xi):
+        xi = np.ascontiguousarray(xi, np.float64)
+        out = np.zeros(self.ns)
+        self._check(self.lib.fcfcg_wp(self.h, capi.ptr(xi), capi.ptr(out)))
+        return out
+
+    # -- files (save_res.c / read_res.c) ------------------------------------
+    def write_paircount(self, fname, ofmt, isauto, weighted, ntr, wtr, norm,
+                        ncnt, cnt):
+        nt = np.zeros(2, np.uint64)
+        nt[:len(ntr)] = ntr
+        wt = np.zeros(2, np.float64)
+        if wtr is not None:
+            wt[:len(wtr)] = wtr
+        ncnt = np.ascontiguousarray(ncnt, np.float64)
+        ic = None if weighted else np.ascontiguousarray(cnt, np.int64)
+        wc = np.ascontiguousarray(cnt, np.float64) if weighted else None
+        self._check(self.lib.fcfcg_write_paircount(
+            self.h, fname.encode(), int(ofmt), int(isauto), int(weighted),
+            capi.ptr(nt), capi.ptr(wt), float(norm), capi.ptr(ncnt),
+            capi.ptr(ic), capi.ptr(wc)))
+
+    def read_paircount(self, fname):
+        au, wt = C.c_int(), C.c_int()
+        nt = np.zeros(2, np.uint64)
+        wtr = np.zeros(2)
+        norm = C.c_double()
+        ncnt = np.zeros(self.ntot)
+        ic = np.zeros(self.ntot, np.int64)
+        wc = np.zeros(self.ntot)
+        self._check(self.lib.fcfcg_read_paircount(
+            self.h, fname.encode(), C.byref(au), C.byref(wt), capi.ptr(nt),
+            capi.ptr(wtr), C.byref(norm), capi.ptr(ncnt), capi.ptr(ic),
+            capi.ptr(wc)))
+        return dict(auto=bool(au.value), weighted=bool(wt.value), ntr=nt,
+                    wtr=wtr, norm=norm.value, ncnt=ncnt,
+                    cnt=wc if wt.value else ic)
+
+    def write_cf(self, fname, xi):
+        xi = np.ascontiguousarray(xi, np.float64)
+        self._check(self.lib.fcfcg_write_cf(self.h, fname.encode(), capi.ptr(xi)))
+
+    def write_multipoles(self, fname, poles, mp):
+        pl = np.ascontiguousarray(poles, np.int32)
+        mp = np.ascontiguousarray(mp, np.float64).ravel()
+        self._check(self.lib.fcfcg_write_multipoles(
+            self.h, fname.encode(), len(pl), capi.ptr(pl), capi.ptr(mp)))
+
+    def write_wp(self, fname, wp):
+        wp = np.ascontiguousarray(wp, np.float64)
+        self._check(self.lib.fcfcg_write_wp(self.h, fname.encode(), capi.ptr(wp)))

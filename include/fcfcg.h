@@ -1,0 +1,226 @@
+/*
+ * fcfcg.h -- C ABI of the GB300 pair-counting engine for FCFC's hot path.
+ *
+ * The engine replaces FCFC's pair counter
+ *     int count_pairs(const void *tree1, const void *tree2, CF *cf,
+ *                     COUNT *cnt, bool isauto, bool withwt)
+ * (src/fcfc/2pt_box/count_func.h:54-59, survey twin src/fcfc/2pt/count_func.h)
+ * together with the set-up it depends on (binning, src/fcfc/2pt_box/setup_cf.c and src/fcfc/2pt/setup_cf.c;
+ * catalogue rescaling, src/fcfc/2pt_box/build_tree.c and src/fcfc/2pt/build_tree.c) and the post-processing that
+ * follows it (normalisation, analytic RR, multipoles, w_p and the pair-count
+ * files, src/fcfc/2pt_box/eval_cf.c and save_res.c).
+ *
+ * Conventions
+ *   - Every function returns FCFCG_OK (0) or a negative error code; the codes
+ *     mirror FCFC's FCFC_ERR_* (src/util/define_comm.h:218-234) and add
+ *     FCFCG_ERR_CUDA / FCFCG_ERR_TIMEOUT / FCFCG_ERR_UNSUPPORTED.
+ *   - No exceptions or aborts cross the ABI.  fcfcg_strerror() names a code,
+ *     fcfcg_last_error() gives the message of the last failure on a context.
+ *   - A context owns all its device memory and one CUDA stream.  Contexts are
+ *     thread-compatible, not thread-safe: one host thread per context.
+ *   - Host arrays are plain pointers and sizes; nothing here needs a CUDA or
+ *     PyTorch header.
+ *   - There is no CPU fallback: without a usable CUDA device fcfcg_create()
+ *     fails with FCFCG_ERR_CUDA.
+ */
+#ifndef FCFCG_H
+#define FCFCG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FCFCG_VERSION "0.1.0"
+#define FCFCG_FCFC_VERSION "1.0.1"   /* FCFC version whose files are written */
+
+/* Error codes (FCFC_ERR_* values from src/util/define_comm.h:218-234). */
+#define FCFCG_OK                 0
+#define FCFCG_ERR_MEMORY        (-1)
+#define FCFCG_ERR_ARG           (-2)
+#define FCFCG_ERR_FILE          (-3)
+#define FCFCG_ERR_CFG           (-4)
+#define FCFCG_ERR_DATA          (-21)
+#define FCFCG_ERR_CNVT          (-22)
+#define FCFCG_ERR_CF            (-24)
+#define FCFCG_ERR_SAVE          (-25)
+#define FCFCG_ERR_UNKNOWN       (-99)
+#define FCFCG_ERR_CUDA          (-100)  /* CUDA runtime failure / no device */
+#define FCFCG_ERR_TIMEOUT       (-101)  /* a bounded device wait ran out */
+#define FCFCG_ERR_UNSUPPORTED   (-102)  /* configuration outside the engine */
+
+/* BINNING_SCHEME (src/fcfc/2pt_box/define.h:46-48). */
+#define FCFCG_BIN_ISO 0
+#define FCFCG_BIN_SMU 1
+#define FCFCG_BIN_SPI 2
+
+/* Geometry: FCFC_2PT_BOX (periodic) or FCFC_2PT (survey). */
+#define FCFCG_GEOM_BOX    0
+#define FCFCG_GEOM_SURVEY 1
+
+/* Precision of the separation arithmetic. */
+#define FCFCG_PREC_FP32_RECHECK 0  /* FP32 separations, FP64 recheck near edges */
+#define FCFCG_PREC_FP64         1  /* every pair in FP64 */
+
+/* Lookup-table kinds (FCFC_LOOKUP_TYPE_*). */
+#define FCFCG_TAB_INT    0
+#define FCFCG_TAB_HYBRID 1
+
+typedef struct fcfcg_ctx fcfcg_ctx;
+
+/*
+ * Binning configuration, as FCFC's keys give it.  Separation (or s_perp)
+ * bins are linear from SEP_BIN_MIN / SEP_BIN_SIZE with ns bins when
+ * sedges == NULL, otherwise the ns+1 edges SEP_BIN_FILE yields after
+ * read_bins (src/fcfc/2pt_box/setup_cf.c:74-119).  Likewise for pi.
+ * ns / np for linear bins are the counts conf_verify derives
+ * (src/fcfc/2pt_box/load_conf.c:985-995); fcfcg_linear_nbin() computes them.
+ */
+typedef struct {
+  int geometry;          /* FCFCG_GEOM_BOX or FCFCG_GEOM_SURVEY */
+  int bintype;           /* BINNING_SCHEME */
+  double box[3];         /* BOX_SIZE (box geometry only) */
+  int ns;                /* number of s (or s_perp) bins */
+  double smin, ds;       /* SEP_BIN_MIN, SEP_BIN_SIZE (linear bins) */
+  const double *sedges;  /* ns+1 edges, or NULL for linear bins */
+  int nmu;               /* MU_BIN_NUM ((s,mu) only) */
+  int np;                /* number of pi bins ((s_perp,pi) only) */
+  double pmin, dpi;      /* PI_BIN_MIN, PI_BIN_SIZE (linear bins) */
+  const double *pedges;  /* np+1 edges, or NULL */
+} fcfcg_binning;
+
+/* Summary of the bin set-up cf_setup would produce. */
+typedef struct {
+  int ns, nmu, np;
+  int64_t ntot;          /* ns * (nmu | np | 1) */
+  int tabtype;           /* FCFCG_TAB_INT or FCFCG_TAB_HYBRID */
+  double rescale;        /* coordinate rescale factor */
+  double box_rescaled[3];
+  int64_t nstab, nptab;  /* lookup-table lengths */
+} fcfcg_bins_info;
+
+/* Counters of the last fcfcg_count() call. */
+typedef struct {
+  uint64_t candidates;   /* pairs whose separation was evaluated */
+  uint64_t in_range;     /* unique pairs that landed in a bin */
+  uint64_t rechecked;    /* pairs re-binned in FP64 */
+  uint64_t recheck_inline; /* rechecks done inline after the queue filled */
+  double ms_grid;        /* device time of the cell-grid build (ms) */
+  double ms_count;       /* device time of the counting kernel (ms) */
+  double ms_recheck;     /* device time of the recheck kernel (ms) */
+  double ms_total;       /* device time of the whole call (ms) */
+  int cells_per_smax;    /* grid refinement used */
+  int ncell[3];
+  int nstencil;
+  uint64_t nchunks;
+  int precision_used;    /* FCFCG_PREC_*: FP32 windows too wide fall to FP64 */
+} fcfcg_stats;
+
+const char *fcfcg_strerror(int err);
+const char *fcfcg_last_error(const fcfcg_ctx *ctx);
+
+/* Number of linear bins conf_verify derives from (min, max, step). */
+int fcfcg_linear_nbin(double vmin, double vmax, double step);
+
+/*
+ * Create a context for one binning set-up on CUDA device `device` (-1: the
+ * current device).  Replaces cf_setup's binning part
+ * (src/fcfc/2pt_box/setup_cf.c:599-680, survey src/fcfc/2pt/setup_cf.c).
+ * Fails with FCFCG_ERR_CFG where cf_setup/conf_verify would reject the
+ * bins (e.g. s_max >= half the box, src/fcfc/2pt_box/load_conf.c:1000-1003).
+ */
+int fcfcg_create(const fcfcg_binning *cfg, int device, fcfcg_ctx **ctx);
+void fcfcg_destroy(fcfcg_ctx *ctx);
+
+/* Host-only bin set-up (no device needed): the same tables fcfcg_create
+ * builds, for inspection.  The returned handle is freed with
+ * fcfcg_destroy(). */
+int fcfcg_create_host(const fcfcg_binning *cfg, fcfcg_ctx **ctx);
+
+int fcfcg_bins_info_get(const fcfcg_ctx *ctx, fcfcg_bins_info *out);
+/* Raw (unrescaled) edges: sbin[ns+1], pbin[np+1] (either may be NULL). */
+int fcfcg_bins_edges(const fcfcg_ctx *ctx, double *sbin, double *pbin);
+/* Reference lookup tables widened to 16 bits (stab[nstab], ptab[nptab]) and
+ * the rescaled squared-s edges / (squared for surveys) pi edges. */
+int fcfcg_bins_tables(const fcfcg_ctx *ctx, uint16_t *stab, uint16_t *ptab,
+    double *s2bin, double *pbin);
+
+/*
+ * Load a catalogue into slot (0..7): host FP64 coordinates as FCFC reads them
+ * (not rescaled; the engine rescales like tree_create,
+ * src/fcfc/2pt_box/build_tree.c:121-131) and optional weights (NULL:
+ * unweighted).  Box catalogues must lie in [0, BOX_SIZE) up to rounding.
+ * The host arrays are copied; they may be freed after the call.
+ */
+int fcfcg_load_catalog(fcfcg_ctx *ctx, int slot, size_t n, const double *x,
+    const double *y, const double *z, const double *w);
+
+/* Same, from device pointers (FP64, n elements each; w may be NULL). */
+int fcfcg_load_catalog_device(fcfcg_ctx *ctx, int slot, size_t n,
+    const double *x, const double *y, const double *z, const double *w);
+
+/* Number of objects and sum of weights (n when unweighted) of a slot. */
+int fcfcg_catalog_info(const fcfcg_ctx *ctx, int slot, size_t *n,
+    double *sumw);
+
+/*
+ * Count pairs between slots a and b; replaces count_pairs
+ * (src/fcfc/2pt_box/count_func.h:54-59).  isauto: a == b, unordered pairs
+ * counted once (not doubled; eval_pairs doubles them).  withwt: weighted
+ * sums (catalogues without weights count as unit weights).  Outputs are
+ * caller-owned arrays of ntot entries, index s + ns * (mu or pi): icnt for
+ * unweighted counts, wcnt for weighted sums (the other may be NULL).
+ */
+int fcfcg_count(fcfcg_ctx *ctx, int slot_a, int slot_b, int isauto,
+    int withwt, int precision, int64_t *icnt, double *wcnt);
+
+int fcfcg_stats_get(const fcfcg_ctx *ctx, fcfcg_stats *out);
+
+/* Grid refinement: cells per maximum separation (0 = automatic). */
+int fcfcg_set_cells_per_smax(fcfcg_ctx *ctx, int k);
+
+/* ---------------- post-processing (src/fcfc/2pt_box/eval_cf.c) ----------- */
+
+/* Normalisation of eval_pairs (eval_cf.c:125-149): auto n(n-1) or W(W-1),
+ * cross n1*n2 or W1*W2. */
+double fcfcg_norm(int isauto, int withwt, double n1_or_w1, double n2_or_w2);
+
+/* Analytic RR per bin for the periodic box (eval_cf.c:220-241). */
+int fcfcg_analytic_rr(const fcfcg_ctx *ctx, double *rr);
+
+/* Legendre multipoles of xi(s,mu) (eval_cf.c:326-354): mp[l*ns + s]. */
+int fcfcg_multipoles(const fcfcg_ctx *ctx, const double *xi, int npole,
+    const int *poles, double *mp);
+
+/* Projected correlation function of xi(s_perp,pi) (eval_cf.c:365-388). */
+int fcfcg_wp(const fcfcg_ctx *ctx, const double *xi, double *wp);
+
+/*
+ * Write a pair-count file exactly as save_res does
+ * (src/fcfc/2pt_box/save_res.c:45-310): ofmt 0 binary, 1 ASCII.
+ * ntr[2]/wtr[2]: numbers / weighted numbers of the tracers (the second is
+ * ignored for auto pairs).  icnt (unweighted) or wcnt (weighted) are the
+ * doubled-for-auto counts FCFC stores.
+ */
+int fcfcg_write_paircount(const fcfcg_ctx *ctx, const char *fname, int ofmt,
+    int isauto, int withwt, const uint64_t ntr[2], const double wtr[2],
+    double norm, const double *ncnt, const int64_t *icnt, const double *wcnt);
+
+/* Read the counts back from a binary pair-count file (read_res.c:256-479);
+ * checks that the file's bins match the context.  Outputs may be NULL. */
+int fcfcg_read_paircount(const fcfcg_ctx *ctx, const char *fname,
+    int *isauto, int *withwt, uint64_t ntr[2], double wtr[2], double *norm,
+    double *ncnt, int64_t *icnt, double *wcnt);
+
+/* Write xi / multipoles / w_p text files as save_res_ascii does. */
+int fcfcg_write_cf(const fcfcg_ctx *ctx, const char *fname, const double *xi);
+int fcfcg_write_multipoles(const fcfcg_ctx *ctx, const char *fname,
+    int npole, const int *poles, const double *mp);
+int fcfcg_write_wp(const fcfcg_ctx *ctx, const char *fname, const double *wp);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
