@@ -1,0 +1,388 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 pair-counting engine on FCFC's clustered-box
+workload, one JSON line on stdout.
+
+Workload ("ns_box_2e6"): Neyman-Scott catalogue, 2e4 uniform parents in a
+periodic box of side 2000 Mpc/h, Poisson(100) children per parent with
+isotropic Gaussian offsets (sigma = 5 Mpc/h), about 2e6 points with
+lognormal(0, 0.3) weights, FP64 coordinates.  One step counts the weighted
+DD pairs twice, as two FCFC runs would:
+  (s, mu)       s in [0, 200) Mpc/h, 40 linear bins, 100 mu bins;
+  (s_perp, pi)  40 logarithmic s_perp bins in [0.1, 100), pi in [0, 40) in
+                40 linear bins.
+The metric is unique in-range pairs per second (pairs that land in a bin,
+i < j), summed over both counts.
+
+  value   -- FP32 + FP64-recheck path, catalogue already in HBM; a step is
+             catalogue preparation (rescale, cell sort) plus both counts,
+             timed with CUDA events on the engine's stream; L2 is flushed
+             between steps.
+  e2e     -- the same step through the C ABI from pinned host buffers: the
+             host-to-device copy of the catalogue and the read-back of the
+             counts are inside the timed region.
+  fp64    -- the all-FP64 GPU path on the same step (one step).
+--impl reference times the CPU restatement of FCFC's counter (oracle/, the
+reference's FP64 per-pair formula, OpenMP on every host core) on a bounded
+sample of the workload (same density, smaller box).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "in-range pairs/s on 1 GB300: FP32+FP64-recheck vs all-FP64, exact counts"
+UNIT = "pairs/s"
+BOX = 2000.0
+LOGBINS = np.geomspace(0.1, 100.0, 41)
+FLOPS_PER_PAIR = {"smu": 10, "spi": 8}   # algorithmic FP32 flops per pair
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def workload(box=BOX, nparent=20000, seed=1):
+    from fcfc_gb300 import synth
+    x = synth.neyman_scott(nparent, box, 100.0, 5.0, seed=seed)
+    w = synth.lognormal_weights(len(x), 0.3, seed=seed + 1)
+    return x, w
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for ln in self.lines:
+            f = [v.strip() for v in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def fp32_peak_tflops(dev):
+    """Measured FP32 (non-tensor) throughput: cuBLAS SGEMM with TF32 off."""
+    import torch
+    torch.backends.cuda.matmul.allow_tf32 = False
+    n = 8192
+    a = torch.randn(n, n, device=dev, dtype=torch.float32)
+    b = torch.randn(n, n, device=dev, dtype=torch.float32)
+    for _ in range(2):
+        torch.mm(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.mm(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary, if there is one."""
+    p = os.path.join(ROOT, "profiles", "k_count32_box_smu_wt_ns_box.txt")
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch_full_workload:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def run_reference(args, rank, world):
+    """CPU restatement of FCFC's counter on a bounded sample of the workload."""
+    if rank != 0:
+        return 0
+    from oracle import fcfc_oracle as fo
+    box = 1200.0   # same density: 2e4 * (1200/2000)^3 parents
+    x, w = workload(box=box, nparent=int(round(20000 * (box / BOX) ** 3)), seed=1)
+    b1 = fo.Bins(False, 1, ns=40, smin=0, ds=5, nmu=100, box=box)
+    b2 = fo.Bins(False, 2, ns=40, sedges=LOGBINS, np_=40, pmin=0, dpi=1, box=box)
+    nthr = os.cpu_count() or 1
+
+    def step():
+        t0 = time.perf_counter()
+        c1 = b1.count(x, wa=w, mode=3)
+        c2 = b2.count(x, wa=w, mode=3)
+        return time.perf_counter() - t0, c1, c2
+
+    # unweighted in-range count once (weighted sums are not pair numbers)
+    n_in = int(b1.count(x, mode=3).sum() + b2.count(x, mode=3).sum())
+    for _ in range(args.warmup):
+        step()
+    tt = 0.0
+    for _ in range(args.steps):
+        dt, _, _ = step()
+        tt += dt
+    val = n_in * args.steps / tt
+    sample = ("Neyman-Scott box L=%g Mpc/h, %d points (same density as the "
+              "2e6-point workload), weighted DD (s,mu)+(s_perp,pi), %d pairs "
+              "per step" % (box, len(x), n_in))
+    out = {
+        "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": tt / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "ns_box_2e6 (bounded CPU sample)", "box": box,
+                   "n_points": len(x), "bins": "smu 40x100 + spi 40x40"},
+        "impl": "reference",
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": nthr,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def cpu_baseline_sample():
+    """A short run of the CPU restatement (10-30 s of CPU work)."""
+    from oracle import fcfc_oracle as fo
+    box = 1000.0
+    x, w = workload(box=box, nparent=int(round(20000 * (box / BOX) ** 3)), seed=3)
+    b1 = fo.Bins(False, 1, ns=40, smin=0, ds=5, nmu=100, box=box)
+    b2 = fo.Bins(False, 2, ns=40, sedges=LOGBINS, np_=40, pmin=0, dpi=1, box=box)
+    n_in = int(b1.count(x, mode=3).sum() + b2.count(x, mode=3).sum())
+    t0 = time.perf_counter()
+    b1.count(x, wa=w, mode=3)
+    b2.count(x, wa=w, mode=3)
+    dt = time.perf_counter() - t0
+    return {"value": n_in / dt, "unit": UNIT, "cores": os.cpu_count() or 1,
+            "kind": "port",
+            "sample": "Neyman-Scott box L=%g Mpc/h, %d points, weighted DD "
+                      "(s,mu)+(s_perp,pi), %d in-range pairs, %.2f s" %
+                      (box, len(x), n_in, dt)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--small", action="store_true",
+                    help="quarter-size box (for profiler captures)")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = env_rank()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        rc = run_reference(args, rank, world)
+        if dist:
+            dist.barrier()
+        return rc
+
+    import torch
+    import fcfc_gb300 as fg
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    box = BOX / 2 if args.small else BOX
+    npar = 20000 // 8 if args.small else 20000
+    x, w = workload(box=box, nparent=npar, seed=1 + rank)
+    n = len(x)
+    # device-resident raw catalogue (FP64, as read)
+    xd = [torch.from_numpy(np.ascontiguousarray(x[:, k])).to(dev) for k in range(3)]
+    wd = torch.from_numpy(w).to(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    p1 = fg.PairCounter("box", fg.BIN_SMU, box=box, smin=0, smax=200, ds=5,
+                        nmu=100, device=local)
+    p2 = fg.PairCounter("box", fg.BIN_SPI, box=box, sedges=LOGBINS, pmin=0,
+                        pmax=40, dpi=1, device=local)
+
+    def step(prec=fg.PREC_FP32_RECHECK):
+        ms = 0.0
+        res = []
+        for pc in (p1, p2):
+            pc.load_device(0, xd[0].data_ptr(), xd[1].data_ptr(),
+                           xd[2].data_ptr(), n, wd.data_ptr())
+            c = pc.count_pairs(0, weighted=True, precision=prec)
+            st = pc.stats()
+            ms += st["ms_total"]
+            res.append((c, st))
+        return ms, res
+
+    # exact in-range pair numbers of this workload (unweighted counts)
+    n_in = []
+    for pc in (p1, p2):
+        pc.load_device(0, xd[0].data_ptr(), xd[1].data_ptr(), xd[2].data_ptr(),
+                       n, wd.data_ptr())
+        n_in.append(int(pc.count_pairs(0, weighted=False).sum()))
+    pairs_per_step = sum(n_in)
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    ms_tot, ms_k1, launches0 = 0.0, 0.0, p1.stats()["launches"] + p2.stats()["launches"]
+    torch.cuda.synchronize()
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ms, res = step()
+        ms_tot += ms
+        ms_k1 += res[0][1]["ms_count"]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall0
+    clocks = clk.stop()
+    launches_total = p1.stats()["launches"] + p2.stats()["launches"] - launches0
+    st1 = res[0][1]
+    st2 = res[1][1]
+    # max over ranks
+    ms_step = ms_tot / args.steps
+    if dist:
+        t = torch.tensor([ms_step], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t[0])
+    value = pairs_per_step * world / (ms_step * 1e-3)
+
+    # all-FP64 GPU path, one step
+    ms64, _ = step(prec=fg.PREC_FP64)
+    fp64_value = pairs_per_step / (ms64 * 1e-3)
+
+    # end to end through the C ABI from pinned host memory
+    xh = [torch.from_numpy(np.ascontiguousarray(x[:, k])).pin_memory() for k in range(3)]
+    wh = torch.from_numpy(w).pin_memory()
+    import ctypes as C
+    lib = fg.capi.load_library()
+    e2e_res = []
+
+    def e2e_step():
+        for pc in (p1, p2):
+            rc = lib.fcfcg_load_catalog(pc.h, 0, n, C.c_void_p(xh[0].data_ptr()),
+                                        C.c_void_p(xh[1].data_ptr()),
+                                        C.c_void_p(xh[2].data_ptr()),
+                                        C.c_void_p(wh.data_ptr()))
+            if rc:
+                raise fg.FCFCGError(rc)
+            e2e_res.append(pc.count_pairs(0, weighted=True))
+
+    e2e_step()
+    torch.cuda.synchronize()
+    te = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        te += time.perf_counter() - t0
+    e2e_ms = te / args.steps * 1e3
+    h2d = 2 * n * 4 * 8
+    d2h = (p1.ntot + p2.ntot) * 16
+
+    # roofline of the dominant kernel: (s, mu) count, FP32 pipe
+    peak = fp32_peak_tflops(dev)
+    k1_ms = ms_k1 / args.steps
+    achieved = n_in[0] * FLOPS_PER_PAIR["smu"] / (k1_ms * 1e-3) / 1e12
+    traffic = profile_traffic()
+    if traffic is not None and args.small:
+        traffic = None
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64-recheck", "data": "synthetic",
+        "config": {"workload": "ns_box_2e6" if not args.small else "ns_box_2.5e5",
+                   "n_points": n, "box": box,
+                   "bins": "(s,mu) 40x100 s<200 + (s_perp,pi) 40 log [0.1,100) x 40 lin [0,40)",
+                   "weighted": True, "pairs_per_step": pairs_per_step,
+                   "pairs_smu": n_in[0], "pairs_spi": n_in[1],
+                   "l2": "flushed between steps (256 MiB write)",
+                   "cells_per_smax": [st1["cells_per_smax"], st2["cells_per_smax"]],
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": ms64,
+                 "speedup_fp32_recheck_over_fp64": value / world / fp64_value},
+        "e2e": {"value": pairs_per_step / (e2e_ms * 1e-3), "unit": UNIT,
+                "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak,
+                     "traffic": traffic,
+                     "kernel": "k_count32<box,smu,weighted>",
+                     "kernel_ms": k1_ms,
+                     "peak_source": "measured cuBLAS SGEMM (TF32 off) on this GPU",
+                     "flops_per_pair": FLOPS_PER_PAIR["smu"]},
+        "counters": {"candidates_smu": st1["candidates"],
+                     "rechecked_smu": st1["rechecked"],
+                     "candidates_spi": st2["candidates"],
+                     "rechecked_spi": st2["rechecked"],
+                     "wall_ms_per_step": wall / args.steps * 1e3},
+        "clocks": clocks,
+        "gpu_launches": int(launches_total),
+    }
+    if rank == 0 and not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline_sample()
+    if dist:
+        dist.barrier()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -48,7 +48,7 @@ class Stats(C.Structure):
                 ("ms_recheck", C.c_double), ("ms_total", C.c_double),
                 ("cells_per_smax", C.c_int), ("ncell", C.c_int * 3),
                 ("nstencil", C.c_int), ("nchunks", C.c_uint64),
-                ("precision_used", C.c_int)]
+                ("precision_used", C.c_int), ("launches", C.c_uint64)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}

@@ -43,21 +43,60 @@ __device__ __forceinline__ void add128(unsigned long long *lohi, long long v) {
   if (hi) atomicAdd(lohi + 1, hi);
 }
 
-/* Fixed-point product of two scaled weights (|w| <= 1), each split into
- * float hi + lo parts: round(w_a w_b 2^F) up to the dropped lo*lo term.
- * Shared by every path so that a pair contributes the same integer. */
-__device__ __forceinline__ long long fix_prod(float ah, float al, float bh,
-    float bl, float twoF) {
-  float p = __fmul_rn(ah, bh);
-  float e = __fmaf_rn(ah, bh, -p);
-  float c = __fmaf_rn(ah, bl, __fmul_rn(al, bh));
-  long long hi = __float2ll_rn(__fmul_rn(p, twoF));
-  int lo = __float2int_rn(__fmul_rn(__fadd_rn(e, c), twoF));
-  return hi + (long long) lo;
+/*
+ * Fixed-point product of two weights scaled to |w| <= 1, with F = 42
+ * fractional bits.  A weight is held as an integer part wi = round(w 2^30)
+ * and a float remainder wr = w - wi 2^-30:
+ *   w_a w_b 2^42 = wi_a wi_b 2^-18 + (w_a wr_b + wr_a w_b) 2^42 (+ wr wr).
+ * The first term is an exact 64-bit product rounded by a shift, the cross
+ * term (|.| <= 2^13) is rounded with the 1.5 * 2^23 float trick.  No 64-bit
+ * float conversions.  Every path uses this function, so a pair always adds
+ * the same integer.
+ */
+__device__ __forceinline__ long long fix_prod(int ia, float ra, float fa,
+    int ib, float rb, float fb) {
+  const long long p = (long long) ia * (long long) ib;
+  const long long main = (p + (1ll << 17)) >> 18;
+  const float c = __fmaf_rn(fa, rb, __fmul_rn(ra, fb));
+  const float t = __fmaf_rn(c, 4398046511104.0f /* 2^42 */, 12582912.0f);
+  return main + (long long) (__float_as_int(t) - 0x4B400000);
+}
+
+__device__ __forceinline__ long long fix_prod_pair(const fcfcg_launch &L,
+    uint32_t a, uint32_t b) {
+  const int2 wa = ((const int2 *) L.A.wq)[a];
+  const int2 wb = ((const int2 *) L.B.wq)[b];
+  const float fa = ((const float4 *) L.A.l4)[a].w;
+  const float fb = ((const float4 *) L.B.l4)[b].w;
+  return fix_prod(wa.x, __int_as_float(wa.y), fa, wb.x, __int_as_float(wb.y),
+                  fb);
 }
 
 #define HALF_U32 0x80000000u
 #define FIX_LIMIT (1ll << 61)
+#define HI_LIMIT (1 << 30)
+
+/* Weighted bin in shared memory as two 32-bit words, value = hi 2^32 + lo
+ * (lo unsigned, hi signed): native 32-bit atomics, the carry out of lo is
+ * read from the returned value, and 2^30 of hi (2^62) moves to the global
+ * 128-bit accumulator whenever hi crosses +-2^30. */
+__device__ __forceinline__ void hist_add_fix32(uint32_t *lo, int *hi,
+    unsigned long long *gwt, int bin, long long v) {
+  const uint32_t vl = (uint32_t) v;
+  const uint32_t old = atomicAdd(lo + bin, vl);
+  const int h = (int) (v >> 32) + (((old + vl) < old) ? 1 : 0);
+  if (h) {
+    const int oh = atomicAdd(hi + bin, h);
+    const int nh = oh + h;
+    if (nh >= HI_LIMIT && oh < HI_LIMIT) {
+      atomicSub(hi + bin, HI_LIMIT);
+      add128(gwt + 2 * bin, 1ll << 62);
+    } else if (nh <= -HI_LIMIT && oh > -HI_LIMIT) {
+      atomicAdd(hi + bin, HI_LIMIT);
+      add128(gwt + 2 * bin, -(1ll << 62));
+    }
+  }
+}
 
 __device__ __forceinline__ void hist_add_count(uint32_t *h,
     unsigned long long *gcnt, int bin) {
@@ -214,20 +253,22 @@ __device__ int ref_bin_pair(const fcfcg_launch &L, uint32_t a, uint32_t b,
 
 /* Bin of an FP32 value v with error bound E (< 1/2) on an axis table,
  * or FCFCG_FTAB_BIN_MASK when out of range; *amb set when an edge lies
- * within E of v. */
+ * within E of v.  CHECK_NAN: the value may be NaN (survey geometry). */
+template <bool CHECK_NAN>
 __device__ __forceinline__ unsigned ftab_bin(const uint16_t *tab, int off,
     int ntab, float v, float E, bool &amb) {
-  if (!(v == v)) {
+  if (CHECK_NAN && !(v == v)) {
     amb = true;
     return FCFCG_FTAB_BIN_MASK;
   }
-  int i = __float2int_rz(v);
-  int t = i - off;
-  if (t < 0 || t >= ntab) return FCFCG_FTAB_BIN_MASK;
-  unsigned e = tab[t];
-  float fr = v - (float) i;
-  amb |= ((e & FCFCG_FTAB_CX) != 0) | (((e & FCFCG_FTAB_LO) != 0) & (fr <= E)) |
-         (((e & FCFCG_FTAB_HI) != 0) & (fr >= 1.f - E));
+  const int i = __float2int_rz(v);
+  const int t = i - off;
+  if ((unsigned) t >= (unsigned) ntab) return FCFCG_FTAB_BIN_MASK;
+  const unsigned e = tab[t];
+  const float fr = v - (float) i;
+  const unsigned m = FCFCG_FTAB_CX | (fr <= E ? FCFCG_FTAB_LO : 0u) |
+                     (fr >= 1.f - E ? FCFCG_FTAB_HI : 0u);
+  amb |= (e & m) != 0u;
   return e & FCFCG_FTAB_BIN_MASK;
 }
 
@@ -312,11 +353,24 @@ __device__ __forceinline__ int first_j(const WarpChunk &w, bool self,
   return t + r;
 }
 
+/* Histogram of the FP32 kernel in shared memory: ntot u32 counts, or
+ * ntot u32 low words followed by ntot s32 high words for weighted sums. */
+template <int WT>
+__device__ __forceinline__ void hist_add(const fcfcg_launch &L, uint32_t *h,
+    int bin, long long w) {
+  if (WT) {
+    if (L.hist_smem) hist_add_fix32(h, (int *) (h + L.ntot), L.gwt, bin, w);
+    else add128(L.gwt + 2 * bin, w);
+  } else {
+    if (L.hist_smem) hist_add_count(h, L.gcnt, bin);
+    else atomicAdd(L.gcnt + bin, 1ull);
+  }
+}
+
 /* Queue a pair for the FP64 recheck; when the queue is full, bin it here. */
 template <int WT>
 __device__ __forceinline__ void enqueue(const fcfcg_launch &L, uint32_t a,
-    uint32_t b, uint32_t code, uint32_t *h32, long long *h64,
-    unsigned long long &n_inline) {
+    uint32_t b, uint32_t code, uint32_t *h, unsigned long long &n_inline) {
   uint32_t slot = atomicAdd(L.qcount, 1u);
   if (slot < L.qcap) {
     *((uint4 *) L.queue + slot) = make_uint4(a, b, code, 0u);
@@ -325,188 +379,415 @@ __device__ __forceinline__ void enqueue(const fcfcg_launch &L, uint32_t a,
   n_inline++;
   int bin = ref_bin_pair(L, a, b, code);
   if (bin < 0) return;
-  if (WT) {
-    const float2 wa = make_float2(((const float4 *) L.A.l4)[a].w, L.A.wlo[a]);
-    const float2 wb = make_float2(((const float4 *) L.B.l4)[b].w, L.B.wlo[b]);
-    long long v = fix_prod(wa.x, wa.y, wb.x, wb.y, ldexpf(1.f, L.fixF));
-    if (L.hist_smem) hist_add_fix(h64, L.gwt, bin, v);
-    else add128(L.gwt + 2 * bin, v);
-  } else {
-    if (L.hist_smem) hist_add_count(h32, L.gcnt, bin);
-    else atomicAdd(L.gcnt + bin, 1ull);
+  hist_add<WT>(L, h, bin, WT ? fix_prod_pair(L, a, b) : 0);
+}
+
+#define CT32_THREADS 256
+#define FCHUNK 64                 /* chunk points a CTA holds (FP32 path) */
+#define QCAP 1024                 /* queued pairs per round */
+
+/* Shared memory of the FP32 kernel after the tables and the histogram.
+ * Per CTA: the chunk points (and weights) and the neighbour list of the
+ * chunk; per warp: the 32 neighbour points of its current block and the
+ * block's in-range pairs (chunk point | lane << 6). */
+struct Stage {
+  float4 *a;        /* FCHUNK: chunk point local x y z, scaled weight */
+  int2 *aw;         /* FCHUNK: chunk point integer weight, remainder bits */
+  uint32_t *pre;    /* nsten + 1: prefix of neighbour sizes */
+  uint32_t *bst;    /* nsten: first sorted index of each neighbour */
+  float4 *b;        /* per warp, 32: neighbour (l_b - D) x y z, index */
+  float4 *bw;       /* per warp, 32: weight, integer weight, remainder */
+  uint16_t *bt;     /* per warp, 32: stencil entry */
+  uint16_t *q;      /* per warp, QCAP: queued pairs */
+};
+
+__host__ __device__ __forceinline__ size_t stage_cta_bytes(int nsten, int wt) {
+  size_t n = (size_t) FCHUNK * 16 + (wt ? (size_t) FCHUNK * 8 : 0);
+  n += (((size_t) nsten + 1) * 4 + 15) & ~(size_t) 15;
+  n += (((size_t) nsten) * 4 + 15) & ~(size_t) 15;
+  return n;
+}
+
+__host__ __device__ __forceinline__ size_t stage_warp_bytes(int wt) {
+  return 32 * 16 + (wt ? 32 * 16 : 0) + 32 * 2 + QCAP * 2;
+}
+
+__host__ __device__ __forceinline__ size_t stage_bytes(int nsten, int wt) {
+  return stage_cta_bytes(nsten, wt) +
+         (size_t) (CT32_THREADS / 32) * stage_warp_bytes(wt);
+}
+
+/* Image code of the neighbour cell of a stencil offset (box). */
+__device__ __forceinline__ uint32_t nb_code(const fcfcg_launch &L, int cx,
+    int cy, int cz, int4 o) {
+  int q[3] = {cx + o.x, cy + o.y, cz + o.z};
+  uint32_t code = 0;
+  for (int k = 0; k < 3; k++) {
+    const int n = L.ncell[k];
+    int w = 0;
+    while (q[k] < 0) { q[k] += n; w--; }
+    while (q[k] >= n) { q[k] -= n; w++; }
+    code |= (uint32_t) (w + 1) << (2 * k);
   }
+  return code;
+}
+
+/*
+ * Bin one queued pair per lane.  FP32 windows decide; ambiguous pairs go to
+ * the FP64 recheck queue.  c2 = twice the chunk cell's centre (survey).
+ */
+template <int GEOM, int BIN, int WT>
+__device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
+    const Stage &S, uint32_t ent, uint32_t first, int cx, int cy, int cz,
+    float c2x, float c2y, float c2z, const uint16_t *fs, const uint16_t *fp,
+    uint32_t *h, uint32_t &n_in, uint32_t &n_q,
+    unsigned long long &n_inline) {
+  const int i = (int) (ent & 63u), src = (int) (ent >> 6);
+  const float4 pa = S.a[i];
+  const float4 pb = S.b[src];
+  const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
+  bool amb = false;
+  int bin = -1;
+  if (BIN == FCFCG_BIN_SPI && GEOM == FCFCG_GEOM_BOX) {
+    const float sp2 = fmaf(dy, dy, dx * dx);
+    const float pi = fabsf(dz);
+    amb = !(sp2 >= L.tiny);
+    unsigned sb = ftab_bin<false>(fs, L.fsoff, L.nfs, sp2, L.Emax, amb);
+    unsigned pbn = ftab_bin<false>(fp, L.fpoff, L.nfp, pi, L.P0, amb);
+    if (!amb) {
+      if (sb == FCFCG_FTAB_BIN_MASK || pbn == FCFCG_FTAB_BIN_MASK) return;
+      bin = (int) sb + (int) pbn * L.ns;
+    }
+  } else {
+    const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    amb = !(s2 >= L.tiny);
+    if (BIN == FCFCG_BIN_ISO) {
+      unsigned sb = ftab_bin<false>(fs, L.fsoff, L.nfs, s2, L.Emax, amb);
+      if (!amb) {
+        if (sb == FCFCG_FTAB_BIN_MASK) return;
+        bin = (int) sb;
+      }
+    } else {
+      const float rs = rsqrtf(s2);
+      const float s = s2 * rs;
+      const float E = fmaf(L.K2, s2, fmaf(L.K1, s, L.K0));
+      float mx = 0.f, my = 0.f, mz = 0.f;
+      if (GEOM == FCFCG_GEOM_SURVEY) {
+        /* line of sight m = x_a + x_b = 2 (l_b - D) + 2 c_A + d */
+        mx = fmaf(2.f, pb.x, c2x) + dx;
+        my = fmaf(2.f, pb.y, c2y) + dy;
+        mz = fmaf(2.f, pb.z, c2z) + dz;
+      }
+      if (BIN == FCFCG_BIN_SMU) {
+        float q;
+        if (GEOM == FCFCG_GEOM_BOX) {
+          q = L.fnmu * fabsf(dz) * rs;
+        } else {
+          const float dm = fmaf(dz, mz, fmaf(dy, my, dx * mx));
+          const float mm = fmaf(mz, mz, fmaf(my, my, mx * mx));
+          q = L.fnmu * fabsf(dm) * rsqrtf(mm * s2);
+        }
+        const float Eq = fmaf(L.Q1, rs, fmaf(L.Q2, q, L.Q0));
+        int qi = mu_bin(q, Eq, amb);
+        unsigned sb = ftab_bin<GEOM == FCFCG_GEOM_SURVEY>(fs, L.fsoff, L.nfs,
+                                                            s2, E, amb);
+        if (!amb) {
+          if (sb == FCFCG_FTAB_BIN_MASK || qi >= L.nmu) return;
+          bin = (int) sb + qi * L.ns;
+        }
+      } else {
+        /* survey (s_perp, pi): pi^2 = (d.m)^2 / |m|^2 */
+        const float dm = fmaf(dz, mz, fmaf(dy, my, dx * mx));
+        const float mm = fmaf(mz, mz, fmaf(my, my, mx * mx));
+        const float pi2 = __fdividef(dm * dm, mm);
+        const float sp2 = s2 - pi2;
+        const float Ep = fmaf(L.P2, s2, fmaf(L.P1, s, L.P0));
+        unsigned pbn = ftab_bin<true>(fp, L.fpoff, L.nfp, pi2, Ep, amb);
+        unsigned sb = ftab_bin<true>(fs, L.fsoff, L.nfs,
+                                     sp2 < 0.f ? 0.f : sp2, E + Ep, amb);
+        if (!amb) {
+          if (sb == FCFCG_FTAB_BIN_MASK || pbn == FCFCG_FTAB_BIN_MASK) return;
+          bin = (int) sb + (int) pbn * L.ns;
+        }
+      }
+    }
+  }
+  const uint32_t ai = first + (uint32_t) i;
+  const uint32_t bj = __float_as_uint(pb.w);
+  if (amb) {
+    n_q++;
+    uint32_t code = 0;
+    if (GEOM == FCFCG_GEOM_BOX)
+      code = nb_code(L, cx, cy, cz, __ldg((const int4 *) L.sten + S.bt[src]));
+    enqueue<WT>(L, ai, bj, code, h, n_inline);
+    return;
+  }
+  n_in++;
+  long long w = 0;
+  if (WT) {
+    const int2 wa = S.aw[i];
+    const float4 bw = S.bw[src];
+    w = fix_prod(wa.x, __int_as_float(wa.y), pa.w, __float_as_int(bw.y), bw.z,
+                 bw.x);
+  }
+  hist_add<WT>(L, h, bin, w);
+}
+
+/* Compare a neighbour point (one per lane) with chunk points [i0, i1):
+ * bit i - i0 of the result marks a candidate inside the outer range. */
+template <int GEOM, int BIN>
+__device__ __forceinline__ uint32_t scan_chunk(const fcfcg_launch &L,
+    const float4 *a, int i0, int i1, int ilim, float bx, float by,
+    float bz) {
+  uint32_t msk = 0;
+#pragma unroll 4
+  for (int i = i0; i < i1; i++) {
+    const float4 pa = a[i];
+    const float dx = pa.x - bx, dy = pa.y - by, dz = pa.z - bz;
+    bool inr;
+    if (BIN == FCFCG_BIN_SPI && GEOM == FCFCG_GEOM_BOX) {
+      const float v = fmaf(dy, dy, dx * dx);
+      inr = (i < ilim) & (fabsf(dz) < L.p_lim) & (v < L.s_lim);
+    } else {
+      const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+      inr = (i < ilim) & (v < L.s_lim);
+    }
+    msk |= (uint32_t) inr << (i - i0);
+  }
+  return msk;
 }
 
 /*
  * FP32 counting kernel.  GEOM: box / survey; BIN: iso / smu / spi;
- * WT: weighted.  Shared memory: FP32 tables then the histogram.
+ * WT: weighted.  Shared memory: FP32 tables, the histogram, the CTA's chunk
+ * and neighbour list, and per warp a block of neighbour points and a queue.
+ *
+ * A CTA holds one chunk (<= 64 points of a cell).  The non-empty neighbour
+ * cells of the stencil are laid end to end (a prefix sum per chunk); the
+ * warps take blocks of 32 consecutive neighbour points in turn, and each
+ * lane compares its point with every chunk point (broadcast from shared
+ * memory), recording those inside the outer range as mask bits.  A block's
+ * in-range pairs are then compacted into the warp queue and binned 32 at a
+ * time, every lane busy.
  */
 template <int GEOM, int BIN, int WT>
-__global__ void __launch_bounds__(CT_THREADS)
+__global__ void __launch_bounds__(CT32_THREADS, 4)
 k_count32(const fcfcg_launch L) {
   extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint32_t sh_chunk;
   uint16_t *fs = (uint16_t *) smem;
   uint16_t *fp = fs + L.nfs;
   size_t hoff = ((size_t) (L.nfs + L.nfp) * sizeof(uint16_t) + 15) & ~(size_t) 15;
-  uint32_t *h32 = (uint32_t *) (smem + hoff);
-  long long *h64 = (long long *) (smem + hoff);
+  uint32_t *h = (uint32_t *) (smem + hoff);
+  size_t soff = hoff + (L.hist_smem ? (size_t) L.ntot * (WT ? 8 : 4) : 0);
+  soff = (soff + 15) & ~(size_t) 15;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Stage S;
+  {
+    unsigned char *b = smem + soff;
+    S.a = (float4 *) b;
+    b += (size_t) FCHUNK * 16;
+    S.aw = (int2 *) b;
+    b += WT ? (size_t) FCHUNK * 8 : 0;
+    S.pre = (uint32_t *) b;
+    b += (((size_t) L.nsten + 1) * 4 + 15) & ~(size_t) 15;
+    S.bst = (uint32_t *) b;
+    b += (((size_t) L.nsten) * 4 + 15) & ~(size_t) 15;
+    b += (size_t) warp * stage_warp_bytes(WT);
+    S.b = (float4 *) b;
+    b += 32 * 16;
+    S.bw = (float4 *) b;
+    b += WT ? 32 * 16 : 0;
+    S.bt = (uint16_t *) b;
+    b += 32 * 2;
+    S.q = (uint16_t *) b;
+  }
   for (int i = threadIdx.x; i < L.nfs; i += blockDim.x) fs[i] = L.fs[i];
   for (int i = threadIdx.x; i < L.nfp; i += blockDim.x) fp[i] = L.fp[i];
-  if (L.hist_smem) {
-    if (WT)
-      for (long i = threadIdx.x; i < L.ntot; i += blockDim.x) h64[i] = 0;
-    else
-      for (long i = threadIdx.x; i < L.ntot; i += blockDim.x) h32[i] = 0;
-  }
-  __syncthreads();
+  if (L.hist_smem)
+    for (long i = threadIdx.x; i < L.ntot * (WT ? 2 : 1); i += blockDim.x) h[i] = 0;
 
-  const float4 *__restrict__ Al4 = (const float4 *) L.A.l4;
   const float4 *__restrict__ Bl4 = (const float4 *) L.B.l4;
+  const int2 *__restrict__ Bwq = (const int2 *) L.B.wq;
   const int4 *__restrict__ sten = (const int4 *) L.sten;
   const float4 *__restrict__ stD = (const float4 *) L.stenD;
-  const float twoF = ldexpf(1.f, L.fixF);
-  unsigned long long n_cand = 0, n_in = 0, n_q = 0, n_inline = 0;
+  const int nwarp = CT32_THREADS / 32;
+  unsigned long long n_cand = 0, n_in64 = 0, n_q64 = 0, n_inline = 0;
 
-  WarpChunk w;
-  while (next_chunk(L, w)) {
-    float4 pa = make_float4(0.f, 0.f, 0.f, 0.f);
-    float walo = 0.f;
-    if (w.active) {
-      pa = Al4[w.ai];
-      if (WT) walo = L.A.wlo[w.ai];
+  for (;;) {
+    __syncthreads();    /* the previous chunk is done with a / pre / bst */
+    if (threadIdx.x == 0) sh_chunk = atomicAdd(L.chunk_head, 1u);
+    __syncthreads();
+    const uint32_t c = sh_chunk;
+    if (c >= L.nchunk) break;
+    const uint4 ch = __ldg(((const uint4 *) L.chunks) + c);
+    const uint32_t cell = ch.x, first = ch.y;
+    const int m = (int) ch.z;
+    const int cx = (int) (cell % (uint32_t) L.ncell[0]);
+    const int cy = (int) ((cell / (uint32_t) L.ncell[0]) % (uint32_t) L.ncell[1]);
+    const int cz = (int) (cell / ((uint32_t) L.ncell[0] * (uint32_t) L.ncell[1]));
+    const int aoff = (int) (first - __ldg(L.A.cstart + cell));
+    float c2x = 0.f, c2y = 0.f, c2z = 0.f;
+    if (GEOM == FCFCG_GEOM_SURVEY) {
+      c2x = 2.f * fmaf((float) cx + 0.5f, L.cwf[0], L.lof[0]);
+      c2y = 2.f * fmaf((float) cy + 0.5f, L.cwf[1], L.lof[1]);
+      c2z = 2.f * fmaf((float) cz + 0.5f, L.cwf[2], L.lof[2]);
     }
-    for (int t = 0; t < L.nsten; t++) {
-      const int4 o = __ldg(sten + t);
-      uint32_t cb, code;
-      if (!neighbour(L, w, o, cb, code)) continue;
-      const uint32_t bstart = __ldg(L.B.cstart + cb);
-      const uint32_t bend = __ldg(L.B.cstart + cb + 1);
-      if (bstart == bend || !w.active) continue;
-      const bool self = L.isauto && o.x == 0 && o.y == 0 && o.z == 0;
-      const float4 D = __ldg(stD + t);
-      const float xi = pa.x + D.x, yi = pa.y + D.y, zi = pa.z + D.z;
-      float cbx = 0.f, cby = 0.f, cbz = 0.f;
-      if (GEOM == FCFCG_GEOM_SURVEY) {
-        /* twice the centre of cell B: m = x_a + x_b = 2 c_B + 2 l_b + d */
-        const int qx = w.cx + o.x, qy = w.cy + o.y, qz = w.cz + o.z;
-        cbx = 2.f * fmaf((float) qx + 0.5f, L.cwf[0], L.lof[0]);
-        cby = 2.f * fmaf((float) qy + 0.5f, L.cwf[1], L.lof[1]);
-        cbz = 2.f * fmaf((float) qz + 0.5f, L.cwf[2], L.lof[2]);
+    if (warp == 1) {
+      for (int k = lane; k < m; k += 32) {
+        S.a[k] = ((const float4 *) L.A.l4)[first + k];
+        if (WT) S.aw[k] = ((const int2 *) L.A.wq)[first + k];
       }
-      const int nb = (int) (bend - bstart);
-      for (int j = first_j(w, self, bstart); j < nb; j += w.G) {
-        const uint32_t bj = bstart + (uint32_t) j;
-        const float4 pb = Bl4[bj];
-        const float dx = xi - pb.x, dy = yi - pb.y, dz = zi - pb.z;
-        n_cand++;
-        bool amb = false;
-        int bin = -1;
-        if (BIN == FCFCG_BIN_SPI && GEOM == FCFCG_GEOM_BOX) {
-          const float pi = fabsf(dz);
-          if (!(pi < L.p_lim)) continue;
-          const float sp2 = fmaf(dy, dy, dx * dx);
-          if (!(sp2 < L.s_lim)) continue;
-          const float rs = rsqrtf(sp2);
-          const float s = sp2 * rs;
-          const float E = fmaf(L.K2, sp2, fmaf(L.K1, s, L.K0));
-          amb = !(sp2 >= L.tiny);
-          unsigned sb = ftab_bin(fs, L.fsoff, L.nfs, sp2, E, amb);
-          unsigned pbn = ftab_bin(fp, L.fpoff, L.nfp, pi, L.P0, amb);
-          if (!amb) {
-            if (sb == FCFCG_FTAB_BIN_MASK || pbn == FCFCG_FTAB_BIN_MASK) continue;
-            bin = (int) sb + (int) pbn * L.ns;
-          }
-        } else {
-          const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-          if (!(s2 < L.s_lim)) continue;
-          const float rs = rsqrtf(s2);
-          const float s = s2 * rs;
-          const float E = fmaf(L.K2, s2, fmaf(L.K1, s, L.K0));
-          amb = !(s2 >= L.tiny);
-          if (BIN == FCFCG_BIN_ISO) {
-            unsigned sb = ftab_bin(fs, L.fsoff, L.nfs, s2, E, amb);
-            if (!amb) {
-              if (sb == FCFCG_FTAB_BIN_MASK) continue;
-              bin = (int) sb;
-            }
-          } else if (BIN == FCFCG_BIN_SMU) {
-            float q;
-            if (GEOM == FCFCG_GEOM_BOX) {
-              q = L.fnmu * fabsf(dz) * rs;
+    } else if (warp == 0) {
+      /* neighbour cells of this chunk, laid end to end */
+      uint32_t run = 0;
+      for (int t0 = 0; t0 < L.nsten; t0 += 32) {
+        const int t = t0 + lane;
+        uint32_t nb = 0, bs = 0;
+        if (t < L.nsten) {
+          const int4 o = __ldg(sten + t);
+          int q[3] = {cx + o.x, cy + o.y, cz + o.z};
+          bool ok = true;
+          for (int k = 0; k < 3; k++) {
+            const int n = L.ncell[k];
+            if (GEOM == FCFCG_GEOM_SURVEY) {
+              ok &= (q[k] >= 0) & (q[k] < n);
             } else {
-              const float mx = fmaf(2.f, pb.x, cbx) + dx;
-              const float my = fmaf(2.f, pb.y, cby) + dy;
-              const float mz = fmaf(2.f, pb.z, cbz) + dz;
-              const float dm = fmaf(dz, mz, fmaf(dy, my, dx * mx));
-              const float mm = fmaf(mz, mz, fmaf(my, my, mx * mx));
-              q = L.fnmu * fabsf(dm) * rsqrtf(mm * s2);
-            }
-            const float Eq = fmaf(L.Q1, rs, fmaf(L.Q2, q, L.Q0));
-            int qi = mu_bin(q, Eq, amb);
-            unsigned sb = ftab_bin(fs, L.fsoff, L.nfs, s2, E, amb);
-            if (!amb) {
-              if (sb == FCFCG_FTAB_BIN_MASK || qi >= L.nmu) continue;
-              bin = (int) sb + qi * L.ns;
-            }
-          } else {
-            /* survey (s_perp, pi): pi^2 = (d.m)^2 / |m|^2 */
-            const float mx = fmaf(2.f, pb.x, cbx) + dx;
-            const float my = fmaf(2.f, pb.y, cby) + dy;
-            const float mz = fmaf(2.f, pb.z, cbz) + dz;
-            const float dm = fmaf(dz, mz, fmaf(dy, my, dx * mx));
-            const float mm = fmaf(mz, mz, fmaf(my, my, mx * mx));
-            const float pi2 = __fdividef(dm * dm, mm);
-            const float sp2 = s2 - pi2;
-            const float Ep = fmaf(L.P2, s2, fmaf(L.P1, s, L.P0));
-            unsigned pbn = ftab_bin(fp, L.fpoff, L.nfp, pi2, Ep, amb);
-            unsigned sb = ftab_bin(fs, L.fsoff, L.nfs, sp2 < 0.f ? 0.f : sp2,
-                                   E + Ep, amb);
-            if (!amb) {
-              if (sb == FCFCG_FTAB_BIN_MASK || pbn == FCFCG_FTAB_BIN_MASK) continue;
-              bin = (int) sb + (int) pbn * L.ns;
+              while (q[k] < 0) q[k] += n;
+              while (q[k] >= n) q[k] -= n;
             }
           }
+          if (ok) {
+            const uint32_t cb = ((uint32_t) q[2] * L.ncell[1] + q[1]) * L.ncell[0] + q[0];
+            bs = __ldg(L.B.cstart + cb);
+            nb = __ldg(L.B.cstart + cb + 1) - bs;
+          }
         }
-        if (amb) {
-          n_q++;
-          enqueue<WT>(L, w.ai, bj, code, h32, h64, n_inline);
-          continue;
+        uint32_t inc = nb;
+        for (int s = 1; s < 32; s <<= 1) {
+          uint32_t u = __shfl_up_sync(FULLMASK, inc, s);
+          if (lane >= s) inc += u;
         }
-        n_in++;
+        if (t < L.nsten) {
+          S.pre[t] = run + inc - nb;
+          S.bst[t] = bs;
+        }
+        run += __shfl_sync(FULLMASK, inc, 31);
+      }
+      if (lane == 0) S.pre[L.nsten] = run;
+    }
+    __syncthreads();
+    const uint32_t total = S.pre[L.nsten];
+    if (warp == 0 && lane == 0) n_cand += (unsigned long long) m * total;
+    uint32_t n_in = 0, n_q = 0;
+
+    for (uint32_t base = (uint32_t) warp * 32; base < total;
+         base += (uint32_t) nwarp * 32) {
+      const uint32_t p = base + (uint32_t) lane;
+      float bx = 0.f, by = 0.f, bz = 0.f;
+      int ilim = 0;
+      if (p < total) {
+        /* neighbour cell of position p: last t with pre[t] <= p */
+        int lo = 0, hi = L.nsten;
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (S.pre[mid] <= p) lo = mid;
+          else hi = mid;
+        }
+        const int t = lo;
+        const uint32_t jc = p - S.pre[t];
+        const uint32_t bj = S.bst[t] + jc;
+        const float4 pb = Bl4[bj];
+        const float4 D = __ldg(stD + t);
+        bx = pb.x - D.x;
+        by = pb.y - D.y;
+        bz = pb.z - D.z;
+        ilim = m;
+        if (L.isauto && t == L.tzero) ilim = min(m, (int) jc - aoff);
+        S.b[lane] = make_float4(bx, by, bz, __uint_as_float(bj));
+        S.bt[lane] = (uint16_t) t;
         if (WT) {
-          const float wblo = L.B.wlo[bj];
-          const long long v = fix_prod(pa.w, walo, pb.w, wblo, twoF);
-          if (L.hist_smem) hist_add_fix(h64, L.gwt, bin, v);
-          else add128(L.gwt + 2 * bin, v);
-        } else {
-          if (L.hist_smem) hist_add_count(h32, L.gcnt, bin);
-          else atomicAdd(L.gcnt + bin, 1ull);
+          const int2 wq = Bwq[bj];
+          S.bw[lane] = make_float4(pb.w, __int_as_float(wq.x),
+                                   __int_as_float(wq.y), 0.f);
         }
       }
+      /* compare with every chunk point (two 32-point halves) */
+      const uint32_t m0 = scan_chunk<GEOM, BIN>(L, S.a, 0, min(m, 32), ilim,
+                                                bx, by, bz);
+      const uint32_t m1 = (m > 32) ? scan_chunk<GEOM, BIN>(L, S.a, 32, m,
+                                                          ilim, bx, by, bz)
+                                   : 0u;
+      /* compact the block's in-range pairs into the queue, QCAP per round */
+      const uint32_t cnt = __popc(m0) + __popc(m1);
+      uint32_t inc = cnt;
+      for (int s = 1; s < 32; s <<= 1) {
+        uint32_t u = __shfl_up_sync(FULLMASK, inc, s);
+        if (lane >= s) inc += u;
+      }
+      const uint32_t tot = __shfl_sync(FULLMASK, inc, 31);
+      const uint32_t excl = inc - cnt;
+      for (uint32_t r0 = 0; r0 < tot; r0 += QCAP) {
+        /* this lane's entries with positions in [r0, r0 + QCAP) */
+        uint32_t lo = excl > r0 ? excl : r0;
+        uint32_t hi = excl + cnt < r0 + QCAP ? excl + cnt : r0 + QCAP;
+        if (lo < hi) {
+          uint32_t b0 = m0, b1 = m1;
+          for (uint32_t sk = lo - excl; sk > 0; sk--) {
+            if (b0) b0 &= b0 - 1;
+            else b1 &= b1 - 1;
+          }
+          for (uint32_t pos = lo; pos < hi; pos++) {
+            uint32_t i;
+            if (b0) {
+              i = (uint32_t) (__ffs(b0) - 1);
+              b0 &= b0 - 1;
+            } else {
+              i = 32u + (uint32_t) (__ffs(b1) - 1);
+              b1 &= b1 - 1;
+            }
+            S.q[pos - r0] = (uint16_t) (i | ((uint32_t) lane << 6));
+          }
+        }
+        __syncwarp();
+        const uint32_t nr = (tot - r0 < QCAP) ? tot - r0 : QCAP;
+        /* pass k: lane l takes entry l * np + k, so that the lanes of a
+         * pass hold pairs of different neighbour points (different bins) */
+        const uint32_t np = (nr + 31) >> 5;
+        for (uint32_t k = 0; k < np; k++) {
+          const uint32_t e = (uint32_t) lane * np + k;
+          if (e < nr)
+            bin_pair<GEOM, BIN, WT>(L, S, S.q[e], first, cx, cy, cz, c2x, c2y,
+                                    c2z, fs, fp, h, n_in, n_q, n_inline);
+        }
+        __syncwarp();
+      }
     }
+    n_in64 += n_in;
+    n_q64 += n_q;
   }
 
   /* statistics */
   for (int o = 16; o > 0; o >>= 1) {
-    n_cand += __shfl_xor_sync(FULLMASK, n_cand, o);
-    n_in += __shfl_xor_sync(FULLMASK, n_in, o);
-    n_q += __shfl_xor_sync(FULLMASK, n_q, o);
+    n_in64 += __shfl_xor_sync(FULLMASK, n_in64, o);
+    n_q64 += __shfl_xor_sync(FULLMASK, n_q64, o);
     n_inline += __shfl_xor_sync(FULLMASK, n_inline, o);
   }
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(L.stats + 0, n_cand);
-    atomicAdd(L.stats + 1, n_in);
-    atomicAdd(L.stats + 2, n_q);
+  if (lane == 0) {
+    if (warp == 0) atomicAdd(L.stats + 0, n_cand);
+    atomicAdd(L.stats + 1, n_in64);
+    atomicAdd(L.stats + 2, n_q64);
     atomicAdd(L.stats + 3, n_inline);
   }
   __syncthreads();
   if (L.hist_smem) {
     for (long i = threadIdx.x; i < L.ntot; i += blockDim.x) {
       if (WT) {
-        long long v = h64[i];
+        const long long v = ((long long) ((int *) h)[L.ntot + i] << 32) +
+                            (long long) h[i];
         if (v) add128(L.gwt + 2 * i, v);
       } else {
-        uint32_t v = h32[i];
+        uint32_t v = h[i];
         if (v) atomicAdd(L.gcnt + i, (unsigned long long) v);
       }
     }
@@ -585,7 +866,6 @@ k_count64(const fcfcg_launch L) {
 /* FP64 recheck of queued pairs. */
 template <int WT>
 __global__ void k_recheck(const fcfcg_launch L, uint32_t nq) {
-  const float twoF = ldexpf(1.f, L.fixF);
   unsigned long long n_in = 0;
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq;
        q += gridDim.x * blockDim.x) {
@@ -593,13 +873,8 @@ __global__ void k_recheck(const fcfcg_launch L, uint32_t nq) {
     int bin = ref_bin_pair(L, e.x, e.y, e.z);
     if (bin < 0) continue;
     n_in++;
-    if (WT) {
-      const float ah = ((const float4 *) L.A.l4)[e.x].w, al = L.A.wlo[e.x];
-      const float bh = ((const float4 *) L.B.l4)[e.y].w, bl = L.B.wlo[e.y];
-      add128(L.gwt + 2 * bin, fix_prod(ah, al, bh, bl, twoF));
-    } else {
-      atomicAdd(L.gcnt + bin, 1ull);
-    }
+    if (WT) add128(L.gwt + 2 * bin, fix_prod_pair(L, e.x, e.y));
+    else atomicAdd(L.gcnt + bin, 1ull);
   }
   for (int o = 16; o > 0; o >>= 1)
     n_in += __shfl_xor_sync(FULLMASK, n_in, o);
@@ -636,13 +911,17 @@ extern "C" int fcfcg_k_count(void *stream, const fcfcg_launch *L,
     int precision, int nsm, size_t *smem_used) {
   kfun_t f;
   size_t smem;
+  int threads;
   if (precision == FCFCG_PREC_FP64) {
     f = pick64(L->geometry, L->withwt);
     smem = L->hist_smem ? (size_t) L->ntot * (L->withwt ? 8 : 4) : 0;
+    threads = CT_THREADS;
   } else {
     f = pick32(L->geometry, L->bintype, L->withwt);
     size_t tab = (((size_t) (L->nfs + L->nfp) * 2) + 15) & ~(size_t) 15;
     smem = tab + (L->hist_smem ? (size_t) L->ntot * (L->withwt ? 8 : 4) : 0);
+    smem = ((smem + 15) & ~(size_t) 15) + stage_bytes(L->nsten, L->withwt);
+    threads = CT32_THREADS;
   }
   if (!f) return (int) cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute((const void *) f,
@@ -650,12 +929,17 @@ extern "C" int fcfcg_k_count(void *stream, const fcfcg_launch *L,
   if (e) return (int) e;
   int per_sm = 0;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *) f,
-                                                    CT_THREADS, smem);
+                                                    threads, smem);
   if (e) return (int) e;
   if (per_sm < 1) return (int) cudaErrorInvalidConfiguration;
   if (smem_used) *smem_used = smem;
-  f<<<nsm * per_sm, CT_THREADS, smem, (cudaStream_t) stream>>>(*L);
+  f<<<nsm * per_sm, threads, smem, (cudaStream_t) stream>>>(*L);
   return (int) cudaGetLastError();
+}
+
+/* Shared memory the FP32 kernel needs beyond its histogram. */
+extern "C" size_t fcfcg_k_count32_stage(int nsten, int withwt) {
+  return stage_bytes(nsten, withwt);
 }
 
 extern "C" int fcfcg_k_recheck(void *stream, const fcfcg_launch *L,

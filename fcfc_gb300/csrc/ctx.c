@@ -24,7 +24,8 @@ typedef struct {
   double bmin[3], bmax[3];         /* bounding box (rescaled) */
   /* sorted copy for the current grid */
   size_t scap;
-  float *l4, *wlo;
+  float *l4;
+  int *wq;
   double *sx, *sy, *sz, *ss, *sw;
   uint32_t *sid, *cell_of;
   uint32_t *cstart;
@@ -56,6 +57,7 @@ struct fcfcg_ctx {
   void *h_pinned;
   size_t h_pinned_cap;
   fcfcg_stats stats;
+  uint64_t launches;
   cudaEvent_t ev[5];
   int sten[4 * FCFCG_MAX_STENCIL];
   float stD[4 * FCFCG_MAX_STENCIL];
@@ -140,7 +142,7 @@ static int upload(fcfcg_ctx *c, void **dst, const void *src, size_t bytes) {
 }
 
 static void slot_free(slot_t *s) {
-  void *p[] = {s->x, s->y, s->z, s->s, s->w, s->l4, s->wlo, s->sx, s->sy,
+  void *p[] = {s->x, s->y, s->z, s->s, s->w, s->l4, s->wq, s->sx, s->sy,
                s->sz, s->ss, s->sw, s->sid, s->cell_of, s->cstart};
   for (size_t i = 0; i < sizeof p / sizeof p[0]; i++)
     if (p[i]) cudaFree(p[i]);
@@ -233,7 +235,7 @@ int fcfcg_create(const fcfcg_binning *cfg, int device, fcfcg_ctx **out) {
   CK(cudaMalloc((void **) &c->d_bbox, sizeof(unsigned long long) * 6));
   CK(cudaMalloc((void **) &c->d_head, sizeof(uint32_t) * 4));
   c->d_qcount = c->d_head + 1;
-  c->qcap = (size_t) 1 << 22;
+  c->qcap = (size_t) 1 << 25;   /* 32M pairs, 512 MiB */
   CK(cudaMalloc((void **) &c->d_queue, sizeof(uint32_t) * 4 * c->qcap));
   CK(cudaStreamSynchronize(c->stream));
   return FCFCG_OK;
@@ -337,6 +339,7 @@ static int load_common(fcfcg_ctx *c, int slot, size_t n, const double *x,
   CK(cudaMemsetAsync(wbits, 0, sizeof(unsigned long long), c->stream));
   CKK(fcfcg_k_prep(c->stream, n, ix, iy, iz, iw, c->bins.rescale, survey,
                    s->x, s->y, s->z, s->s, s->w, wbits));
+  c->launches += n ? 2 : 0;
   /* bounding box of the rescaled catalogue and max |w| */
   unsigned long long init[6] = {~0ull, ~0ull, ~0ull, 0, 0, 0};
   CK(cudaMemcpyAsync(c->d_bbox, init, sizeof init, cudaMemcpyHostToDevice,
@@ -502,7 +505,9 @@ static int grid_setup(fcfcg_ctx *c, grid_t *g, const slot_t *A,
   for (;;) {
     double tot = 1;
     for (int d = 0; d < 3; d++) {
-      double cwt = g->reach[d] / k * scale;
+      /* cells a little wider than reach / k, so that k layers of neighbours
+       * cover every separation below the reach */
+      double cwt = g->reach[d] / k * scale * (1 + 1e-6);
       int n = (int) floor(ext[d] / cwt);
       if (n < 1) n = 1;
       if (n > 4096) n = 4096;
@@ -525,7 +530,7 @@ static int stencil_build(fcfcg_ctx *c, const grid_t *g, int isauto, int *sten,
     float *stD, int *nsten, double *dmax) {
   const fcfcg_bins *b = &c->bins;
   const int box = (b->geometry == FCFCG_GEOM_BOX);
-  const double margin = 1 + 1e-6;
+  const double margin = 1 + 1e-9;
   int r[3];
   for (int d = 0; d < 3; d++) {
     r[d] = (int) ceil(g->reach[d] * margin / g->cw[d]);
@@ -593,12 +598,12 @@ static int slot_grid(fcfcg_ctx *c, slot_t *s, const grid_t *g) {
     return FCFCG_OK;
   const size_t n = s->n, m = n ? n : 1;
   if (s->scap < m) {
-    void *p[] = {s->l4, s->wlo, s->sx, s->sy, s->sz, s->ss, s->sw, s->sid,
+    void *p[] = {s->l4, s->wq, s->sx, s->sy, s->sz, s->ss, s->sw, s->sid,
                  s->cell_of};
     for (size_t i = 0; i < sizeof p / sizeof p[0]; i++)
       if (p[i]) cudaFree(p[i]);
     CK(cudaMalloc((void **) &s->l4, sizeof(float) * 4 * m));
-    CK(cudaMalloc((void **) &s->wlo, sizeof(float) * m));
+    CK(cudaMalloc((void **) &s->wq, sizeof(int) * 2 * m));
     CK(cudaMalloc((void **) &s->sx, sizeof(double) * m));
     CK(cudaMalloc((void **) &s->sy, sizeof(double) * m));
     CK(cudaMalloc((void **) &s->sz, sizeof(double) * m));
@@ -620,9 +625,10 @@ static int slot_grid(fcfcg_ctx *c, slot_t *s, const grid_t *g) {
   const int survey = (c->bins.geometry == FCFCG_GEOM_SURVEY);
   CKK(fcfcg_k_grid(c->stream, n, s->x, s->y, s->z, survey ? s->s : NULL,
                    s->w, s->has_w, s->wexp, g->n, g->cw, g->lo, s->cell_of,
-                   s->cstart, c->cfill, c->scan_tmp, st, s->l4, s->wlo,
+                   s->cstart, c->cfill, c->scan_tmp, st, s->l4, s->wq,
                    s->sx, s->sy, s->sz, survey ? s->ss : NULL, s->sw,
                    s->sid));
+  c->launches += n ? 5 : 3;
   memcpy(s->gsig_n, g->n, sizeof g->n);
   memcpy(s->gsig_cw, g->cw, sizeof g->cw);
   memcpy(s->gsig_lo, g->lo, sizeof g->lo);
@@ -692,6 +698,7 @@ static int fp32_bounds(const fcfcg_ctx *c, const grid_t *g, double dmax,
   } else {
     L->s_lim = (float) (smax2 + Es + 1e-6 * (1 + smax2));
   }
+  L->Emax = (float) (Es * 1.01);
   if (!(Es < 0.45) || !(Ep < 0.45)) return -1;
   if (b->s.nbin > FCFCG_FTAB_MAXBIN || !b->s.ftab) return -1;
   if (b->bintype == FCFCG_BIN_SPI &&
@@ -764,11 +771,6 @@ int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
   if (rc) return rc;
   rc = upload(c, (void **) &c->d_stenD, stD, sizeof(float) * 4 * nsten);
   if (rc) return rc;
-  uint32_t nchunk = 0;
-  CKK(fcfcg_k_chunks(c->stream, A->cstart, ncell, c->cchunk, c->scan_tmp, st,
-                     c->chunks, &nchunk));
-  CK(cudaEventRecord(c->ev[1], c->stream));
-
   fcfcg_launch L;
   memset(&L, 0, sizeof L);
   L.geometry = b->geometry;
@@ -784,17 +786,18 @@ int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
     L.lof[d] = (float) g.lo[d];
   }
   L.nsten = nsten;
+  L.tzero = -1;
+  for (int t = 0; t < nsten; t++)
+    if (!sten[4 * t] && !sten[4 * t + 1] && !sten[4 * t + 2]) L.tzero = t;
   L.sten = c->d_sten;
   L.stenD = c->d_stenD;
-  CK(cudaStreamSynchronize(c->stream));
-  L.nchunk = nchunk;
   L.chunks = c->chunks;
   L.chunk_head = c->d_head;
   const slot_t *S[2] = {A, B};
   fcfcg_dcat *D[2] = {&L.A, &L.B};
   for (int q = 0; q < 2; q++) {
     D[q]->l4 = S[q]->l4;
-    D[q]->wlo = S[q]->wlo;
+    D[q]->wq = S[q]->wq;
     D[q]->x = S[q]->sx;
     D[q]->y = S[q]->sy;
     D[q]->z = S[q]->sz;
@@ -849,9 +852,26 @@ int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
   size_t tabbytes = (prec == FCFCG_PREC_FP32_RECHECK)
       ? (((size_t) (L.nfs + L.nfp) * 2 + 15) & ~(size_t) 15) : 0;
   size_t hbytes = (size_t) b->ntot * (withwt ? 8 : 4);
-  L.hist_smem = (tabbytes + hbytes <= 160 * 1024);
-  if (tabbytes > 160 * 1024) prec = FCFCG_PREC_FP64;
+  size_t stage = (prec == FCFCG_PREC_FP32_RECHECK)
+      ? fcfcg_k_count32_stage(nsten, withwt) : 0;
+  if (tabbytes + stage > 200 * 1024) {
+    prec = FCFCG_PREC_FP64;
+    tabbytes = 0;
+    stage = 0;
+  }
+  L.hist_smem = (tabbytes + stage + hbytes <= 200 * 1024);
 
+  /* work chunks: 64 points per CTA in the FP32 kernel, 32 per warp in the
+   * FP64 kernel */
+  uint32_t nchunk = 0;
+  const uint32_t clen = (prec == FCFCG_PREC_FP32_RECHECK) ? FCFCG_CHUNK32
+                                                          : FCFCG_CHUNK;
+  CKK(fcfcg_k_chunks(c->stream, A->cstart, ncell, clen, c->cchunk,
+                     c->scan_tmp, st, c->chunks, &nchunk));
+  c->launches += 5;
+  CK(cudaEventRecord(c->ev[1], c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  L.nchunk = nchunk;
   CK(cudaMemsetAsync(c->d_cnt, 0, sizeof(unsigned long long) * b->ntot,
                      c->stream));
   CK(cudaMemsetAsync(c->d_wt, 0, sizeof(unsigned long long) * 2 * b->ntot,
@@ -862,6 +882,7 @@ int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
   CK(cudaEventRecord(c->ev[2], c->stream));
   size_t smem = 0;
   CKK(fcfcg_k_count(c->stream, &L, prec, c->nsm, &smem));
+  c->launches += 1;
   CK(cudaEventRecord(c->ev[3], c->stream));
   uint32_t nq = 0;
   if (prec == FCFCG_PREC_FP32_RECHECK) {
@@ -870,6 +891,7 @@ int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
     CK(cudaStreamSynchronize(c->stream));
     if (nq > c->qcap) nq = (uint32_t) c->qcap;
     CKK(fcfcg_k_recheck(c->stream, &L, nq));
+    c->launches += nq ? 1 : 0;
   }
   CK(cudaEventRecord(c->ev[4], c->stream));
   /* results */
@@ -920,6 +942,7 @@ int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
   o->nstencil = nsten;
   o->nchunks = nchunk;
   o->precision_used = prec;
+  o->launches = c->launches;
   (void) smem;
   return FCFCG_OK;
 }

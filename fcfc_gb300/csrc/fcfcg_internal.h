@@ -15,7 +15,8 @@ extern "C" {
 #endif
 
 #define FCFCG_MAX_SLOT 8
-#define FCFCG_CHUNK 32            /* points of one cell a warp holds */
+#define FCFCG_CHUNK 32            /* chunk length of the FP64 kernel */
+#define FCFCG_CHUNK32 64          /* chunk length of the FP32 kernel */
 #define FCFCG_MAX_STENCIL 4096
 #define FCFCG_FTAB_BIN_MASK 0x1FFFu
 #define FCFCG_FTAB_LO 0x2000u     /* an edge lies in [i - 1/2, i] */
@@ -66,8 +67,9 @@ const double *fcfcg_ctx_box_raw(const fcfcg_ctx *c);
 
 typedef struct {
   /* sorted catalogue on the device */
-  const float *l4;       /* float4 per point: local x, y, z, scaled w_hi */
-  const float *wlo;      /* scaled w_lo */
+  const float *l4;       /* float4 per point: local x, y, z, scaled weight */
+  const int *wq;         /* int2 per point: round(w 2^30) and the float bits
+                            of the remainder, w scaled to |w| <= 1 */
   const double *x, *y, *z, *s, *w;   /* rescaled FP64, |x|^2, weight */
   const uint32_t *id;    /* input index */
   const uint32_t *cstart;/* ncell + 1 */
@@ -99,6 +101,8 @@ typedef struct {
   float P0, P1, P2;            /* E(pi) (box) or E(pi^2) (survey) */
   float Q0, Q1, Q2;            /* E(q), q = nmu mu: Q1 / s + Q2 q + Q0 */
   float tiny;                  /* s^2 below: always recheck */
+  float Emax;                  /* E at the top of the s axis (iso, spi) */
+  int tzero;                   /* stencil index of the zero offset */
   float fnmu;
   /* FP64 reference binning */
   const uint16_t *rs, *rp;
@@ -131,11 +135,12 @@ int fcfcg_k_grid(void *stream, size_t n, const double *x, const double *y,
     const double *z, const double *s, const double *w, int has_w, int wexp,
     const int ncell[3], const double cw[3], const double lo[3],
     uint32_t *cell_of, uint32_t *cstart, uint32_t *cfill, uint32_t *scan_tmp,
-    size_t scan_tmp_len, float *l4, float *wlo, double *sx, double *sy,
+    size_t scan_tmp_len, float *l4, int *wq, double *sx, double *sy,
     double *sz, double *ss, double *sw, uint32_t *sid);
 int fcfcg_k_chunks(void *stream, const uint32_t *cstart, uint32_t ncell,
-    uint32_t *cchunk, uint32_t *scan_tmp, size_t scan_tmp_len,
+    uint32_t clen, uint32_t *cchunk, uint32_t *scan_tmp, size_t scan_tmp_len,
     uint32_t *chunks, uint32_t *nchunk_out);
+size_t fcfcg_k_count32_stage(int nsten, int withwt);
 int fcfcg_k_bbox(void *stream, size_t n, const double *x, const double *y,
     const double *z, unsigned long long *bits6);
 int fcfcg_k_count(void *stream, const fcfcg_launch *L, int precision,

@@ -241,7 +241,7 @@ __global__ void k_scatter(size_t n, const double *__restrict__ x,
     int wexp, int nx, int ny, double cwx, double cwy, double cwz, double lox,
     double loy, double loz, const uint32_t *__restrict__ cell_of,
     const uint32_t *__restrict__ cstart, uint32_t *__restrict__ cfill,
-    float4 *__restrict__ l4, float *__restrict__ wlo, double *__restrict__ sx,
+    float4 *__restrict__ l4, int2 *__restrict__ wq, double *__restrict__ sx,
     double *__restrict__ sy, double *__restrict__ sz, double *__restrict__ ss,
     double *__restrict__ sw, uint32_t *__restrict__ sid) {
   for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n;
@@ -256,15 +256,16 @@ __global__ void k_scatter(size_t n, const double *__restrict__ x,
     double ccy = loy + (cy + 0.5) * cwy;
     double ccz = loz + (cz + 0.5) * cwz;
     double wv = has_w ? w[i] : 1.0;
-    double ws = ldexp(wv, -wexp);
-    float whi = (float) ws;
+    double ws = ldexp(wv, -wexp);            /* |ws| <= 1 */
+    int wi = (int) __double2ll_rn(ws * 1073741824.0);
+    float wr = (float) (ws - (double) wi * (1.0 / 1073741824.0));
     float4 v;
     v.x = (float) (a - ccx);
     v.y = (float) (b - ccy);
     v.z = (float) (d - ccz);
-    v.w = whi;
+    v.w = (float) ws;
     l4[pos] = v;
-    wlo[pos] = (float) (ws - (double) whi);
+    wq[pos] = make_int2(wi, __float_as_int(wr));
     sx[pos] = a;
     sy[pos] = b;
     sz[pos] = d;
@@ -278,7 +279,7 @@ extern "C" int fcfcg_k_grid(void *stream, size_t n, const double *x,
     const double *y, const double *z, const double *s, const double *w,
     int has_w, int wexp, const int ncell[3], const double cw[3],
     const double lo[3], uint32_t *cell_of, uint32_t *cstart, uint32_t *cfill,
-    uint32_t *scan_tmp, size_t scan_tmp_len, float *l4, float *wlo,
+    uint32_t *scan_tmp, size_t scan_tmp_len, float *l4, int *wq,
     double *sx, double *sy, double *sz, double *ss, double *sw,
     uint32_t *sid) {
   cudaStream_t st = (cudaStream_t) stream;
@@ -299,43 +300,46 @@ extern "C" int fcfcg_k_grid(void *stream, size_t n, const double *x,
     k_scatter<<<grid_for(n, PREP_THREADS), PREP_THREADS, 0, st>>>(
         n, x, y, z, s, w, has_w, wexp, ncell[0], ncell[1], cw[0], cw[1],
         cw[2], lo[0], lo[1], lo[2], cell_of, cstart, cfill, (float4 *) l4,
-        wlo, sx, sy, sz, ss, sw, sid);
+        (int2 *) wq, sx, sy, sz, ss, sw, sid);
     if ((e = cudaGetLastError())) return (int) e;
   }
   return 0;
 }
 
-/* Work chunks: every cell is cut into pieces of at most FCFCG_CHUNK points. */
+/* Work chunks: every cell is cut into pieces of at most clen points, as
+ * evenly as possible. */
 __global__ void k_chunk_count(const uint32_t *__restrict__ cstart,
-    uint32_t ncell, uint32_t *__restrict__ cchunk) {
+    uint32_t ncell, uint32_t clen, uint32_t *__restrict__ cchunk) {
   for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
        c += gridDim.x * blockDim.x) {
     uint32_t m = cstart[c + 1] - cstart[c];
-    cchunk[c] = (m + FCFCG_CHUNK - 1) / FCFCG_CHUNK;
+    cchunk[c] = (m + clen - 1) / clen;
   }
 }
 
 __global__ void k_chunk_emit(const uint32_t *__restrict__ cstart,
-    uint32_t ncell, const uint32_t *__restrict__ coff,
+    uint32_t ncell, uint32_t clen, const uint32_t *__restrict__ coff,
     uint4 *__restrict__ chunks) {
   for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
        c += gridDim.x * blockDim.x) {
     uint32_t a = cstart[c], m = cstart[c + 1] - a;
     uint32_t k = coff[c];
-    for (uint32_t q = 0; q < m; q += FCFCG_CHUNK) {
-      uint32_t len = (m - q < FCFCG_CHUNK) ? m - q : FCFCG_CHUNK;
-      chunks[k++] = make_uint4(c, a + q, len, 0);
+    uint32_t nch = (m + clen - 1) / clen;
+    for (uint32_t q = 0; q < nch; q++) {
+      uint32_t b0 = (uint32_t) (((unsigned long long) m * q) / nch);
+      uint32_t b1 = (uint32_t) (((unsigned long long) m * (q + 1)) / nch);
+      chunks[k++] = make_uint4(c, a + b0, b1 - b0, 0);
     }
   }
 }
 
 extern "C" int fcfcg_k_chunks(void *stream, const uint32_t *cstart,
-    uint32_t ncell, uint32_t *cchunk, uint32_t *scan_tmp,
+    uint32_t ncell, uint32_t clen, uint32_t *cchunk, uint32_t *scan_tmp,
     size_t scan_tmp_len, uint32_t *chunks, uint32_t *nchunk_out) {
   cudaStream_t st = (cudaStream_t) stream;
   (void) scan_tmp_len;
   k_chunk_count<<<grid_for(ncell, PREP_THREADS), PREP_THREADS, 0, st>>>(
-      cstart, ncell, cchunk);
+      cstart, ncell, clen, cchunk);
   cudaError_t e = cudaGetLastError();
   if (e) return (int) e;
   /* cchunk holds ncell + 1 slots: scan in place via the offset array */
@@ -344,7 +348,7 @@ extern "C" int fcfcg_k_chunks(void *stream, const uint32_t *cstart,
   if (r) return r;
   if (chunks) {
     k_chunk_emit<<<grid_for(ncell, PREP_THREADS), PREP_THREADS, 0, st>>>(
-        cstart, ncell, coff, (uint4 *) chunks);
+        cstart, ncell, clen, coff, (uint4 *) chunks);
     if ((e = cudaGetLastError())) return (int) e;
   }
   if (nchunk_out)

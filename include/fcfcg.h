@@ -116,6 +116,7 @@ typedef struct {
   int nstencil;
   uint64_t nchunks;
   int precision_used;    /* FCFCG_PREC_*: FP32 windows too wide fall to FP64 */
+  uint64_t launches;     /* kernels launched by this context since creation */
 } fcfcg_stats;
 
 const char *fcfcg_strerror(int err);

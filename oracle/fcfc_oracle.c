@@ -540,7 +540,8 @@ static int fco_grid_build(fco_grid *g, const fco_cat *c) {
 }
 
 /*
- * Count pairs.  mode 0: cell grid; mode 1: brute force over all pairs.
+ * Count pairs.  mode 0: cell grid with cells of side s_max; mode 1: brute
+ * force over all pairs; mode k >= 2: cells of side s_max / k.
  * isauto: unordered pairs of catalogue A with itself (counted once each,
  * as count_pairs does before eval_pairs doubles them).
  * Outputs: icnt (unweighted) or wcnt (weighted), ntot entries, zeroed here.
@@ -593,9 +594,17 @@ int fco_count(const fco_bins *b, size_t na, const double *ax, const double *ay,
       }
     }
   } else {
-    /* Grid with cell side >= s_max; images come from the cell offsets. */
+    /* Grid with cells of side >= reach / kc and a stencil of cell offsets
+     * pruned by the smallest distance between the two cells; images come
+     * from the offsets, so small boxes (few cells per side) stay correct. */
+    const int kc = (mode >= 2) ? mode : 1;
     fco_grid g;
     memset(&g, 0, sizeof g);
+    double reach[3] = {smax, smax, smax};
+    if (!b->survey && b->bintype == FCO_BIN_SPI) {
+      reach[0] = reach[1] = b->sbin[b->ns] * (1 + 1e-9);
+      reach[2] = b->pbin[b->np] * (1 + 1e-9);
+    }
     if (b->survey) {
       double lo[3], hi[3];
       for (int k = 0; k < 3; k++) { lo[k] = INFINITY; hi[k] = -INFINITY; }
@@ -611,7 +620,7 @@ int fco_count(const fco_bins *b, size_t na, const double *ax, const double *ay,
       for (int k = 0; k < 3; k++) {
         if (!(hi[k] >= lo[k])) { lo[k] = 0; hi[k] = 1; }
         double ext = hi[k] - lo[k];
-        int n = (int) (ext / smax);
+        int n = (int) (ext / (reach[k] / kc * (1 + 1e-6)));
         if (n < 1) n = 1;
         if (n > 512) n = 512;
         g.n[k] = n; g.lo[k] = lo[k];
@@ -619,7 +628,7 @@ int fco_count(const fco_bins *b, size_t na, const double *ax, const double *ay,
       }
     } else {
       for (int k = 0; k < 3; k++) {
-        int n = (int) (b->bsize[k] / smax);
+        int n = (int) (b->bsize[k] / (reach[k] / kc * (1 + 1e-6)));
         if (n < 1) n = 1;
         if (n > 512) n = 512;
         g.n[k] = n; g.lo[k] = 0; g.cw[k] = b->bsize[k] / n;
@@ -630,18 +639,40 @@ int fco_count(const fco_bins *b, size_t na, const double *ax, const double *ay,
     if (isauto) gb = g;
     else if (fco_grid_build(&gb, &B)) { fco_grid_free(&g); goto oom; }
 
-    /* Offsets: along each axis -1..1 when the axis has >= 3 cells, otherwise
-     * every distinct image an in-range pair can use. */
-    int off[3][8], noff[3];
+    /* stencil */
+    int r[3];
     for (int k = 0; k < 3; k++) {
-      noff[k] = 0;
-      if (b->survey || g.n[k] >= 3) {
-        off[k][noff[k]++] = -1; off[k][noff[k]++] = 0; off[k][noff[k]++] = 1;
-      } else {
-        /* n = 1 or 2: offsets reaching every image within one box side */
-        for (int o = -g.n[k]; o <= g.n[k]; o++) off[k][noff[k]++] = o;
-      }
+      r[k] = (int) ceil(reach[k] * (1 + 1e-9) / g.cw[k]);
+      if (b->survey && r[k] > g.n[k] - 1) r[k] = g.n[k] - 1;
     }
+    int nst = 0;
+    int *st = malloc(sizeof(int) * 3 * (2 * r[0] + 1) * (2 * r[1] + 1) *
+                     (2 * r[2] + 1));
+    if (!st) { fco_grid_free(&g); if (!isauto) fco_grid_free(&gb); goto oom; }
+    for (int oz = -r[2]; oz <= r[2]; oz++)
+      for (int oy = -r[1]; oy <= r[1]; oy++)
+        for (int ox = -r[0]; ox <= r[0]; ox++) {
+          int o[3] = {ox, oy, oz};
+          if (isauto) {
+            int sgn = oz ? oz : (oy ? oy : ox);
+            if (sgn < 0) continue;
+          }
+          double gap[3];
+          for (int k = 0; k < 3; k++) {
+            int a = abs(o[k]);
+            gap[k] = (a > 0 ? a - 1 : 0) * g.cw[k];
+          }
+          if (!b->survey && b->bintype == FCO_BIN_SPI) {
+            if (gap[2] > reach[2] * (1 + 1e-6)) continue;
+            if (gap[0] * gap[0] + gap[1] * gap[1] >
+                reach[0] * reach[0] * (1 + 1e-6)) continue;
+          } else if (gap[0] * gap[0] + gap[1] * gap[1] + gap[2] * gap[2] >
+                     smax * smax * (1 + 1e-6)) {
+            continue;
+          }
+          st[3 * nst] = ox; st[3 * nst + 1] = oy; st[3 * nst + 2] = oz;
+          nst++;
+        }
     const size_t nc = (size_t) g.n[0] * g.n[1] * g.n[2];
 #pragma omp parallel for schedule(dynamic, 4) num_threads(nth)
     for (size_t ca = 0; ca < nc; ca++) {
@@ -652,32 +683,25 @@ int fco_count(const fco_bins *b, size_t na, const double *ax, const double *ay,
 #endif
       int64_t *hi = ih + (size_t) t * ntot;
       double *hw = wh + (size_t) t * ntot;
+      if (g.start[ca] == g.start[ca + 1]) continue;
       int c[3] = {(int) (ca % g.n[0]), (int) ((ca / g.n[0]) % g.n[1]),
           (int) (ca / ((size_t) g.n[0] * g.n[1]))};
-      for (int u = 0; u < noff[2]; u++)
-      for (int v = 0; v < noff[1]; v++)
-      for (int s = 0; s < noff[0]; s++) {
-        int o[3] = {off[0][s], off[1][v], off[2][u]};
-        /* auto: each unordered image once -- offsets > 0 lexicographically
-         * (z, y, x), plus the zero offset as a triangle. */
-        int zero = (o[0] == 0 && o[1] == 0 && o[2] == 0);
-        if (isauto && !zero) {
-          int sgn = o[2] ? o[2] : (o[1] ? o[1] : o[0]);
-          if (sgn < 0) continue;
-        }
+      for (int q = 0; q < nst; q++) {
+        const int *o = st + 3 * q;
+        const int zero = (o[0] == 0 && o[1] == 0 && o[2] == 0);
         int cb[3];
         double sh[3] = {0, 0, 0};
         int skip = 0;
         for (int k = 0; k < 3; k++) {
-          int q = c[k] + o[k];
+          int v = c[k] + o[k];
           if (b->survey) {
-            if (q < 0 || q >= g.n[k]) { skip = 1; break; }
+            if (v < 0 || v >= g.n[k]) { skip = 1; break; }
           } else {
-            int w = (int) floor((double) q / g.n[k]);
-            q -= w * g.n[k];
+            int w = (int) floor((double) v / g.n[k]);
+            v -= w * g.n[k];
             sh[k] = -(double) w * b->bsize[k];
           }
-          cb[k] = q;
+          cb[k] = v;
         }
         if (skip) continue;
         size_t cbid = ((size_t) cb[2] * g.n[1] + cb[1]) * g.n[0] + cb[0];
@@ -695,6 +719,7 @@ int fco_count(const fco_bins *b, size_t na, const double *ax, const double *ay,
         }
       }
     }
+    free(st);
     fco_grid_free(&g);
     if (!isauto) fco_grid_free(&gb);
   }

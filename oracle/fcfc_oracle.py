@@ -31,7 +31,7 @@ def build(force: bool = False) -> str:
         return _LIB
     os.makedirs(_LIBDIR, exist_ok=True)
     tmp = _LIB + ".tmp%d" % os.getpid()
-    subprocess.check_call(["gcc", "-O2", "-std=c99", "-ffp-contract=off",
+    subprocess.check_call(["gcc", "-O3", "-std=c99", "-ffp-contract=off",
                            "-fno-fast-math", "-fopenmp", "-shared", "-fPIC",
                            "-o", tmp, _SRC, "-lm"])
     os.replace(tmp, _LIB)

@@ -16,7 +16,7 @@ def _pairs(case):
 
 
 @pytest.mark.parametrize("name", CASES)
-@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("mode", [0, 1, 3])
 def test_oracle_matches_reference(name, mode):
     case = Case(name)
     bins = fo.Bins(survey=not case.box, **case.bins_kwargs())
