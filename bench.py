@@ -148,6 +148,16 @@ def profile_traffic():
     return None
 
 
+def max_over_ranks(value, dist):
+    """Step time of the slowest rank (replicas run independent jobs)."""
+    if dist is None or not dist.is_initialized():
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0])
+
+
 def run_reference(args, rank, world):
     """CPU restatement of FCFC's counter on a bounded sample of the workload."""
     if rank != 0:
@@ -294,11 +304,7 @@ def main():
     st1 = res[0][1]
     st2 = res[1][1]
     # max over ranks
-    ms_step = ms_tot / args.steps
-    if dist:
-        t = torch.tensor([ms_step], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t[0])
+    ms_step = max_over_ranks(ms_tot / args.steps, dist)
     value = pairs_per_step * world / (ms_step * 1e-3)
 
     # all-FP64 GPU path, one step

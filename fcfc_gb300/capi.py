@@ -91,6 +91,8 @@ PROTOTYPES = {
                                         C.c_int, P, P, C.c_double, P, P, P]),
     "fcfcg_read_paircount": (C.c_int, [P, C.c_char_p, P, P, P, P, P, P, P,
                                        P]),
+    "fcfcg_cf_eval": (C.c_int, [C.c_char_p, C.c_int, C.c_char_p, P, P,
+                                C.c_long, P]),
     "fcfcg_write_cf": (C.c_int, [P, C.c_char_p, P]),
     "fcfcg_write_multipoles": (C.c_int, [P, C.c_char_p, C.c_int, P, P]),
     "fcfcg_write_wp": (C.c_int, [P, C.c_char_p, P]),

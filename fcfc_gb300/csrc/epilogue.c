@@ -364,3 +364,162 @@ int fcfcg_write_wp(const fcfcg_ctx *c, const char *fname, const double *wp) {
   if (fclose(fp)) e = 1;
   return e ? FCFCG_ERR_SAVE : FCFCG_OK;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Correlation-function estimators.                                          */
+
+/*
+ * FCFC evaluates CF_ESTIMATOR strings per bin with libast after replacing
+ * each pair label by its normalised counts and "@@" by the analytic RR
+ * (src/fcfc/2pt_box/setup_cf.c:130-215, eval_cf.c:258-315).  This is a
+ * recursive-descent evaluator for the arithmetic part of that language:
+ * numbers, pair labels, @@, parentheses, unary minus, ** (power), * / %,
+ * + -, and the functions abs, sqrt, ln, log (base 10).  Operators bind as
+ * in libast: unary minus before **, ** before * / %, then + -.
+ */
+typedef struct {
+  const char *s;
+  int npc;
+  const char *labels;
+  const double *ncnt;
+  const double *rr;
+  long ntot, bin;
+  int err;
+} est_t;
+
+static void est_ws(est_t *e) {
+  while (*e->s == ' ' || *e->s == '\t') e->s++;
+}
+
+static double est_add(est_t *e);
+
+static double est_primary(est_t *e) {
+  est_ws(e);
+  const char *c = e->s;
+  if (*c == '(') {
+    e->s++;
+    double v = est_add(e);
+    est_ws(e);
+    if (*e->s != ')') {
+      e->err = 1;
+      return 0;
+    }
+    e->s++;
+    return v;
+  }
+  if (c[0] == '@' && c[1] == '@') {
+    e->s += 2;
+    if (!e->rr) {
+      e->err = 2;
+      return 0;
+    }
+    return e->rr[e->bin];
+  }
+  if (c[0] >= 'A' && c[0] <= 'Z' && c[1] >= 'A' && c[1] <= 'Z') {
+    for (int k = 0; k < e->npc; k++) {
+      if (e->labels[2 * k] == c[0] && e->labels[2 * k + 1] == c[1]) {
+        e->s += 2;
+        return e->ncnt[(size_t) k * e->ntot + e->bin];
+      }
+    }
+    e->err = 3;
+    return 0;
+  }
+  static const char *fn[] = {"abs", "sqrt", "ln", "log"};
+  for (int k = 0; k < 4; k++) {
+    size_t l = strlen(fn[k]);
+    if (!strncmp(c, fn[k], l)) {
+      const char *d = c + l;
+      while (*d == ' ') d++;
+      if (*d != '(') break;
+      e->s = d;
+      double v = est_primary(e);
+      switch (k) {
+        case 0: return fabs(v);
+        case 1: return sqrt(v);
+        case 2: return log(v);
+        default: return log10(v);
+      }
+    }
+  }
+  if ((*c >= '0' && *c <= '9') || *c == '.') {
+    char *end;
+    double v = strtod(c, &end);
+    if (end == c) {
+      e->err = 4;
+      return 0;
+    }
+    e->s = end;
+    return v;
+  }
+  e->err = 5;
+  return 0;
+}
+
+static double est_unary(est_t *e) {
+  est_ws(e);
+  if (*e->s == '-') {
+    e->s++;
+    return -est_unary(e);
+  }
+  if (*e->s == '+') {
+    e->s++;
+    return est_unary(e);
+  }
+  return est_primary(e);
+}
+
+static double est_pow(est_t *e) {
+  double v = est_unary(e);
+  est_ws(e);
+  if (e->s[0] == '*' && e->s[1] == '*') {
+    e->s += 2;
+    double r = est_pow(e);
+    return pow(v, r);
+  }
+  return v;
+}
+
+static double est_mul(est_t *e) {
+  double v = est_pow(e);
+  for (;;) {
+    est_ws(e);
+    char op = *e->s;
+    if ((op == '*' && e->s[1] != '*') || op == '/' || op == '%') {
+      e->s++;
+      double r = est_pow(e);
+      v = (op == '*') ? v * r : (op == '/' ? v / r : fmod(v, r));
+    } else {
+      return v;
+    }
+  }
+}
+
+static double est_add(est_t *e) {
+  double v = est_mul(e);
+  for (;;) {
+    est_ws(e);
+    char op = *e->s;
+    if (op == '+' || op == '-') {
+      e->s++;
+      double r = est_mul(e);
+      v = (op == '+') ? v + r : v - r;
+    } else {
+      return v;
+    }
+  }
+}
+
+int fcfcg_cf_eval(const char *expr, int npc, const char *labels,
+    const double *ncnt, const double *rr, long ntot, double *out) {
+  if (!expr || npc < 0 || (npc && (!labels || !ncnt)) || ntot < 1 || !out)
+    return FCFCG_ERR_ARG;
+  for (long b = 0; b < ntot; b++) {
+    est_t e = {expr, npc, labels, ncnt, rr, ntot, b, 0};
+    double v = est_add(&e);
+    est_ws(&e);
+    if (e.err || *e.s) return FCFCG_ERR_CFG;
+    out[b] = v;
+  }
+  return FCFCG_OK;
+}

@@ -1,0 +1,286 @@
+"""FCFC-compatible run flow on the GB300 engine.
+
+Takes FCFC's configuration keys (a libcfg-style file or a dict), counts the
+pairs listed in PAIR_COUNT on the GPU, writes PAIR_COUNT_FILE, evaluates
+CF_ESTIMATOR into CF_OUTPUT_FILE, and the Legendre multipoles / projected
+correlation function into MULTIPOLE_FILE / PROJECTED_FILE -- the sequence of
+FCFC's eval_cf (src/fcfc/2pt_box/eval_cf.c:405, survey src/fcfc/2pt/eval_cf.c).
+Existing pair-count files are read back instead of recounted when OVERWRITE
+is 0 or 1, as FCFC's check_output decides (src/fcfc/2pt_box/load_conf.c:582-650).
+
+    python -m fcfc_gb300.runner --box -c fcfc_2pt_box.conf
+    python -m fcfc_gb300.runner --survey -c fcfc_2pt.conf
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import os
+import re
+import shlex
+import sys
+
+import numpy as np
+
+from . import capi
+from .capi import BIN_SMU, BIN_SPI, FCFCGError
+from .engine import PairCounter
+
+
+# --------------------------------------------------------------------------
+# configuration
+
+def parse_conf(text: str) -> dict:
+    """libcfg syntax: KEY = value or [a, b, ...]; '#' comments; '\\' joins
+    lines; values may be quoted."""
+    out = {}
+    text = re.sub(r"\\\s*\n", " ", text)
+    for line in text.splitlines():
+        s = line.strip()
+        if not s or s.startswith("#"):
+            continue
+        if "=" not in s:
+            continue
+        k, v = s.split("=", 1)
+        k = k.strip()
+        v = _strip_comment(v).strip()
+        if not v:
+            continue
+        if v.startswith("["):
+            inner = v[1:v.rindex("]")] if "]" in v else v[1:]
+            lex = shlex.shlex(inner, posix=True)
+            lex.whitespace = ","
+            lex.whitespace_split = True
+            lex.commenters = ""
+            out[k] = [t.strip() for t in lex]
+        else:
+            out[k] = _unquote(v)
+    return out
+
+
+def _strip_comment(v):
+    q = None
+    for i, ch in enumerate(v):
+        if ch in "'\"":
+            q = None if q == ch else (ch if q is None else q)
+        elif ch == "#" and q is None:
+            return v[:i]
+    return v
+
+
+def _unquote(v):
+    v = v.strip()
+    if len(v) >= 2 and v[0] == v[-1] and v[0] in "'\"":
+        return v[1:-1]
+    return v
+
+
+def _arr(conf, key, n=None, default=None, cast=str):
+    v = conf.get(key, default)
+    if v is None:
+        return None
+    if not isinstance(v, list):
+        v = [v]
+    v = [cast(x) if not isinstance(x, str) or cast is str else cast(_unquote(x))
+         for x in v]
+    if n is not None and len(v) == 1 and n > 1:
+        v = v * n
+    return v
+
+
+def _bool(x):
+    return str(x).strip().upper() in ("T", "TRUE", "1", "Y", "YES")
+
+
+# --------------------------------------------------------------------------
+# catalogues
+
+def read_catalog(path, formatter=None, position=("$1", "$2", "$3"),
+                 weight=None, skip=0, comment=None):
+    """ASCII catalogue with column indicators $n (or ${n}); .npy arrays are
+    read directly (columns x y z [w])."""
+    if path.endswith(".npy"):
+        a = np.load(path)
+        w = a[:, 3] if (weight is not None and a.shape[1] > 3) else None
+        return a[:, :3].astype(np.float64), w
+    cols = []
+    for p in list(position) + ([weight] if weight else []):
+        m = re.fullmatch(r"\$\{?(\d+)\}?", str(p).strip())
+        if not m:
+            raise FCFCGError(capi.ERR_CFG, "only column indicators $n are "
+                             "supported in POSITION/WEIGHT: %r" % p)
+        cols.append(int(m.group(1)) - 1)
+    if formatter:
+        # skipped columns (%*...) do not count
+        fmts = formatter.split()
+        kept = [i for i, f in enumerate(fmts) if not f.startswith("%*")]
+        cols = [kept[c] for c in cols]
+    data = np.loadtxt(path, comments=comment or None, skiprows=int(skip or 0),
+                      usecols=cols, ndmin=2)
+    x = np.ascontiguousarray(data[:, :3], np.float64)
+    w = np.ascontiguousarray(data[:, 3], np.float64) if weight else None
+    return x, w
+
+
+def read_bins_file(path):
+    """Edges as FCFC's read_bins builds them (setup_cf.c:74-119)."""
+    t = np.loadtxt(path, comments="#", ndmin=2)
+    e = np.empty(len(t) + 1)
+    e[0] = t[0, 0]
+    for i in range(1, len(t)):
+        if abs(t[i, 0] - t[i - 1, 1]) > 1e-10:
+            raise FCFCGError(capi.ERR_FILE, "discontinuous separation bins")
+        e[i] = t[i, 0] if t[i, 0] == t[i - 1, 1] else 0.5 * (t[i, 0] + t[i - 1, 1])
+    e[-1] = t[-1, 1]
+    return e
+
+
+# --------------------------------------------------------------------------
+
+def run(conf: dict, geometry: str = "box", device: int = -1,
+        precision: int = capi.PREC_FP32_RECHECK, verbose: bool = False):
+    """Run one FCFC job.  Returns a dict with counts, xi, multipoles, wp."""
+    box = geometry == "box"
+    files = _arr(conf, "CATALOG")
+    ncat = len(files)
+    labels = _arr(conf, "CATALOG_LABEL") or [chr(ord("A") + i) for i in range(ncat)]
+    fmtr = _arr(conf, "ASCII_FORMATTER", ncat)
+    pos = _arr(conf, "POSITION")
+    wts = _arr(conf, "WEIGHT", ncat)
+    skip = _arr(conf, "ASCII_SKIP", ncat, default=[0] * ncat)
+    cmt = _arr(conf, "ASCII_COMMENT", ncat)
+    bintype = int(conf.get("BINNING_SCHEME", 0))
+    pairs = _arr(conf, "PAIR_COUNT")
+    pcout = _arr(conf, "PAIR_COUNT_FILE")
+    est = _arr(conf, "CF_ESTIMATOR") or []
+    cfout = _arr(conf, "CF_OUTPUT_FILE") or []
+    poles = [int(p) for p in (_arr(conf, "MULTIPOLE") or [])]
+    mpout = _arr(conf, "MULTIPOLE_FILE") or []
+    do_wp = _bool(conf.get("PROJECTED_CF", "F"))
+    wpout = _arr(conf, "PROJECTED_FILE") or []
+    ofmt = int(conf.get("OUTPUT_FORMAT", 0))
+    ovw = int(conf.get("OVERWRITE", 0))
+    if not box and any(_bool(v) for v in (_arr(conf, "COORD_CONVERT", ncat) or [])):
+        raise FCFCGError(capi.ERR_UNSUPPORTED,
+                         "COORD_CONVERT: give comoving coordinates")
+
+    kw = dict(geometry=geometry, bintype=bintype, device=device)
+    if box:
+        b = [float(v) for v in _arr(conf, "BOX_SIZE")]
+        kw["box"] = b * 3 if len(b) == 1 else b
+    if conf.get("SEP_BIN_FILE"):
+        kw["sedges"] = read_bins_file(conf["SEP_BIN_FILE"])
+    else:
+        kw.update(smin=float(conf["SEP_BIN_MIN"]), smax=float(conf["SEP_BIN_MAX"]),
+                  ds=float(conf["SEP_BIN_SIZE"]))
+    if bintype == BIN_SMU:
+        kw["nmu"] = int(conf["MU_BIN_NUM"])
+    if bintype == BIN_SPI:
+        if conf.get("PI_BIN_FILE"):
+            kw["pedges"] = read_bins_file(conf["PI_BIN_FILE"])
+        else:
+            kw.update(pmin=float(conf["PI_BIN_MIN"]), pmax=float(conf["PI_BIN_MAX"]),
+                      dpi=float(conf["PI_BIN_SIZE"]))
+
+    pc = PairCounter(**kw)
+    # catalogues, loaded on first use
+    loaded = {}
+    pi = 0
+    for i in range(ncat):
+        pass
+
+    def slot_of(lab):
+        i = labels.index(lab)
+        if i not in loaded:
+            p3 = pos[3 * i: 3 * i + 3]
+            w = wts[i] if wts and wts[i] not in (None, "", "''", '""') else None
+            x, ww = read_catalog(files[i], fmtr[i] if fmtr else None, p3, w,
+                                 skip[i], cmt[i] if cmt else None)
+            pc.load(i, x, ww)
+            loaded[i] = (len(x), ww is not None)
+        return i
+
+    weighted_cat = {}
+    for i, lab in enumerate(labels):
+        w = wts[i] if wts else None
+        weighted_cat[lab] = w not in (None, "", "''", '""')
+
+    ncnt_all = []
+    out = {"counts": {}, "norm": {}}
+    for k, pair in enumerate(pairs):
+        a, bl = pair[0], pair[1]
+        isauto = a == bl
+        weighted = weighted_cat[a] or weighted_cat[bl]
+        fn = pcout[k]
+        if os.path.exists(fn) and ovw <= 1:
+            r = pc.read_paircount(fn)
+            ncnt_all.append(r["ncnt"])
+            out["counts"][pair] = r["cnt"]
+            out["norm"][pair] = r["norm"]
+            continue
+        sa = slot_of(a)
+        sb = slot_of(bl)
+        cnt = pc.count_pairs(sa, None if isauto else sb, weighted=weighted,
+                             precision=precision)
+        na, wa = pc.catalog_info(sa)
+        nb, wb = pc.catalog_info(sb)
+        if weighted:
+            n1, n2 = wa, wb
+        else:
+            n1, n2 = float(na), float(nb)
+        cnt2, norm, ncnt = pc.normalise(cnt, isauto, weighted, n1, n2)
+        pc.write_paircount(fn, ofmt, isauto, weighted,
+                           [na] if isauto else [na, nb],
+                           [wa] if isauto else [wa, wb], norm, ncnt, cnt2)
+        ncnt_all.append(ncnt)
+        out["counts"][pair] = cnt2
+        out["norm"][pair] = norm
+        if verbose:
+            print("counted %s: %s" % (pair, pc.stats()))
+
+    rr = pc.analytic_rr() if box else None
+    if est:
+        lab = "".join(pairs).encode()
+        nc = np.ascontiguousarray(np.stack(ncnt_all), np.float64)
+        out["xi"] = []
+        out["mp"] = []
+        out["wp"] = []
+        for k, e in enumerate(est):
+            xi = np.zeros(pc.ntot)
+            rc = pc.lib.fcfcg_cf_eval(
+                e.encode(), len(pairs), lab, capi.ptr(nc),
+                capi.ptr(rr) if rr is not None else None, pc.ntot,
+                capi.ptr(xi))
+            if rc:
+                raise FCFCGError(rc, "CF_ESTIMATOR %r" % e)
+            pc.write_cf(cfout[k], xi)
+            out["xi"].append(xi)
+            if poles and bintype == BIN_SMU:
+                mp = pc.multipoles(xi, poles)
+                pc.write_multipoles(mpout[k], poles, mp)
+                out["mp"].append(mp)
+            elif do_wp and bintype == BIN_SPI:
+                wp = pc.wp(xi)
+                pc.write_wp(wpout[k], wp)
+                out["wp"].append(wp)
+    return out
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description="FCFC run flow on the GB300 engine")
+    g = ap.add_mutually_exclusive_group()
+    g.add_argument("--box", action="store_true", help="FCFC_2PT_BOX keys")
+    g.add_argument("--survey", action="store_true", help="FCFC_2PT keys")
+    ap.add_argument("-c", "--conf", required=True)
+    ap.add_argument("--fp64", action="store_true", help="all-FP64 GPU path")
+    ap.add_argument("-v", "--verbose", action="store_true")
+    a = ap.parse_args(argv)
+    conf = parse_conf(open(a.conf).read())
+    run(conf, "survey" if a.survey else "box",
+        precision=capi.PREC_FP64 if a.fp64 else capi.PREC_FP32_RECHECK,
+        verbose=a.verbose)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

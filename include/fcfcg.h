@@ -215,6 +215,17 @@ int fcfcg_read_paircount(const fcfcg_ctx *ctx, const char *fname,
     int *isauto, int *withwt, uint64_t ntr[2], double wtr[2], double *norm,
     double *ncnt, int64_t *icnt, double *wcnt);
 
+/*
+ * Evaluate a CF_ESTIMATOR expression per bin (eval_cf.c:258-315): pair
+ * labels (two capitals, e.g. "DD") stand for the normalised counts of pair
+ * k (labels[2k], labels[2k+1]; ncnt[k * ntot + bin]), "@@" for the analytic
+ * RR (rr, may be NULL when unused).  Arithmetic as libast: numbers, ( ),
+ * unary -, ** , * / %, + -, abs sqrt ln log.  FCFCG_ERR_CFG on a syntax
+ * error or an unknown label.
+ */
+int fcfcg_cf_eval(const char *expr, int npc, const char *labels,
+    const double *ncnt, const double *rr, long ntot, double *out);
+
 /* Write xi / multipoles / w_p text files as save_res_ascii does. */
 int fcfcg_write_cf(const fcfcg_ctx *ctx, const char *fname, const double *xi);
 int fcfcg_write_multipoles(const fcfcg_ctx *ctx, const char *fname,
