@@ -93,6 +93,8 @@ PROTOTYPES = {
                                        P]),
     "fcfcg_cf_eval": (C.c_int, [C.c_char_p, C.c_int, C.c_char_p, P, P,
                                 C.c_long, P]),
+    "fcfcg_count_noalloc": (C.c_int, [P, C.c_int, C.c_size_t, P, P, P,
+                                      C.c_size_t, P, P, P, P, P]),
     "fcfcg_write_cf": (C.c_int, [P, C.c_char_p, P]),
     "fcfcg_write_multipoles": (C.c_int, [P, C.c_char_p, C.c_int, P, P]),
     "fcfcg_write_wp": (C.c_int, [P, C.c_char_p, P]),

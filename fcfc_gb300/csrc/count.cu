@@ -25,6 +25,7 @@
 #include <cuda_runtime.h>
 #include <float.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "fcfcg_internal.h"
 
@@ -952,4 +953,207 @@ extern "C" int fcfcg_k_recheck(void *stream, const fcfcg_launch *L,
   else
     k_recheck<0><<<blocks, 256, 0, (cudaStream_t) stream>>>(*L, nq);
   return (int) cudaGetLastError();
+}
+
+/* ------------------------------------------------------------------------ */
+/* Allocation-free variant of the FP64 counting kernel.                     */
+
+/*
+ * Scratch of fcfcg_count_noalloc: the 64-bit bin accumulators followed by the
+ * FP64 binning tables, in one fixed device array.  Every GPU that loads the
+ * library keeps these bytes until the process exits.
+ */
+static __device__ __align__(256) unsigned char
+    g_noalloc_scratch[FCFCG_NOALLOC_SCRATCH_BYTES];
+
+#define NOALLOC_MAX_DEV 64
+static void *g_noalloc_addr[NOALLOC_MAX_DEV];
+
+#define NA_TILE 256
+
+/* All pairs of two catalogues (raw FP64 coordinates on the device), each
+ * pair binned by the reference's FP64 formula and counted in the scratch
+ * accumulators.  Periodic images: the minimal image, with the shift on the
+ * first catalogue's point (cross) or the smaller index (auto). */
+template <int GEOM>
+__global__ void __launch_bounds__(NA_TILE)
+k_count64_noalloc(const fcfcg_launch L, double rescale, size_t na,
+    const double *__restrict__ xa, const double *__restrict__ ya,
+    const double *__restrict__ za, size_t nb, const double *__restrict__ xb,
+    const double *__restrict__ yb, const double *__restrict__ zb,
+    unsigned long long *acc) {
+  __shared__ double tx[NA_TILE], ty[NA_TILE], tz[NA_TILE], ts[NA_TILE];
+  const size_t ntile = (nb + NA_TILE - 1) / NA_TILE;
+  const size_t nblk = (na + NA_TILE - 1) / NA_TILE;
+  for (size_t w = blockIdx.x; w < nblk * ntile; w += gridDim.x) {
+    const size_t ib = w / ntile, jt = w % ntile;
+    if (L.isauto && jt < ib) continue;           /* j >= i blocks only */
+    const size_t i = ib * NA_TILE + threadIdx.x;
+    double x1 = 0, y1 = 0, z1 = 0, s1 = 0;
+    if (i < na) {
+      x1 = xa[i];
+      y1 = ya[i];
+      z1 = za[i];
+      if (rescale != 1) {
+        x1 = __dmul_rn(x1, rescale);
+        y1 = __dmul_rn(y1, rescale);
+        z1 = __dmul_rn(z1, rescale);
+      }
+      s1 = __dadd_rn(__dadd_rn(__dmul_rn(x1, x1), __dmul_rn(y1, y1)),
+                     __dmul_rn(z1, z1));
+    }
+    __syncthreads();
+    const size_t j0 = jt * NA_TILE;
+    {
+      const size_t j = j0 + threadIdx.x;
+      double a = 0, b = 0, c = 0;
+      if (j < nb) {
+        a = xb[j];
+        b = yb[j];
+        c = zb[j];
+        if (rescale != 1) {
+          a = __dmul_rn(a, rescale);
+          b = __dmul_rn(b, rescale);
+          c = __dmul_rn(c, rescale);
+        }
+      }
+      tx[threadIdx.x] = a;
+      ty[threadIdx.x] = b;
+      tz[threadIdx.x] = c;
+      ts[threadIdx.x] = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)),
+                                  __dmul_rn(c, c));
+    }
+    __syncthreads();
+    if (i < na) {
+      const int jn = (int) ((nb - j0 < NA_TILE) ? nb - j0 : NA_TILE);
+      for (int k = 0; k < jn; k++) {
+        const size_t j = j0 + (size_t) k;
+        if (L.isauto && j <= i) continue;
+        int bin;
+        if (GEOM == FCFCG_GEOM_SURVEY) {
+          bin = ref_bin_survey(L, x1, y1, z1, s1, tx[k], ty[k], tz[k], ts[k]);
+        } else {
+          const double d[3] = {__dsub_rn(x1, tx[k]), __dsub_rn(y1, ty[k]),
+                               __dsub_rn(z1, tz[k])};
+          const double p[3] = {x1, y1, z1}, q[3] = {tx[k], ty[k], tz[k]};
+          double r[3];
+          for (int a = 0; a < 3; a++) {
+            const double hL = L.box[a] * 0.5;
+            const double sh = (d[a] > hL) ? -L.box[a] : ((d[a] < -hL) ? L.box[a] : 0.0);
+            r[a] = __dsub_rn(__dadd_rn(p[a], sh), q[a]);
+          }
+          bin = ref_bin_box(L, r[0], r[1], r[2]);
+        }
+        if (bin >= 0) atomicAdd(acc + bin, 1ull);
+      }
+    }
+  }
+}
+
+__global__ void k_noalloc_copy(const unsigned long long *acc, long n,
+    long long *out) {
+  for (long i = blockIdx.x * (long) blockDim.x + threadIdx.x; i < n;
+       i += (long) gridDim.x * blockDim.x)
+    out[i] = (long long) acc[i];
+}
+
+static size_t na_align(size_t n) { return (n + 255) & ~(size_t) 255; }
+
+extern "C" int fcfcg_count_noalloc(const fcfcg_ctx *bins_ctx, int isauto,
+    size_t na, const double *xa, const double *ya, const double *za,
+    size_t nb, const double *xb, const double *yb, const double *zb,
+    long long *counts, void *stream) {
+  const fcfcg_bins *b = fcfcg_ctx_bins(bins_ctx);
+  if (!b || !counts || (na && (!xa || !ya || !za))) return FCFCG_ERR_ARG;
+  if (isauto) {
+    nb = na;
+    xb = xa;
+    yb = ya;
+    zb = za;
+  } else if (nb && (!xb || !yb || !zb)) {
+    return FCFCG_ERR_ARG;
+  }
+  /* layout of the scratch: accumulators, then the reference tables */
+  const size_t o_acc = 0;
+  const size_t o_rs = na_align(o_acc + sizeof(unsigned long long) * b->ntot);
+  const size_t o_se = na_align(o_rs + sizeof(uint16_t) * b->s.nrtab);
+  const int spi = (b->bintype == FCFCG_BIN_SPI);
+  const size_t o_rp = na_align(o_se + sizeof(double) * (b->s.nbin + 1));
+  const size_t o_pe = na_align(o_rp + (spi ? sizeof(uint16_t) * b->p.nrtab : 0));
+  const size_t end = o_pe + (spi ? sizeof(double) * (b->p.nbin + 1) : 0);
+  if (end > FCFCG_NOALLOC_SCRATCH_BYTES) return FCFCG_ERR_UNSUPPORTED;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e) return FCFCG_ERR_CUDA;
+  if (dev < 0 || dev >= NOALLOC_MAX_DEV) return FCFCG_ERR_UNSUPPORTED;
+  if (!g_noalloc_addr[dev]) {
+    /* first call on this device: the device address of the scratch array
+     * (the host-side symbol is only a stand-in) */
+    void *p = NULL;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e || !p) return FCFCG_ERR_CUDA;
+    g_noalloc_addr[dev] = p;
+  }
+  unsigned char *base = (unsigned char *) g_noalloc_addr[dev];
+  cudaStream_t st = (cudaStream_t) stream;
+  fcfcg_launch L;
+  memset(&L, 0, sizeof L);
+  L.geometry = b->geometry;
+  L.bintype = b->bintype;
+  L.isauto = isauto;
+  for (int k = 0; k < 3; k++) L.box[k] = b->box[k];
+  L.ns = b->ns;
+  L.nmu = b->nmu;
+  L.np = b->np;
+  L.ntot = b->ntot;
+  L.rs = (const uint16_t *) (base + o_rs);
+  L.rsoff = b->s.roff;
+  L.nrs = b->s.nrtab;
+  L.s2edge = (const double *) (base + o_se);
+  L.s2min = b->s.vmin;
+  L.s2max = b->s.vmax;
+  L.smin0 = b->s.min0;
+  if (spi) {
+    L.rp = (const uint16_t *) (base + o_rp);
+    L.rpoff = b->p.roff;
+    L.nrp = b->p.nrtab;
+    L.pedge = (const double *) (base + o_pe);
+    L.pmin = b->p.vmin;
+    L.pmax = b->p.vmax;
+    L.pmin0 = b->p.min0;
+  }
+  unsigned long long *acc = (unsigned long long *) (base + o_acc);
+  if ((e = cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * b->ntot, st)))
+    return FCFCG_ERR_CUDA;
+  if ((e = cudaMemcpyAsync(base + o_rs, b->s.rtab,
+                           sizeof(uint16_t) * b->s.nrtab,
+                           cudaMemcpyHostToDevice, st)) ||
+      (e = cudaMemcpyAsync(base + o_se, b->s.edge,
+                           sizeof(double) * (b->s.nbin + 1),
+                           cudaMemcpyHostToDevice, st)))
+    return FCFCG_ERR_CUDA;
+  if (spi &&
+      ((e = cudaMemcpyAsync(base + o_rp, b->p.rtab,
+                            sizeof(uint16_t) * b->p.nrtab,
+                            cudaMemcpyHostToDevice, st)) ||
+       (e = cudaMemcpyAsync(base + o_pe, b->p.edge,
+                            sizeof(double) * (b->p.nbin + 1),
+                            cudaMemcpyHostToDevice, st))))
+    return FCFCG_ERR_CUDA;
+  if (na && nb) {
+    const size_t work = ((na + NA_TILE - 1) / NA_TILE) *
+                        ((nb + NA_TILE - 1) / NA_TILE);
+    const unsigned blocks = (unsigned) (work < 152 * 8 ? work : 152 * 8);
+    if (b->geometry == FCFCG_GEOM_SURVEY)
+      k_count64_noalloc<FCFCG_GEOM_SURVEY><<<blocks, NA_TILE, 0, st>>>(
+          L, b->rescale, na, xa, ya, za, nb, xb, yb, zb, acc);
+    else
+      k_count64_noalloc<FCFCG_GEOM_BOX><<<blocks, NA_TILE, 0, st>>>(
+          L, b->rescale, na, xa, ya, za, nb, xb, yb, zb, acc);
+    if ((e = cudaGetLastError())) return FCFCG_ERR_CUDA;
+  }
+  k_noalloc_copy<<<(unsigned) ((b->ntot + 255) / 256 < 1024 ? (b->ntot + 255) / 256 : 1024),
+                   256, 0, st>>>(acc, b->ntot, counts);
+  if ((e = cudaGetLastError())) return FCFCG_ERR_CUDA;
+  return FCFCG_OK;
 }

@@ -232,6 +232,42 @@ int fcfcg_write_multipoles(const fcfcg_ctx *ctx, const char *fname,
     int npole, const int *poles, const double *mp);
 int fcfcg_write_wp(const fcfcg_ctx *ctx, const char *fname, const double *wp);
 
+/* ---------------- allocation-free counting ------------------------------ */
+
+/* Bytes of the fixed device scratch fcfcg_count_noalloc works in. */
+#define FCFCG_NOALLOC_SCRATCH_BYTES (4u << 20)
+
+/*
+ * Unweighted pair counts for callers that cannot allocate device memory
+ * (code running inside another framework's memory pool, a CUDA graph being
+ * built, or an embedding that forbids cudaMalloc).  No counterpart in the
+ * reference; it is a variant of the FP64 counting kernel.
+ *
+ * bins_ctx: a host-only context (fcfcg_create_host) describing the bins; it
+ * is only read.  xa/ya/za (na objects) and xb/yb/zb (nb, ignored when
+ * isauto) are FP64 device pointers with the coordinates as read (the call
+ * rescales them as FCFC does); counts is a device array of ntot int64, set
+ * to the undoubled counts of count_pairs.  Every pair is binned by the FP64
+ * formula by brute force, so this is meant for modest catalogues.  The
+ * work runs on `stream` (a cudaStream_t, NULL for the default stream); the
+ * call returns without waiting.
+ *
+ * The call allocates nothing, host or device.  Its scratch is one static
+ * device array of FCFCG_NOALLOC_SCRATCH_BYTES (4 MiB) that every GPU loading
+ * the library holds until the process exits; bin set-ups needing more (the
+ * 64-bit accumulators of ntot bins plus the lookup tables) are rejected with
+ * FCFCG_ERR_UNSUPPORTED.  The scratch is shared by all calls and keeps the
+ * last call's contents (the accumulators are cleared at the start of each
+ * call), so calls whose work overlaps on a GPU race: order them on one
+ * stream.  The first call on a device looks up the device address of the
+ * scratch (cudaGetSymbolAddress); make that first call before any stream
+ * capture.
+ */
+int fcfcg_count_noalloc(const fcfcg_ctx *bins_ctx, int isauto, size_t na,
+    const double *xa, const double *ya, const double *za, size_t nb,
+    const double *xb, const double *yb, const double *zb, long long *counts,
+    void *stream);
+
 #ifdef __cplusplus
 }
 #endif
