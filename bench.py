@@ -276,10 +276,13 @@ def main():
 
     # exact in-range pair numbers of this workload (unweighted counts)
     n_in = []
+    tuned = []
     for pc in (p1, p2):
         pc.load_device(0, xd[0].data_ptr(), xd[1].data_ptr(), xd[2].data_ptr(),
                        n, wd.data_ptr())
         n_in.append(int(pc.count_pairs(0, weighted=False).sum()))
+        # grid refinement for this density, timed once before the run
+        tuned.append(pc.autotune(0, weighted=True)[0])
     pairs_per_step = sum(n_in)
     for _ in range(max(args.warmup, 0)):
         step()
@@ -288,7 +291,8 @@ def main():
         dist.barrier()
     clk = ClockSampler(local)
     clk.start()
-    ms_tot, ms_k1, launches0 = 0.0, 0.0, p1.stats()["launches"] + p2.stats()["launches"]
+    ms_tot, ms_k1, ms_k2 = 0.0, 0.0, 0.0
+    launches0 = p1.stats()["launches"] + p2.stats()["launches"]
     torch.cuda.synchronize()
     t_wall0 = time.perf_counter()
     for _ in range(args.steps):
@@ -297,6 +301,7 @@ def main():
         ms, res = step()
         ms_tot += ms
         ms_k1 += res[0][1]["ms_count"]
+        ms_k2 += res[1][1]["ms_count"]
     torch.cuda.synchronize()
     wall = time.perf_counter() - t_wall0
     clocks = clk.stop()
@@ -360,6 +365,7 @@ def main():
                    "pairs_smu": n_in[0], "pairs_spi": n_in[1],
                    "l2": "flushed between steps (256 MiB write)",
                    "cells_per_smax": [st1["cells_per_smax"], st2["cells_per_smax"]],
+                   "cells_per_smax_autotuned": tuned,
                    "parallelism": "replicas" if world > 1 else "1 GPU"},
         "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": ms64,
                  "speedup_fp32_recheck_over_fp64": value / world / fp64_value},
@@ -377,7 +383,9 @@ def main():
                      "rechecked_smu": st1["rechecked"],
                      "candidates_spi": st2["candidates"],
                      "rechecked_spi": st2["rechecked"],
-                     "wall_ms_per_step": wall / args.steps * 1e3},
+                     "wall_ms_per_step": wall / args.steps * 1e3,
+                     "kernel_ms_smu": ms_k1 / args.steps,
+                     "kernel_ms_spi": ms_k2 / args.steps},
         "clocks": clocks,
         "gpu_launches": int(launches_total),
     }

@@ -83,6 +83,8 @@ PROTOTYPES = {
                               P, P]),
     "fcfcg_stats_get": (C.c_int, [P, C.POINTER(Stats)]),
     "fcfcg_set_cells_per_smax": (C.c_int, [P, C.c_int]),
+    "fcfcg_autotune": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int,
+                                 C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "fcfcg_norm": (C.c_double, [C.c_int, C.c_int, C.c_double, C.c_double]),
     "fcfcg_analytic_rr": (C.c_int, [P, P]),
     "fcfcg_multipoles": (C.c_int, [P, P, C.c_int, P, P]),

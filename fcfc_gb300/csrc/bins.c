@@ -167,27 +167,45 @@ static int axis_bin(const fcfcg_axis *a, double v) {
 
 int fcfcg_axis_ftab(fcfcg_axis *a, int unused) {
   (void) unused;
-  long lo = a->min0 ? 0 : (long) floor(a->vmin) - 1;
-  long hi = (long) ceil(a->vmax) + 2;
+  /* cell width: the smallest power of two (>= 1 unit) that keeps the table
+   * within FCFCG_FTAB_MAXLEN cells */
+  int sh = 0;
+  for (;;) {
+    const double w = ldexp(1.0, sh);
+    long lo = a->min0 ? 0 : (long) floor(a->vmin / w) - 1;
+    long hi = (long) ceil(a->vmax / w) + 2;
+    if (hi - lo <= FCFCG_FTAB_MAXLEN || sh > 40) break;
+    sh++;
+  }
+  const double w = ldexp(1.0, sh);
+  long lo = a->min0 ? 0 : (long) floor(a->vmin / w) - 1;
+  long hi = (long) ceil(a->vmax / w) + 2;
   long m = hi - lo;
   free(a->ftab);
+  free(a->fedge);
   a->ftab = malloc(sizeof(uint16_t) * m);
-  if (!a->ftab) return FCFCG_ERR_MEMORY;
+  a->fedge = malloc(sizeof(float) * (a->nbin + 1));
+  if (!a->ftab || !a->fedge) return FCFCG_ERR_MEMORY;
+  for (int k = 0; k <= a->nbin; k++) a->fedge[k] = (float) a->edge[k];
   const int first = a->min0 ? 1 : 0;
   for (long c = 0; c < m; c++) {
-    const double i = (double) (lo + c);
-    int b = axis_bin(a, i);
+    const double x0 = (double) (lo + c) * w, x1 = x0 + w;
+    int b = axis_bin(a, x0);
     unsigned v = (b < 0) ? FCFCG_FTAB_BIN_MASK : (unsigned) b;
+    int inside = 0;
     for (int k = first; k <= a->nbin; k++) {
       const double e = a->edge[k];
-      if (e >= i - 0.5 && e <= i) v |= FCFCG_FTAB_LO;
-      if (e >= i + 1 && e <= i + 1.5) v |= FCFCG_FTAB_HI;
-      if (e > i && e < i + 1) v |= FCFCG_FTAB_CX;
+      if (e >= x0 - 0.5 * w && e <= x0) v |= FCFCG_FTAB_LO;
+      if (e >= x1 && e <= x1 + 0.5 * w) v |= FCFCG_FTAB_HI;
+      if (e > x0 && e < x1) inside++;
     }
+    if (inside == 1) v |= FCFCG_FTAB_CX1;
+    else if (inside > 1) v |= FCFCG_FTAB_CXM;
     a->ftab[c] = (uint16_t) v;
   }
   a->foff = lo;
   a->nftab = m;
+  a->fshift = sh;
   return FCFCG_OK;
 }
 
@@ -211,6 +229,7 @@ static void axis_free(fcfcg_axis *a) {
   free(a->edge);
   free(a->rtab);
   free(a->ftab);
+  free(a->fedge);
   memset(a, 0, sizeof *a);
 }
 

@@ -252,25 +252,38 @@ __device__ int ref_bin_pair(const fcfcg_launch &L, uint32_t a, uint32_t b,
 /* ------------------------------------------------------------------------ */
 /* FP32 edge-window lookup.                                                 */
 
-/* Bin of an FP32 value v with error bound E (< 1/2) on an axis table,
- * or FCFCG_FTAB_BIN_MASK when out of range; *amb set when an edge lies
- * within E of v.  CHECK_NAN: the value may be NaN (survey geometry). */
+/* Bin of an FP32 value v with error bound E on an axis table (cells of
+ * width 1 / inv, E < half a cell), or FCFCG_FTAB_BIN_MASK when out of
+ * range; *amb is set when an edge lies within E of v.  A cell with one edge
+ * inside compares v with that edge (fe: the edges rounded to FP32).
+ * CHECK_NAN: the value may be NaN (survey geometry). */
 template <bool CHECK_NAN>
 __device__ __forceinline__ unsigned ftab_bin(const uint16_t *tab, int off,
-    int ntab, float v, float E, bool &amb) {
+    int ntab, float inv, const float *fe, int nbin, float v, float E,
+    bool &amb) {
   if (CHECK_NAN && !(v == v)) {
     amb = true;
     return FCFCG_FTAB_BIN_MASK;
   }
-  const int i = __float2int_rz(v);
+  const float u = v * inv;
+  const int i = __float2int_rz(u);
   const int t = i - off;
   if ((unsigned) t >= (unsigned) ntab) return FCFCG_FTAB_BIN_MASK;
   const unsigned e = tab[t];
-  const float fr = v - (float) i;
-  const unsigned m = FCFCG_FTAB_CX | (fr <= E ? FCFCG_FTAB_LO : 0u) |
-                     (fr >= 1.f - E ? FCFCG_FTAB_HI : 0u);
+  const float fr = u - (float) i;
+  const float Eu = E * inv;
+  const unsigned m = FCFCG_FTAB_CXM | (fr <= Eu ? FCFCG_FTAB_LO : 0u) |
+                     (fr >= 1.f - Eu ? FCFCG_FTAB_HI : 0u);
   amb |= (e & m) != 0u;
-  return e & FCFCG_FTAB_BIN_MASK;
+  unsigned b = e & FCFCG_FTAB_BIN_MASK;
+  if (e & FCFCG_FTAB_CX1) {
+    const int k = (b == FCFCG_FTAB_BIN_MASK) ? 0 : (int) b + 1;
+    const float ef = fe[k];
+    const float d = v - ef;
+    amb |= fabsf(d) <= fmaf(fabsf(ef), 1.2e-7f, E);
+    if (d >= 0.f) b = (k == nbin) ? FCFCG_FTAB_BIN_MASK : (unsigned) k;
+  }
+  return b;
 }
 
 /* Integer bin of q = nmu * mu with error Eq; edges at every integer >= 1. */
@@ -441,8 +454,8 @@ template <int GEOM, int BIN, int WT>
 __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
     const Stage &S, uint32_t ent, uint32_t first, int cx, int cy, int cz,
     float c2x, float c2y, float c2z, const uint16_t *fs, const uint16_t *fp,
-    uint32_t *h, uint32_t &n_in, uint32_t &n_q,
-    unsigned long long &n_inline) {
+    const float *fse, const float *fpe, uint32_t *h, uint32_t &n_in,
+    uint32_t &n_q, unsigned long long &n_inline) {
   const int i = (int) (ent & 63u), src = (int) (ent >> 6);
   const float4 pa = S.a[i];
   const float4 pb = S.b[src];
@@ -453,8 +466,8 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
     const float sp2 = fmaf(dy, dy, dx * dx);
     const float pi = fabsf(dz);
     amb = !(sp2 >= L.tiny);
-    unsigned sb = ftab_bin<false>(fs, L.fsoff, L.nfs, sp2, L.Emax, amb);
-    unsigned pbn = ftab_bin<false>(fp, L.fpoff, L.nfp, pi, L.P0, amb);
+    unsigned sb = ftab_bin<false>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb, sp2, L.Emax, amb);
+    unsigned pbn = ftab_bin<false>(fp, L.fpoff, L.nfp, L.fpinv, fpe, L.npb, pi, L.P0, amb);
     if (!amb) {
       if (sb == FCFCG_FTAB_BIN_MASK || pbn == FCFCG_FTAB_BIN_MASK) return;
       bin = (int) sb + (int) pbn * L.ns;
@@ -463,7 +476,7 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
     const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     amb = !(s2 >= L.tiny);
     if (BIN == FCFCG_BIN_ISO) {
-      unsigned sb = ftab_bin<false>(fs, L.fsoff, L.nfs, s2, L.Emax, amb);
+      unsigned sb = ftab_bin<false>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb, s2, L.Emax, amb);
       if (!amb) {
         if (sb == FCFCG_FTAB_BIN_MASK) return;
         bin = (int) sb;
@@ -490,7 +503,7 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
         }
         const float Eq = fmaf(L.Q1, rs, fmaf(L.Q2, q, L.Q0));
         int qi = mu_bin(q, Eq, amb);
-        unsigned sb = ftab_bin<GEOM == FCFCG_GEOM_SURVEY>(fs, L.fsoff, L.nfs,
+        unsigned sb = ftab_bin<GEOM == FCFCG_GEOM_SURVEY>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb,
                                                             s2, E, amb);
         if (!amb) {
           if (sb == FCFCG_FTAB_BIN_MASK || qi >= L.nmu) return;
@@ -503,8 +516,8 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
         const float pi2 = __fdividef(dm * dm, mm);
         const float sp2 = s2 - pi2;
         const float Ep = fmaf(L.P2, s2, fmaf(L.P1, s, L.P0));
-        unsigned pbn = ftab_bin<true>(fp, L.fpoff, L.nfp, pi2, Ep, amb);
-        unsigned sb = ftab_bin<true>(fs, L.fsoff, L.nfs,
+        unsigned pbn = ftab_bin<true>(fp, L.fpoff, L.nfp, L.fpinv, fpe, L.npb, pi2, Ep, amb);
+        unsigned sb = ftab_bin<true>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb,
                                      sp2 < 0.f ? 0.f : sp2, E + Ep, amb);
         if (!amb) {
           if (sb == FCFCG_FTAB_BIN_MASK || pbn == FCFCG_FTAB_BIN_MASK) return;
@@ -536,11 +549,12 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
 
 /* Compare a neighbour point (one per lane) with chunk points [i0, i1):
  * bit i - i0 of the result marks a candidate inside the outer range. */
-template <int GEOM, int BIN>
-__device__ __forceinline__ uint32_t scan_chunk(const fcfcg_launch &L,
+template <int GEOM, int BIN, bool LIMIT>
+__device__ __forceinline__ uint32_t scan_chunk_(const fcfcg_launch &L,
     const float4 *a, int i0, int i1, int ilim, float bx, float by,
     float bz) {
   uint32_t msk = 0;
+  const float s_lim = L.s_lim, p_lim = L.p_lim;
 #pragma unroll 4
   for (int i = i0; i < i1; i++) {
     const float4 pa = a[i];
@@ -548,14 +562,25 @@ __device__ __forceinline__ uint32_t scan_chunk(const fcfcg_launch &L,
     bool inr;
     if (BIN == FCFCG_BIN_SPI && GEOM == FCFCG_GEOM_BOX) {
       const float v = fmaf(dy, dy, dx * dx);
-      inr = (i < ilim) & (fabsf(dz) < L.p_lim) & (v < L.s_lim);
+      inr = (fabsf(dz) < p_lim) & (v < s_lim);
     } else {
       const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-      inr = (i < ilim) & (v < L.s_lim);
+      inr = v < s_lim;
     }
+    if (LIMIT) inr &= (i < ilim);
     msk |= (uint32_t) inr << (i - i0);
   }
   return msk;
+}
+
+/* The i < ilim test only matters in the chunk's own cell (auto counts). */
+template <int GEOM, int BIN>
+__device__ __forceinline__ uint32_t scan_chunk(const fcfcg_launch &L,
+    const float4 *a, int i0, int i1, int ilim, float bx, float by,
+    float bz) {
+  if (__all_sync(FULLMASK, ilim >= i1))
+    return scan_chunk_<GEOM, BIN, false>(L, a, i0, i1, ilim, bx, by, bz);
+  return scan_chunk_<GEOM, BIN, true>(L, a, i0, i1, ilim, bx, by, bz);
 }
 
 /*
@@ -578,7 +603,10 @@ k_count32(const fcfcg_launch L) {
   __shared__ uint32_t sh_chunk;
   uint16_t *fs = (uint16_t *) smem;
   uint16_t *fp = fs + L.nfs;
-  size_t hoff = ((size_t) (L.nfs + L.nfp) * sizeof(uint16_t) + 15) & ~(size_t) 15;
+  float *fse = (float *) (smem + (((size_t) (L.nfs + L.nfp) * 2 + 3) & ~(size_t) 3));
+  float *fpe = fse + L.nsb + 1;
+  size_t hoff = (size_t) ((unsigned char *) (fpe + (L.npb ? L.npb + 1 : 0)) - smem);
+  hoff = (hoff + 15) & ~(size_t) 15;
   uint32_t *h = (uint32_t *) (smem + hoff);
   size_t soff = hoff + (L.hist_smem ? (size_t) L.ntot * (WT ? 8 : 4) : 0);
   soff = (soff + 15) & ~(size_t) 15;
@@ -605,6 +633,9 @@ k_count32(const fcfcg_launch L) {
   }
   for (int i = threadIdx.x; i < L.nfs; i += blockDim.x) fs[i] = L.fs[i];
   for (int i = threadIdx.x; i < L.nfp; i += blockDim.x) fp[i] = L.fp[i];
+  for (int i = threadIdx.x; i <= L.nsb; i += blockDim.x) fse[i] = L.fse[i];
+  if (L.npb)
+    for (int i = threadIdx.x; i <= L.npb; i += blockDim.x) fpe[i] = L.fpe[i];
   if (L.hist_smem)
     for (long i = threadIdx.x; i < L.ntot * (WT ? 2 : 1); i += blockDim.x) h[i] = 0;
 
@@ -759,7 +790,8 @@ k_count32(const fcfcg_launch L) {
           const uint32_t e = (uint32_t) lane * np + k;
           if (e < nr)
             bin_pair<GEOM, BIN, WT>(L, S, S.q[e], first, cx, cy, cz, c2x, c2y,
-                                    c2z, fs, fp, h, n_in, n_q, n_inline);
+                                    c2z, fs, fp, fse, fpe, h, n_in, n_q,
+                                    n_inline);
         }
         __syncwarp();
       }
@@ -919,7 +951,7 @@ extern "C" int fcfcg_k_count(void *stream, const fcfcg_launch *L,
     threads = CT_THREADS;
   } else {
     f = pick32(L->geometry, L->bintype, L->withwt);
-    size_t tab = (((size_t) (L->nfs + L->nfp) * 2) + 15) & ~(size_t) 15;
+    size_t tab = fcfcg_k_count32_tab_bytes(L->nfs, L->nfp, L->nsb, L->npb);
     smem = tab + (L->hist_smem ? (size_t) L->ntot * (L->withwt ? 8 : 4) : 0);
     smem = ((smem + 15) & ~(size_t) 15) + stage_bytes(L->nsten, L->withwt);
     threads = CT32_THREADS;
@@ -936,6 +968,14 @@ extern "C" int fcfcg_k_count(void *stream, const fcfcg_launch *L,
   if (smem_used) *smem_used = smem;
   f<<<nsm * per_sm, threads, smem, (cudaStream_t) stream>>>(*L);
   return (int) cudaGetLastError();
+}
+
+/* Shared memory of the FP32 tables and edges (aligned for the histogram). */
+extern "C" size_t fcfcg_k_count32_tab_bytes(int nfs, int nfp, int nsb,
+    int npb) {
+  size_t n = (((size_t) (nfs + nfp) * 2 + 3) & ~(size_t) 3);
+  n += sizeof(float) * ((size_t) nsb + 1 + (npb ? (size_t) npb + 1 : 0));
+  return (n + 15) & ~(size_t) 15;
 }
 
 /* Shared memory the FP32 kernel needs beyond its histogram. */

@@ -47,6 +47,7 @@ struct fcfcg_ctx {
   uint32_t *cfill, *scan_tmp, *cchunk, *chunks;
   size_t cfill_cap, scan_cap, cchunk_cap, chunk_cap;
   uint16_t *d_fs, *d_fp, *d_rs, *d_rp;
+  float *d_fse, *d_fpe;
   double *d_s2edge, *d_pedge;
   int *d_sten;
   float *d_stenD;
@@ -61,6 +62,9 @@ struct fcfcg_ctx {
   cudaEvent_t ev[5];
   int sten[4 * FCFCG_MAX_STENCIL];
   float stD[4 * FCFCG_MAX_STENCIL];
+  /* autotuned grid refinement, keyed on the expected neighbours per object */
+  int tuned_k;
+  int tuned_key;
 };
 
 static void set_err(fcfcg_ctx *c, const char *fmt, ...) {
@@ -155,7 +159,8 @@ void fcfcg_destroy(fcfcg_ctx *c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (int i = 0; i < FCFCG_MAX_SLOT; i++) slot_free(c->slot + i);
-    void *p[] = {c->cfill, c->scan_tmp, c->cchunk, c->chunks, c->d_fs,
+    void *p[] = {c->cfill, c->scan_tmp, c->cchunk, c->chunks, c->d_fse,
+                 c->d_fpe, c->d_fs,
                  c->d_fp, c->d_rs, c->d_rp, c->d_s2edge, c->d_pedge,
                  c->d_sten, c->d_stenD, c->d_cnt, c->d_wt, c->d_stats,
                  c->d_bbox, c->d_wd, c->d_head, c->d_queue};
@@ -215,6 +220,8 @@ int fcfcg_create(const fcfcg_binning *cfg, int device, fcfcg_ctx **out) {
   if (b->s.ftab) {
     rc = upload(c, (void **) &c->d_fs, b->s.ftab, sizeof(uint16_t) * b->s.nftab);
     if (rc) return rc;
+    rc = upload(c, (void **) &c->d_fse, b->s.fedge, sizeof(float) * (b->s.nbin + 1));
+    if (rc) return rc;
   }
   if (b->bintype == FCFCG_BIN_SPI) {
     rc = upload(c, (void **) &c->d_rp, b->p.rtab, sizeof(uint16_t) * b->p.nrtab);
@@ -225,6 +232,9 @@ int fcfcg_create(const fcfcg_binning *cfg, int device, fcfcg_ctx **out) {
     if (b->p.ftab) {
       rc = upload(c, (void **) &c->d_fp, b->p.ftab,
                   sizeof(uint16_t) * b->p.nftab);
+      if (rc) return rc;
+      rc = upload(c, (void **) &c->d_fpe, b->p.fedge,
+                  sizeof(float) * (b->p.nbin + 1));
       if (rc) return rc;
     }
   }
@@ -444,7 +454,14 @@ typedef struct {
   double reach[3];     /* largest separation along each axis that counts */
   double reach3;       /* largest 3D separation that counts */
   int k;
+  int key;             /* autotuning key */
 } grid_t;
+
+/* Autotuning key: log2 of the mean number of objects in a reach box. */
+static int tune_key(double density, const double reach[3]) {
+  double v = density * reach[0] * reach[1] * reach[2];
+  return (int) floor(log2(v > 1e-30 ? v : 1e-30) + 0.5);
+}
 
 static double box_volume(const double v[3]) { return v[0] * v[1] * v[2]; }
 
@@ -498,7 +515,10 @@ static int grid_setup(fcfcg_ctx *c, grid_t *g, const slot_t *A,
   double ext[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
   double vol = box_volume(ext);
   double density = (double) B->n / (vol > 0 ? vol : 1);
-  int k = c->kcell ? c->kcell : pick_k(density, r3);
+  g->key = tune_key(density, g->reach);
+  int k = c->kcell;
+  if (!k) k = (c->tuned_k && c->tuned_key == g->key) ? c->tuned_k
+                                                      : pick_k(density, r3);
   g->k = k;
   const double maxcells = 16.0 * 1024 * 1024;
   double scale = 1;
@@ -699,15 +719,21 @@ static int fp32_bounds(const fcfcg_ctx *c, const grid_t *g, double dmax,
     L->s_lim = (float) (smax2 + Es + 1e-6 * (1 + smax2));
   }
   L->Emax = (float) (Es * 1.01);
-  if (!(Es < 0.45) || !(Ep < 0.45)) return -1;
   if (b->s.nbin > FCFCG_FTAB_MAXBIN || !b->s.ftab) return -1;
   if (b->bintype == FCFCG_BIN_SPI &&
       (b->p.nbin > FCFCG_FTAB_MAXBIN || !b->p.ftab))
     return -1;
+  /* windows below half a table cell */
+  if (!(Es < 0.45 * ldexp(1.0, b->s.fshift))) return -1;
+  if (b->bintype == FCFCG_BIN_SPI && !(Ep < 0.45 * ldexp(1.0, b->p.fshift)))
+    return -1;
   /* the FP32 tables must cover every value below the limits */
-  if ((double) L->s_lim >= (double) (b->s.foff + b->s.nftab - 1)) return -1;
+  if ((double) L->s_lim * ldexp(1.0, -b->s.fshift) >=
+      (double) (b->s.foff + b->s.nftab - 1))
+    return -1;
   if (b->bintype == FCFCG_BIN_SPI && box &&
-      (double) L->p_lim >= (double) (b->p.foff + b->p.nftab - 1))
+      (double) L->p_lim * ldexp(1.0, -b->p.fshift) >=
+          (double) (b->p.foff + b->p.nftab - 1))
     return -1;
   return 0;
 }
@@ -843,14 +869,20 @@ int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
     L.fs = c->d_fs;
     L.nfs = (int) b->s.nftab;
     L.fsoff = (int) b->s.foff;
+    L.fsinv = (float) ldexp(1.0, -b->s.fshift);
+    L.fse = c->d_fse;
+    L.nsb = b->s.nbin;
     if (b->bintype == FCFCG_BIN_SPI) {
       L.fp = c->d_fp;
       L.nfp = (int) b->p.nftab;
       L.fpoff = (int) b->p.foff;
+      L.fpinv = (float) ldexp(1.0, -b->p.fshift);
+      L.fpe = c->d_fpe;
+      L.npb = b->p.nbin;
     }
   }
   size_t tabbytes = (prec == FCFCG_PREC_FP32_RECHECK)
-      ? (((size_t) (L.nfs + L.nfp) * 2 + 15) & ~(size_t) 15) : 0;
+      ? fcfcg_k_count32_tab_bytes(L.nfs, L.nfp, L.nsb, L.npb) : 0;
   size_t hbytes = (size_t) b->ntot * (withwt ? 8 : 4);
   size_t stage = (prec == FCFCG_PREC_FP32_RECHECK)
       ? fcfcg_k_count32_stage(nsten, withwt) : 0;
@@ -953,6 +985,55 @@ const fcfcg_bins *fcfcg_ctx_bins(const fcfcg_ctx *c) {
 
 const double *fcfcg_ctx_box_raw(const fcfcg_ctx *c) {
   return c ? c->bins.box_raw : NULL;
+}
+
+int fcfcg_autotune(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
+    int *best_k, double *best_ms) {
+  if (!c || c->host_only) return FCFCG_ERR_ARG;
+  const long ntot = c->bins.ntot;
+  int64_t *ic = malloc(sizeof(int64_t) * ntot);
+  double *wc = malloc(sizeof(double) * ntot);
+  if (!ic || !wc) {
+    free(ic);
+    free(wc);
+    return FCFCG_ERR_MEMORY;
+  }
+  const int saved = c->kcell;
+  int bk = 0, key = 0, rc = FCFCG_OK;
+  double bms = 1e300;
+  for (int k = 1; k <= 5; k++) {
+    c->kcell = k;
+    double ms = 0;
+    for (int rep = 0; rep < 2 && rc == FCFCG_OK; rep++) {
+      rc = fcfcg_count(c, sa, sb, isauto, withwt, FCFCG_PREC_FP32_RECHECK,
+                       ic, wc);
+      ms = c->stats.ms_count + c->stats.ms_recheck;
+    }
+    if (rc == FCFCG_ERR_UNSUPPORTED) {   /* stencil too large: stop here */
+      rc = FCFCG_OK;
+      break;
+    }
+    if (rc) break;
+    if (ms < bms) {
+      bms = ms;
+      bk = k;
+    }
+  }
+  c->kcell = saved;
+  if (rc == FCFCG_OK && bk) {
+    /* the key of this catalogue pair, as the grid set-up computes it */
+    grid_t g;
+    memset(&g, 0, sizeof g);
+    grid_setup(c, &g, c->slot + sa, c->slot + sb);
+    key = g.key;
+    c->tuned_k = bk;
+    c->tuned_key = key;
+  }
+  free(ic);
+  free(wc);
+  if (best_k) *best_k = bk;
+  if (best_ms) *best_ms = bms;
+  return rc;
 }
 
 int fcfcg_stats_get(const fcfcg_ctx *c, fcfcg_stats *out) {

@@ -18,11 +18,15 @@ extern "C" {
 #define FCFCG_CHUNK 32            /* chunk length of the FP64 kernel */
 #define FCFCG_CHUNK32 64          /* chunk length of the FP32 kernel */
 #define FCFCG_MAX_STENCIL 4096
-#define FCFCG_FTAB_BIN_MASK 0x1FFFu
-#define FCFCG_FTAB_LO 0x2000u     /* an edge lies in [i - 1/2, i] */
-#define FCFCG_FTAB_HI 0x4000u     /* an edge lies in [i + 1, i + 3/2] */
-#define FCFCG_FTAB_CX 0x8000u     /* an edge lies strictly inside (i, i + 1) */
-#define FCFCG_FTAB_MAXBIN 8190    /* largest bin index an FP32 table holds */
+/* FP32 edge-window tables: one uint16 per cell of width w = 2^-shift units
+ * of the binned quantity; cell i covers [i w, (i + 1) w). */
+#define FCFCG_FTAB_BIN_MASK 0x0FFFu /* bin at the cell start, or "out" */
+#define FCFCG_FTAB_LO 0x1000u     /* an edge lies in [i w - w/2, i w] */
+#define FCFCG_FTAB_HI 0x2000u     /* an edge lies in [(i+1) w, (i+1) w + w/2] */
+#define FCFCG_FTAB_CX1 0x4000u    /* exactly one edge strictly inside */
+#define FCFCG_FTAB_CXM 0x8000u    /* several edges strictly inside */
+#define FCFCG_FTAB_MAXBIN 4094    /* largest bin index an FP32 table holds */
+#define FCFCG_FTAB_MAXLEN 4096    /* cells of an FP32 table */
 
 /*
  * One binned quantity (s^2, s_perp^2, pi or pi^2), as FCFC looks it up:
@@ -36,7 +40,9 @@ typedef struct {
   uint16_t *rtab;        /* reference table (host) */
   long nrtab, roff;
   uint16_t *ftab;        /* FP32 window table (host) */
-  long nftab, foff;
+  long nftab, foff;      /* cells, index of the first cell */
+  int fshift;            /* cell width 2^fshift units */
+  float *fedge;          /* nbin + 1 edges rounded to FP32 (host) */
   double vmin, vmax;     /* edge[0], edge[nbin] */
   int min0;              /* edge[0] == 0: no lower range check (smin0) */
 } fcfcg_axis;
@@ -96,6 +102,9 @@ typedef struct {
   /* FP32 tables (copied to shared memory) */
   const uint16_t *fs, *fp;
   int nfs, nfp, fsoff, fpoff;
+  float fsinv, fpinv;          /* 1 / cell width of the FP32 tables */
+  const float *fse, *fpe;      /* FP32 edges (nbin + 1 each) */
+  int nsb, npb;                /* bins of the s and pi axes */
   float s_lim, p_lim;          /* values at/above: out of range for sure */
   float K0, K1, K2;            /* E(s^2) = K2 s^2 + K1 s + K0 */
   float P0, P1, P2;            /* E(pi) (box) or E(pi^2) (survey) */
@@ -141,6 +150,7 @@ int fcfcg_k_chunks(void *stream, const uint32_t *cstart, uint32_t ncell,
     uint32_t clen, uint32_t *cchunk, uint32_t *scan_tmp, size_t scan_tmp_len,
     uint32_t *chunks, uint32_t *nchunk_out);
 size_t fcfcg_k_count32_stage(int nsten, int withwt);
+size_t fcfcg_k_count32_tab_bytes(int nfs, int nfp, int nsb, int npb);
 int fcfcg_k_bbox(void *stream, size_t n, const double *x, const double *y,
     const double *z, unsigned long long *bits6);
 int fcfcg_k_count(void *stream, const fcfcg_launch *L, int precision,

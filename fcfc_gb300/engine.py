@@ -131,6 +131,17 @@ class PairCounter:
     def set_cells_per_smax(self, k: int):
         self._check(self.lib.fcfcg_set_cells_per_smax(self.h, int(k)))
 
+    def autotune(self, a: int, b: int | None = None, weighted=False):
+        """Time the FP32 count at 1..5 cells per maximum separation and keep
+        the fastest for catalogues of this density; returns (k, ms)."""
+        isauto = b is None or b == a
+        k = C.c_int()
+        ms = C.c_double()
+        self._check(self.lib.fcfcg_autotune(self.h, a, a if b is None else b,
+                                            int(isauto), int(bool(weighted)),
+                                            C.byref(k), C.byref(ms)))
+        return k.value, ms.value
+
     # -- counting -----------------------------------------------------------
     def count_pairs(self, a: int, b: int | None = None, weighted=False,
                     precision=PREC_FP32_RECHECK, out=None):

@@ -182,6 +182,16 @@ int fcfcg_stats_get(const fcfcg_ctx *ctx, fcfcg_stats *out);
 /* Grid refinement: cells per maximum separation (0 = automatic). */
 int fcfcg_set_cells_per_smax(fcfcg_ctx *ctx, int k);
 
+/*
+ * Autotune the grid refinement for this binning and catalogue pair: times
+ * the FP32 count at 1..5 cells per maximum separation and keeps the fastest
+ * for catalogues of the same number density (key: log2 of the mean number
+ * of objects within the maximum separation box).  Later automatic counts of
+ * matching density use it.
+ */
+int fcfcg_autotune(fcfcg_ctx *ctx, int slot_a, int slot_b, int isauto,
+    int withwt, int *best_k, double *best_ms);
+
 /* ---------------- post-processing (src/fcfc/2pt_box/eval_cf.c) ----------- */
 
 /* Normalisation of eval_pairs (eval_cf.c:125-149): auto n(n-1) or W(W-1),
