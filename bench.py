@@ -205,11 +205,10 @@ def run_reference(args, rank, world):
     return 0
 
 
-def cpu_baseline_sample():
-    """A short run of the CPU restatement (10-30 s of CPU work)."""
+def cpu_baseline_sample(x, w, box):
+    """The CPU restatement of FCFC's counter (oracle/, OpenMP on every host
+    core) on the whole workload, one weighted step: 10-30 s of CPU work."""
     from oracle import fcfc_oracle as fo
-    box = 1000.0
-    x, w = workload(box=box, nparent=int(round(20000 * (box / BOX) ** 3)), seed=3)
     b1 = fo.Bins(False, 1, ns=40, smin=0, ds=5, nmu=100, box=box)
     b2 = fo.Bins(False, 2, ns=40, sedges=LOGBINS, np_=40, pmin=0, dpi=1, box=box)
     n_in = int(b1.count(x, mode=3).sum() + b2.count(x, mode=3).sum())
@@ -219,9 +218,9 @@ def cpu_baseline_sample():
     dt = time.perf_counter() - t0
     return {"value": n_in / dt, "unit": UNIT, "cores": os.cpu_count() or 1,
             "kind": "port",
-            "sample": "Neyman-Scott box L=%g Mpc/h, %d points, weighted DD "
-                      "(s,mu)+(s_perp,pi), %d in-range pairs, %.2f s" %
-                      (box, len(x), n_in, dt)}
+            "sample": "the full workload (%d points, L=%g Mpc/h), one weighted "
+                      "DD (s,mu)+(s_perp,pi) step, %d in-range pairs, %.2f s" %
+                      (len(x), box, n_in, dt)}
 
 
 def main():
@@ -390,7 +389,7 @@ def main():
         "gpu_launches": int(launches_total),
     }
     if rank == 0 and not args.no_cpu:
-        out["cpu_baseline"] = cpu_baseline_sample()
+        out["cpu_baseline"] = cpu_baseline_sample(x, w, box)
     if dist:
         dist.barrier()
     if rank == 0:
