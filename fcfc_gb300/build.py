@@ -18,9 +18,10 @@ LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libfcfcg.so")
 
-CU_SOURCES = ["prep.cu", "count.cu"]
-C_SOURCES = ["bins.c", "ctx.c", "epilogue.c"]
-HEADERS = ["fcfcg_internal.h", os.path.join("..", "..", "include", "fcfcg.h")]
+CU_SOURCES = ["prep.cu", "count.cu", "cnvt.cu"]
+C_SOURCES = ["bins.c", "ctx.c", "epilogue.c", "cnvt.c"]
+HEADERS = ["fcfcg_internal.h", "legauss_tab.h",
+           os.path.join("..", "..", "include", "fcfcg.h")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -41,6 +41,37 @@ class BinsInfo(C.Structure):
                 ("nstab", C.c_int64), ("nptab", C.c_int64)]
 
 
+class Cosmo(C.Structure):
+    """fcfcg_cosmo: OMEGA_M, OMEGA_LAMBDA, DE_EOS_W, CMVDST_ERR and the
+    Z_CMVDST_FILE table of FCFC_2PT's coordinate conversion."""
+    _fields_ = [("omega_m", C.c_double), ("omega_l", C.c_double),
+                ("has_omega_l", C.c_int), ("dew", C.c_double),
+                ("cmvdst_err", C.c_double), ("nsample", C.c_size_t),
+                ("z_sample", _dp), ("d_sample", _dp)]
+
+
+def make_cosmo(omega_m=0.31, omega_l=None, dew=-1.0, cmvdst_err=0.0,
+               ztable=None):
+    """Cosmo struct plus the arrays it points to (keep both alive).
+    ztable: (z, d) rows of a Z_CMVDST_FILE, which replaces integration."""
+    c = Cosmo()
+    c.omega_m = float(omega_m)
+    c.has_omega_l = omega_l is not None
+    c.omega_l = float(omega_l) if omega_l is not None else 0.0
+    c.dew = float(dew)
+    c.cmvdst_err = float(cmvdst_err)
+    keep = []
+    if ztable is not None:
+        t = np.asarray(ztable, np.float64)
+        zs = np.ascontiguousarray(t[:, 0])
+        ds = np.ascontiguousarray(t[:, 1])
+        keep = [zs, ds]
+        c.nsample = len(zs)
+        c.z_sample = zs.ctypes.data_as(_dp)
+        c.d_sample = ds.ctypes.data_as(_dp)
+    return c, keep
+
+
 class Stats(C.Structure):
     _fields_ = [("candidates", C.c_uint64), ("in_range", C.c_uint64),
                 ("rechecked", C.c_uint64), ("recheck_inline", C.c_uint64),
@@ -77,6 +108,12 @@ PROTOTYPES = {
     "fcfcg_bins_tables": (C.c_int, [P, P, P, P, P]),
     "fcfcg_load_catalog": (C.c_int, [P, C.c_int, C.c_size_t, P, P, P, P]),
     "fcfcg_load_catalog_device": (C.c_int, [P, C.c_int, C.c_size_t, P, P, P, P]),
+    "fcfcg_cnvt_coord": (C.c_int, [P, C.c_size_t, P, P, P, P, P, P,
+                                   C.POINTER(Cosmo), C.POINTER(C.c_int)]),
+    "fcfcg_load_catalog_radecz": (C.c_int, [P, C.c_int, C.c_size_t, P, P, P, P,
+                                            C.POINTER(Cosmo)]),
+    "fcfcg_load_catalog_radecz_device": (C.c_int, [P, C.c_int, C.c_size_t, P, P,
+                                                   P, P, C.POINTER(Cosmo)]),
     "fcfcg_catalog_info": (C.c_int, [P, C.c_int, C.POINTER(C.c_size_t),
                                      C.POINTER(C.c_double)]),
     "fcfcg_count": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,

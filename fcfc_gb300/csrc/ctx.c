@@ -65,6 +65,10 @@ struct fcfcg_ctx {
   /* autotuned grid refinement, keyed on the expected neighbours per object */
   int tuned_k;
   int tuned_key;
+  /* RA/Dec/z conversion scratch */
+  void *d_cnvt;
+  size_t cnvt_cap;
+  int cnvt_order;
 };
 
 static void set_err(fcfcg_ctx *c, const char *fmt, ...) {
@@ -163,7 +167,7 @@ void fcfcg_destroy(fcfcg_ctx *c) {
                  c->d_fpe, c->d_fs,
                  c->d_fp, c->d_rs, c->d_rp, c->d_s2edge, c->d_pedge,
                  c->d_sten, c->d_stenD, c->d_cnt, c->d_wt, c->d_stats,
-                 c->d_bbox, c->d_wd, c->d_head, c->d_queue};
+                 c->d_bbox, c->d_wd, c->d_head, c->d_queue, c->d_cnvt};
     for (size_t i = 0; i < sizeof p / sizeof p[0]; i++)
       if (p[i]) cudaFree(p[i]);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
@@ -299,7 +303,8 @@ int fcfcg_set_cells_per_smax(fcfcg_ctx *c, int k) {
 /* Catalogues.                                                               */
 
 static int load_common(fcfcg_ctx *c, int slot, size_t n, const double *x,
-    const double *y, const double *z, const double *w, int on_device) {
+    const double *y, const double *z, const double *w, int on_device,
+    const fcfcg_cosmo *cosmo) {
   if (!c || c->host_only) return FCFCG_ERR_ARG;
   if (slot < 0 || slot >= FCFCG_MAX_SLOT) {
     set_err(c, "slot %d out of range", slot);
@@ -345,6 +350,22 @@ static int load_common(fcfcg_ctx *c, int slot, size_t n, const double *x,
     iw = w ? (tw = s->w) : NULL;
   }
   (void) tx; (void) ty; (void) tz; (void) tw;
+  if (cosmo) {
+    /* RA/Dec/z -> comoving x, y, z into the slot's arrays (in place for
+     * host input), before rescaling, as tree_create orders them */
+    long nl = 0;
+    int rc = fcfcg_cnvt_device(c->stream, n, ix, iy, iz, s->x, s->y, s->z,
+                               cosmo, &c->d_cnvt, &c->cnvt_cap,
+                               &c->cnvt_order, &nl, c->err, sizeof c->err);
+    c->launches += (uint64_t) nl;
+    if (rc) {
+      s->n = 0;
+      return rc;
+    }
+    ix = s->x;
+    iy = s->y;
+    iz = s->z;
+  }
   unsigned long long *wbits = c->d_stats + 7;
   CK(cudaMemsetAsync(wbits, 0, sizeof(unsigned long long), c->stream));
   CKK(fcfcg_k_prep(c->stream, n, ix, iy, iz, iw, c->bins.rescale, survey,
@@ -429,12 +450,50 @@ static int load_common(fcfcg_ctx *c, int slot, size_t n, const double *x,
 
 int fcfcg_load_catalog(fcfcg_ctx *c, int slot, size_t n, const double *x,
     const double *y, const double *z, const double *w) {
-  return load_common(c, slot, n, x, y, z, w, 0);
+  return load_common(c, slot, n, x, y, z, w, 0, NULL);
 }
 
 int fcfcg_load_catalog_device(fcfcg_ctx *c, int slot, size_t n,
     const double *x, const double *y, const double *z, const double *w) {
-  return load_common(c, slot, n, x, y, z, w, 1);
+  return load_common(c, slot, n, x, y, z, w, 1, NULL);
+}
+
+static int radecz_ok(fcfcg_ctx *c, const fcfcg_cosmo *cosmo) {
+  if (!c || c->host_only || !cosmo) return FCFCG_ERR_ARG;
+  if (c->bins.geometry != FCFCG_GEOM_SURVEY) {
+    set_err(c, "coordinate conversion applies to survey catalogues only");
+    return FCFCG_ERR_ARG;
+  }
+  return FCFCG_OK;
+}
+
+int fcfcg_load_catalog_radecz(fcfcg_ctx *c, int slot, size_t n,
+    const double *ra, const double *dec, const double *z, const double *w,
+    const fcfcg_cosmo *cosmo) {
+  int rc = radecz_ok(c, cosmo);
+  if (rc) return rc;
+  return load_common(c, slot, n, ra, dec, z, w, 0, cosmo);
+}
+
+int fcfcg_load_catalog_radecz_device(fcfcg_ctx *c, int slot, size_t n,
+    const double *ra, const double *dec, const double *z, const double *w,
+    const fcfcg_cosmo *cosmo) {
+  int rc = radecz_ok(c, cosmo);
+  if (rc) return rc;
+  return load_common(c, slot, n, ra, dec, z, w, 1, cosmo);
+}
+
+int fcfcg_cnvt_coord(fcfcg_ctx *c, size_t n, const double *ra,
+    const double *dec, const double *z, double *x, double *y, double *zc,
+    const fcfcg_cosmo *cosmo, int *order) {
+  if (!c || c->host_only || !cosmo) return FCFCG_ERR_ARG;
+  CK(cudaSetDevice(c->device));
+  long nl = 0;
+  int rc = fcfcg_cnvt_device(c->stream, n, ra, dec, z, x, y, zc, cosmo,
+                             &c->d_cnvt, &c->cnvt_cap, order, &nl, c->err,
+                             sizeof c->err);
+  c->launches += (uint64_t) nl;
+  return rc;
 }
 
 int fcfcg_catalog_info(const fcfcg_ctx *c, int slot, size_t *n,

@@ -160,6 +160,30 @@ int fcfcg_k_flush_count(void *stream, const fcfcg_launch *L);
 size_t fcfcg_scan_tmp_len(size_t n);
 const char *fcfcg_cuda_errstr(int code);
 
+/* RA/Dec/z conversion (cnvt.c host set-up, cnvt.cu kernels). */
+typedef struct {
+  double om, ol, ok;     /* Omega_m, Omega_Lambda, Omega_k */
+  double widx;           /* 3 (1 + w), 0 for a cosmological constant */
+  double c01;            /* SPEED_OF_LIGHT * 0.01 */
+  int order;             /* Gauss-Legendre order */
+} fcfcg_cnvt_par;
+int fcfcg_k_zrange(void *stream, size_t n, const double *z,
+    unsigned long long *bits2);
+int fcfcg_k_cnvt_integr(void *stream, size_t n, const double *ra,
+    const double *dec, const double *z, double *x, double *y, double *zc,
+    const fcfcg_cnvt_par *p);
+int fcfcg_k_cnvt_spline(void *stream, size_t n, const double *ra,
+    const double *dec, const double *z, double *x, double *y, double *zc,
+    const double *zs, const double *ds, const double *ypp, size_t nsp,
+    unsigned long long *nbad);
+/* Converts n objects on `stream` (device pointers, outputs may alias the
+ * inputs); *scratch / *scratch_cap is a device buffer the call may grow;
+ * *launches counts kernel launches; a message goes to err. */
+int fcfcg_cnvt_device(void *stream, size_t n, const double *ra,
+    const double *dec, const double *z, double *x, double *y, double *zc,
+    const fcfcg_cosmo *cosmo, void **scratch, size_t *scratch_cap,
+    int *order, long *launches, char *err, size_t errlen);
+
 #ifdef __cplusplus
 }
 #endif

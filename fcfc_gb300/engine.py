@@ -121,6 +121,36 @@ class PairCounter:
             C.c_void_p(z_ptr), C.c_void_p(w_ptr) if w_ptr else None))
         self._n[slot] = (int(n), w_ptr is not None)
 
+    def load_radecz(self, slot: int, radecz, w=None, omega_m=0.31,
+                    omega_l=None, dew=-1.0, cmvdst_err=0.0, ztable=None):
+        """Load a catalogue given as RA, Dec (degrees) and redshift (N x 3
+        host array), converted to comoving coordinates on the device as
+        FCFC_2PT's COORD_CONVERT does: Gauss-Legendre integration in the given
+        cosmology, or the spline through ``ztable`` rows (z, d)."""
+        a = np.asarray(radecz, np.float64)
+        cols = [np.ascontiguousarray(a[:, k]) for k in range(3)]
+        ww = None if w is None else np.ascontiguousarray(w, np.float64)
+        cs, keep = capi.make_cosmo(omega_m, omega_l, dew, cmvdst_err, ztable)
+        self._check(self.lib.fcfcg_load_catalog_radecz(
+            self.h, int(slot), len(a), *[capi.ptr(c) for c in cols],
+            capi.ptr(ww), C.byref(cs)))
+        del keep
+        self._n[slot] = (len(a), w is not None)
+
+    def convert_device(self, n: int, ra_ptr: int, dec_ptr: int, z_ptr: int,
+                       x_ptr: int, y_ptr: int, zc_ptr: int, omega_m=0.31,
+                       omega_l=None, dew=-1.0, cmvdst_err=0.0, ztable=None):
+        """fcfcg_cnvt_coord on device arrays; returns the Gauss-Legendre order
+        (0 for the spline)."""
+        cs, keep = capi.make_cosmo(omega_m, omega_l, dew, cmvdst_err, ztable)
+        order = C.c_int()
+        vp = C.c_void_p
+        self._check(self.lib.fcfcg_cnvt_coord(
+            self.h, int(n), vp(ra_ptr), vp(dec_ptr), vp(z_ptr), vp(x_ptr),
+            vp(y_ptr), vp(zc_ptr), C.byref(cs), C.byref(order)))
+        del keep
+        return order.value
+
     def catalog_info(self, slot: int):
         n = C.c_size_t()
         sw = C.c_double()

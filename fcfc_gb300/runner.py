@@ -122,6 +122,41 @@ def read_catalog(path, formatter=None, position=("$1", "$2", "$3"),
     return x, w
 
 
+def read_ztable(path):
+    """Z_CMVDST_FILE: two numbers (z, comoving distance) per line; '#' lines
+    and blank lines are skipped, as read_ascii_table does
+    (src/io/read_ascii.c:398-500)."""
+    rows = []
+    with open(path) as f:
+        for line in f:
+            t = line.lstrip()
+            if not t or t.startswith("#"):
+                continue
+            v = t.split()
+            try:
+                rows.append((float(v[0]), float(v[1])))
+            except (IndexError, ValueError):
+                raise FCFCGError(capi.ERR_FILE, "failed to read line: %s" % t)
+    return np.array(rows, np.float64).reshape(-1, 2)
+
+
+def cosmo_from_conf(conf):
+    """The conversion keys of FCFC_2PT (load_conf.c:532-536): OMEGA_M,
+    OMEGA_LAMBDA, DE_EOS_W, CMVDST_ERR, or Z_CMVDST_FILE."""
+    if conf.get("Z_CMVDST_FILE"):
+        return dict(ztable=read_ztable(conf["Z_CMVDST_FILE"]))
+    if "OMEGA_M" not in conf:
+        raise FCFCGError(capi.ERR_CFG, "OMEGA_M is not set")
+    c = dict(omega_m=float(conf["OMEGA_M"]))
+    if "OMEGA_LAMBDA" in conf:
+        c["omega_l"] = float(conf["OMEGA_LAMBDA"])
+    if "DE_EOS_W" in conf:
+        c["dew"] = float(conf["DE_EOS_W"])
+    if "CMVDST_ERR" in conf:
+        c["cmvdst_err"] = float(conf["CMVDST_ERR"])
+    return c
+
+
 def read_bins_file(path):
     """Edges as FCFC's read_bins builds them (setup_cf.c:74-119)."""
     t = np.loadtxt(path, comments="#", ndmin=2)
@@ -160,9 +195,18 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
     wpout = _arr(conf, "PROJECTED_FILE") or []
     ofmt = int(conf.get("OUTPUT_FORMAT", 0))
     ovw = int(conf.get("OVERWRITE", 0))
-    if not box and any(_bool(v) for v in (_arr(conf, "COORD_CONVERT", ncat) or [])):
-        raise FCFCGError(capi.ERR_UNSUPPORTED,
-                         "COORD_CONVERT: give comoving coordinates")
+    cnvt = [False] * ncat
+    cosmo = None
+    if not box:
+        # one value for all catalogues, else at least one per catalogue
+        # (load_conf.c:885-906)
+        cv = _arr(conf, "COORD_CONVERT", ncat)
+        if cv:
+            if len(cv) < ncat:
+                raise FCFCGError(capi.ERR_CFG, "too few elements of COORD_CONVERT")
+            cnvt = [_bool(v) for v in cv[:ncat]]
+        if any(cnvt):
+            cosmo = cosmo_from_conf(conf)
 
     kw = dict(geometry=geometry, bintype=bintype, device=device)
     if box:
@@ -185,9 +229,6 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
     pc = PairCounter(**kw)
     # catalogues, loaded on first use
     loaded = {}
-    pi = 0
-    for i in range(ncat):
-        pass
 
     def slot_of(lab):
         i = labels.index(lab)
@@ -196,7 +237,10 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
             w = wts[i] if wts and wts[i] not in (None, "", "''", '""') else None
             x, ww = read_catalog(files[i], fmtr[i] if fmtr else None, p3, w,
                                  skip[i], cmt[i] if cmt else None)
-            pc.load(i, x, ww)
+            if cnvt[i]:
+                pc.load_radecz(i, x, ww, **cosmo)
+            else:
+                pc.load(i, x, ww)
             loaded[i] = (len(x), ww is not None)
         return i
 

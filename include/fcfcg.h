@@ -162,6 +162,64 @@ int fcfcg_load_catalog(fcfcg_ctx *ctx, int slot, size_t n, const double *x,
 int fcfcg_load_catalog_device(fcfcg_ctx *ctx, int slot, size_t n,
     const double *x, const double *y, const double *z, const double *w);
 
+/*
+ * Fiducial cosmology of FCFC_2PT's coordinate conversion (COORD_CONVERT = T):
+ * the keys OMEGA_M, OMEGA_LAMBDA, DE_EOS_W, CMVDST_ERR and Z_CMVDST_FILE
+ * (src/fcfc/2pt/load_conf.c:532-536), checked as check_cosmo and conf_verify
+ * check them (load_conf.c:700-735, 925-933).
+ *   omega_m       0 < omega_m <= 1.
+ *   omega_l       >= 0, used when has_omega_l; otherwise flat
+ *                 (Omega_Lambda = 1 - omega_m, Omega_k = 0).
+ *   dew           dark-energy w <= -1/3; 0 selects -1 (a cosmological
+ *                 constant, FCFC's default).
+ *   cmvdst_err    integration tolerance >= DBL_EPSILON; 0 selects 1e-8.
+ *   nsample, z_sample, d_sample   the (z, comoving distance) table of
+ *                 Z_CMVDST_FILE, host arrays in any row order (sorted by z
+ *                 inside, stably, as FCFC's timsort does); nsample = 0
+ *                 selects Gauss-Legendre integration instead.
+ */
+typedef struct {
+  double omega_m;
+  double omega_l;
+  int has_omega_l;
+  double dew;
+  double cmvdst_err;
+  size_t nsample;
+  const double *z_sample;
+  const double *d_sample;
+} fcfcg_cosmo;
+
+/*
+ * RA, Dec (degrees) and redshift to comoving x, y, z (Mpc/h) on the device,
+ * FP64: replaces cnvt_coord (src/fcfc/2pt/cnvt_coord.c:383-441).  With
+ * integration the Gauss-Legendre order is chosen as cnvt_legauss_order does
+ * (:267-307: the smallest order, from 4, at which consecutive orders agree to
+ * cmvdst_err on 128 redshifts spanning the catalogue) and returned in *order
+ * (may be NULL; 0 for the spline).  All six arrays are device pointers of n
+ * FP64 elements; x/y/zc may alias ra/dec/z.  The call synchronises the
+ * context's stream.  Errors: FCFCG_ERR_DATA for a negative or non-finite
+ * redshift (FCFC exits on a negative one); FCFCG_ERR_CNVT when the
+ * integration does not converge by order 32, the table has fewer than two
+ * rows, or a redshift lies outside the table (FCFC would carry an infinite
+ * distance on); FCFCG_ERR_CFG for a cosmology FCFC rejects.
+ */
+int fcfcg_cnvt_coord(fcfcg_ctx *ctx, size_t n, const double *ra,
+    const double *dec, const double *z, double *x, double *y, double *zc,
+    const fcfcg_cosmo *cosmo, int *order);
+
+/*
+ * Load a catalogue given as RA, Dec, redshift: converted on the device
+ * (fcfcg_cnvt_coord), then loaded as fcfcg_load_catalog does — FCFC_2PT's
+ * tree_create order (src/fcfc/2pt/build_tree.c:237-262).  Survey contexts
+ * only.  *_device takes device pointers.
+ */
+int fcfcg_load_catalog_radecz(fcfcg_ctx *ctx, int slot, size_t n,
+    const double *ra, const double *dec, const double *z, const double *w,
+    const fcfcg_cosmo *cosmo);
+int fcfcg_load_catalog_radecz_device(fcfcg_ctx *ctx, int slot, size_t n,
+    const double *ra, const double *dec, const double *z, const double *w,
+    const fcfcg_cosmo *cosmo);
+
 /* Number of objects and sum of weights (n when unweighted) of a slot. */
 int fcfcg_catalog_info(const fcfcg_ctx *ctx, int slot, size_t *n,
     double *sumw);

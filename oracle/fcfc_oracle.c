@@ -24,6 +24,12 @@
  *                                        (scalar FP64 build, no FMA contraction),
  *                                        src/fcfc/2pt/metric_common.c:142-260
  *   - hybrid walk-down                   src/fcfc/2pt_box/metric_common.c:56-64
+ *   - RA/Dec/z -> comoving coordinates   src/fcfc/2pt/cnvt_coord.c:113-186
+ *                                        (redshift samples), :202-250
+ *                                        (integrand, Gauss-Legendre sum),
+ *                                        :267-307 (order), :321-337
+ *                                        (integration), :58-95 (spline
+ *                                        lookup), src/math/cspline.c:34-110
  *
  * The dual k-d tree of the reference (src/fcfc/2pt_box/dual_tree.c) only
  * decides which pairs are visited; every visited pair is binned by the
@@ -743,4 +749,158 @@ oom:
   fco_cat_free(&A);
   if (!isauto) fco_cat_free(&B);
   return -1;
+}
+
+/* ------------------------------------------------------------------------ */
+/* RA/Dec/z -> comoving coordinates (COORD_CONVERT), FP64 with the C        */
+/* library's cos/sin/pow/sqrt, in the reference's operation order.  The     */
+/* Gauss-Legendre nodes and weights are the engine's generated table, whose  */
+/* every entry equals the reference's legauss.c (checked by the generator).  */
+
+#include "../fcfc_gb300/csrc/legauss_tab.h"
+
+static const double fco_glx[FCFCG_GL_LEN] = FCFCG_GL_X_INIT;
+static const double fco_glw[FCFCG_GL_LEN] = FCFCG_GL_W_INIT;
+
+typedef struct { double om, ol, ok, widx; } fco_cosmo;
+
+/* cnvt_integrand, cnvt_coord.c:202-212 */
+static double fco_integrand(const fco_cosmo *c, double z) {
+  double z1 = z + 1;
+  double z2 = z1 * z1;
+  double d = c->om * z2 * z1;
+  if (c->ok) d += c->ok * z2;
+  if (c->widx) d += c->ol * pow(z1, c->widx);
+  else d += c->ol;
+  d = 299792.458 * 0.01 / sqrt(d);
+  return d;
+}
+
+/* cnvt_legauss, cnvt_coord.c:227-250 */
+static double fco_legauss(const fco_cosmo *c, int order, double z) {
+  double zp = z * 0.5;
+  double sum = 0;
+  int i;
+  for (i = FCFCG_GL_START(order);
+       i < FCFCG_GL_START(order) + (order >> 1); i++) {
+    double x = fco_glx[i];
+    double w = fco_glw[i];
+    double z1 = zp * (1 + x);
+    double z2 = zp * (1 - x);
+    sum += w * (fco_integrand(c, z1) + fco_integrand(c, z2));
+  }
+  if (order & 1) sum += fco_glw[i] * fco_integrand(c, zp);
+  return sum * zp;
+}
+
+/* cnvt_legauss_order (cnvt_coord.c:267-307) over cnvt_z_sample's 128
+ * redshifts (:113-186); -1 when no order up to 32 converges. */
+int fco_cnvt_order(double om, double ol, double ok, double widx, double err,
+    size_t n, const double *z) {
+  fco_cosmo c = {om, ol, ok, widx};
+  double zmax = -DBL_MAX, zmin = DBL_MAX;
+  for (size_t i = 0; i < n; i++) {
+    if (zmax < z[i]) zmax = z[i];
+    if (zmin > z[i]) zmin = z[i];
+  }
+  if (zmin > zmax) return -1;
+  const int num = 128;
+  int order = 0;
+  for (int i = 0; i < num; i++) {
+    double zt = zmin + i * (zmax - zmin) / (num - 1);
+    double oint, nint = 0;
+    int k = FCFCG_GL_MIN_ORDER - 1;
+    do {
+      if (k >= FCFCG_GL_MAX_ORDER) return -1;
+      oint = nint;
+      nint = fco_legauss(&c, ++k, zt);
+    } while (fabs(nint - oint) > nint * err);
+    if (order < k) order = k;
+  }
+  return order;
+}
+
+/* cnvt_coord_integr, cnvt_coord.c:321-337 (x, y, zc may alias the input) */
+void fco_cnvt_integr(double om, double ol, double ok, double widx, int order,
+    size_t n, const double *ra, const double *dec, const double *z,
+    double *x, double *y, double *zc) {
+  fco_cosmo c = {om, ol, ok, widx};
+  const double d2r = 0x1.1df46a2529d39p-6;   /* DEGREE_2_RAD */
+#ifdef _OPENMP
+#pragma omp parallel for
+#endif
+  for (size_t i = 0; i < n; i++) {
+    double a = ra[i] * d2r;
+    double b = dec[i] * d2r;
+    double dist = fco_legauss(&c, order, z[i]);
+    x[i] = dist * cos(b) * cos(a);
+    y[i] = dist * cos(b) * sin(a);
+    zc[i] = dist * sin(b);
+  }
+}
+
+/* Natural cubic spline through (zs, ds), zs sorted ascending
+ * (cspline_ypp / cspline_eval, src/math/cspline.c:34-110), evaluated as
+ * sample_interp does (cnvt_coord.c:58-72); returns the number of redshifts
+ * outside [zs[0], zs[m-1]) (their distance is HUGE_VAL). */
+size_t fco_cnvt_spline(size_t m, const double *zs, const double *ds,
+    size_t n, const double *ra, const double *dec, const double *z,
+    double *x, double *y, double *zc) {
+  double *ypp = malloc(m * sizeof(double)), *cp = malloc(m * sizeof(double));
+  double newx = zs[1], newy = ds[1];
+  double c = zs[1] - zs[0];
+  double newd = (ds[1] - ds[0]) / c;
+  cp[0] = cp[m - 1] = ypp[0] = ypp[m - 1] = 0;
+  size_t j = 1;
+  while (j < m - 1) {
+    double oldx = newx, oldy = newy, a = c, oldd = newd;
+    newx = zs[j + 1];
+    newy = ds[j + 1];
+    c = newx - oldx;
+    newd = (newy - oldy) / c;
+    double b = (c + a) * 2;
+    double invd = 1 / (b - a * cp[j - 1]);
+    double d = (newd - oldd) * 6;
+    ypp[j] = (d - a * ypp[j - 1]) * invd;
+    cp[j] = c * invd;
+    j += 1;
+  }
+  while (j) {
+    j -= 1;
+    ypp[j] -= cp[j] * ypp[j + 1];
+  }
+  const double d2r = 0x1.1df46a2529d39p-6;
+  size_t bad = 0;
+  for (size_t k = 0; k < n; k++) {
+    double v = z[k], dist;
+    size_t i = 0, l = 0, u = m - 1;
+    if (v < zs[l] || v >= zs[u]) {
+      dist = HUGE_VAL;
+      bad++;
+    } else {
+      while (l <= u) {
+        i = (l + u) >> 1;
+        if (zs[i + 1] <= v) l = i + 1;
+        else if (zs[i] > v) u = i - 1;
+        else break;
+      }
+      size_t jj = i + 1;
+      double ba = zs[jj] - zs[i];
+      double xa = v - zs[i];
+      double bx = zs[jj] - v;
+      double ba2 = ba * ba;
+      double lower = xa * ds[jj] + bx * ds[i];
+      double cc = (xa * xa - ba2) * xa * ypp[jj];
+      double dd = (bx * bx - ba2) * bx * ypp[i];
+      dist = (lower + 0x1.5555555555555p-3 * (cc + dd)) / ba;
+    }
+    double a = ra[k] * d2r;
+    double b = dec[k] * d2r;
+    x[k] = dist * cos(b) * cos(a);
+    y[k] = dist * cos(b) * sin(a);
+    zc[k] = dist * sin(b);
+  }
+  free(ypp);
+  free(cp);
+  return bad;
 }

@@ -20,6 +20,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _SRC = os.path.join(_HERE, "fcfc_oracle.c")
 _LIBDIR = os.path.join(_HERE, "lib")
 _LIB = os.path.join(_LIBDIR, "libfcfc_oracle.so")
+_DEPS = [_SRC, os.path.join(os.path.dirname(_HERE), "fcfc_gb300", "csrc",
+                            "legauss_tab.h")]
 
 BIN_ISO, BIN_SMU, BIN_SPI = 0, 1, 2
 
@@ -27,7 +29,7 @@ BIN_ISO, BIN_SMU, BIN_SPI = 0, 1, 2
 def build(force: bool = False) -> str:
     """Compile the oracle into oracle/lib/ (gcc, OpenMP, no FMA contraction)."""
     if not force and os.path.exists(_LIB) and \
-            os.path.getmtime(_LIB) >= os.path.getmtime(_SRC):
+            all(os.path.getmtime(_LIB) >= os.path.getmtime(d) for d in _DEPS):
         return _LIB
     os.makedirs(_LIBDIR, exist_ok=True)
     tmp = _LIB + ".tmp%d" % os.getpid()
@@ -66,6 +68,13 @@ def lib():
         L.fco_count.restype = C.c_int
         L.fco_count.argtypes = [P, C.c_size_t, P, P, P, P, C.c_size_t, P, P, P, P,
                                 C.c_int, C.c_int, C.c_int, C.c_int, P, P]
+        L.fco_cnvt_order.restype = C.c_int
+        L.fco_cnvt_order.argtypes = [D, D, D, D, D, C.c_size_t, P]
+        L.fco_cnvt_integr.argtypes = [D, D, D, D, C.c_int, C.c_size_t, P, P, P,
+                                      P, P, P]
+        L.fco_cnvt_spline.restype = C.c_size_t
+        L.fco_cnvt_spline.argtypes = [C.c_size_t, P, P, C.c_size_t, P, P, P, P,
+                                      P, P]
     return _lib
 
 
@@ -166,3 +175,45 @@ class Bins:
         if rc:
             raise MemoryError("oracle count failed")
         return wcnt if weighted else icnt
+
+
+def cosmo_params(omega_m, omega_l=None, dew=-1.0):
+    """(Omega_m, Omega_Lambda, Omega_k, widx) as check_cosmo and cnvt_coord
+    derive them (src/fcfc/2pt/load_conf.c:700-735, cnvt_coord.c:416)."""
+    if omega_l is None:
+        ol, ok = 1.0 - omega_m, 0.0
+    else:
+        ol, ok = float(omega_l), 1.0 - omega_m - omega_l
+    widx = 0.0 if dew == -1 else 3 * (1 + dew)
+    return float(omega_m), ol, ok, widx
+
+
+def convert_integr(radecz, omega_m, omega_l=None, dew=-1.0, err=1e-8):
+    """FCFC's COORD_CONVERT by Gauss-Legendre integration: (xyz, order)."""
+    a = np.ascontiguousarray(radecz, np.float64)
+    cols = [np.ascontiguousarray(a[:, k]) for k in range(3)]
+    p = cosmo_params(omega_m, omega_l, dew)
+    L = lib()
+    order = L.fco_cnvt_order(*p, float(err), len(a), _ptr(cols[2]))
+    if order < 0:
+        raise ValueError("integration does not converge")
+    out = [np.empty(len(a)) for _ in range(3)]
+    L.fco_cnvt_integr(*p, order, len(a), *[_ptr(c) for c in cols],
+                      *[_ptr(o) for o in out])
+    return np.stack(out, axis=1), order
+
+
+def convert_spline(radecz, zs, ds):
+    """FCFC's COORD_CONVERT through Z_CMVDST_FILE: the table is sorted stably
+    by z first (read_sample's timsort); returns (xyz, n_outside)."""
+    zs = np.asarray(zs, np.float64)
+    ds = np.asarray(ds, np.float64)
+    o = np.argsort(zs, kind="stable")
+    zs = np.ascontiguousarray(zs[o])
+    ds = np.ascontiguousarray(ds[o])
+    a = np.ascontiguousarray(radecz, np.float64)
+    cols = [np.ascontiguousarray(a[:, k]) for k in range(3)]
+    out = [np.empty(len(a)) for _ in range(3)]
+    bad = lib().fco_cnvt_spline(len(zs), _ptr(zs), _ptr(ds), len(a),
+                                *[_ptr(c) for c in cols], *[_ptr(x) for x in out])
+    return np.stack(out, axis=1), int(bad)

@@ -118,6 +118,26 @@ def survey_cases():
         bintype=1, cats={"D": np.c_[rd, wd]}, pairs=["DD"], cf=["DD"],
         poles=[0], nmu=10, sbin=dict(smin=0, smax=50, ds=5), convert=True,
         omega_m=0.31)
+    # Unweighted, so the integer counts pin the conversion bit for bit:
+    # a curved wCDM cosmology (Omega_k != 0, w != -1: the pow branch) ...
+    kw2 = dict(ra=(150.0, 160.0), dec=(20.0, 30.0), zmu=0.6, zsig=0.08,
+               zr=(0.5, 0.7))
+    rd2 = synth.survey_radecz(2000, seed=23, **kw2)
+    rr2 = synth.survey_radecz(5000, seed=24, **kw2)
+    c["survey_smu_cnvt_wcdm"] = dict(
+        bintype=1, cats={"D": rd2, "R": rr2}, pairs=["DD", "DR", "RR"],
+        cf=ls, poles=[0, 2], nmu=10, sbin=dict(smin=0, smax=40, ds=4),
+        convert=True, omega_m=0.3, omega_l=0.65, dew=-0.9, cmvdst_err=1e-10)
+    # ... and a (z, comoving distance) table given by Z_CMVDST_FILE, rows out
+    # of order, with a comment and a blank line.
+    zt = np.linspace(0.45, 0.75, 61)
+    dt = synth.comoving_distance(zt, 0.29)
+    perm = np.random.default_rng(25).permutation(len(zt))
+    c["survey_spi_cnvt_spline"] = dict(
+        bintype=2, cats={"D": rd2, "R": rr2}, pairs=["DD", "DR", "RR"],
+        cf=ls, wp=True, sbin=dict(smin=0, smax=30, ds=3),
+        pbin=dict(pmin=0, pmax=30, dpi=3), convert=True,
+        ztab=np.c_[zt[perm], dt[perm]])
     return c
 
 
@@ -148,6 +168,19 @@ def write_conf(case, tmp, exe_box):
         cnv = "T" if case.get("convert") else "F"
         lines.append("COORD_CONVERT = [%s]" % ", ".join([cnv] * len(labels)))
         lines.append("OMEGA_M = %r" % case.get("omega_m", 0.31))
+        if "omega_l" in case:
+            lines.append("OMEGA_LAMBDA = %r" % case["omega_l"])
+        if "dew" in case:
+            lines.append("DE_EOS_W = %r" % case["dew"])
+        if "cmvdst_err" in case:
+            lines.append("CMVDST_ERR = %r" % case["cmvdst_err"])
+        if "ztab" in case:
+            fn = os.path.join(tmp, "zcmv.txt")
+            with open(fn, "w") as f:
+                f.write("# z  comoving distance (Mpc/h)\n\n")
+                for zz, dd in case["ztab"]:
+                    f.write("%.17g %.17g\n" % (zz, dd))
+            lines.append("Z_CMVDST_FILE = %s" % fn)
     lines.append("BINNING_SCHEME = %d" % case["bintype"])
     lines.append("PAIR_COUNT = [%s]" % ", ".join(case["pairs"]))
     lines.append("PAIR_COUNT_FILE = [%s]" % ", ".join(
@@ -196,14 +229,32 @@ def run_case(name, case, exe):
             for p in case["pairs"]:
                 shutil.copy(os.path.join(tmp, p + ".bin"),
                             os.path.join(out, p + (".bin" if ofmt == 0 else ".txt")))
+        orders = []
+        if case.get("convert") and "ztab" not in case:
+            # the Gauss-Legendre order FCFC picks, from its verbose output
+            lines = [l for l in write_conf(case, tmp, box)
+                     if not l.startswith("VERBOSE")]
+            lines += ["OUTPUT_FORMAT = 0", "VERBOSE = T"]
+            with open(conf, "w") as f:
+                f.write("\n".join(lines) + "\n")
+            log = subprocess.run([exe, "-c", conf], check=True, env=env,
+                                 capture_output=True, text=True).stdout
+            tag = "Legendre-Gauss integration with order"
+            orders = [int(l.split(tag)[1]) for l in log.splitlines() if tag in l]
         for fn in ("xi.txt", "mp.txt", "wp.txt"):
             if os.path.exists(os.path.join(tmp, fn)):
                 shutil.copy(os.path.join(tmp, fn), os.path.join(out, fn))
         if "sfile" in case:
             shutil.copy(os.path.join(tmp, "sbins.txt"), os.path.join(out, "sbins.txt"))
+        if "ztab" in case:
+            shutil.copy(os.path.join(tmp, "zcmv.txt"), os.path.join(out, "zcmv.txt"))
     for lab, a in case["cats"].items():
         np.save(os.path.join(out, lab + ".npy"), np.ascontiguousarray(a))
-    meta = {k: v for k, v in case.items() if k not in ("cats", "sfile")}
+    meta = {k: v for k, v in case.items() if k not in ("cats", "sfile", "ztab")}
+    if "ztab" in case:
+        meta["zfile"] = "zcmv.txt"
+    if orders:
+        meta["cnvt_order"] = orders   # one per catalogue, in label order
     meta["labels"] = list(case["cats"].keys())
     meta["weighted"] = {l: bool(a.shape[1] > 3) for l, a in case["cats"].items()}
     meta["geometry"] = "box" if box else "survey"

@@ -11,9 +11,20 @@ from fcfc_gb300 import pcfile
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def case_names():
-    return sorted(d for d in os.listdir(GOLDEN)
-                  if os.path.isfile(os.path.join(GOLDEN, d, "meta.json")))
+def case_names(convert=None):
+    """Golden case names; convert=True / False keeps only the cases whose
+    catalogues are RA/Dec/z (COORD_CONVERT) / Cartesian."""
+    out = []
+    for d in sorted(os.listdir(GOLDEN)):
+        fn = os.path.join(GOLDEN, d, "meta.json")
+        if not os.path.isfile(fn):
+            continue
+        if convert is not None:
+            with open(fn) as f:
+                if bool(json.load(f).get("convert")) != convert:
+                    continue
+        out.append(d)
+    return out
 
 
 class Case:
@@ -63,6 +74,28 @@ class Case:
         if self.box:
             kw["box"] = (m["box"] * 3)[:3] if len(m["box"]) == 1 else m["box"]
         return kw
+
+    @property
+    def convert(self):
+        return bool(self.meta.get("convert"))
+
+    def cosmo(self):
+        """OMEGA_M, OMEGA_LAMBDA (None: flat), DE_EOS_W, CMVDST_ERR."""
+        m = self.meta
+        return dict(omega_m=m.get("omega_m", 0.31), omega_l=m.get("omega_l"),
+                    dew=m.get("dew", -1.0), err=m.get("cmvdst_err", 1e-8))
+
+    def ztable(self):
+        """Z_CMVDST_FILE rows (z, d) in file order, or None."""
+        if not self.meta.get("zfile"):
+            return None
+        rows = []
+        with open(os.path.join(self.dir, self.meta["zfile"])) as f:
+            for line in f:
+                t = line.strip()
+                if t and not t.startswith("#"):
+                    rows.append([float(v) for v in t.split()[:2]])
+        return np.array(rows)
 
     def xyzw(self, label):
         a = self.cats[label]

@@ -14,7 +14,7 @@ pytestmark = pytest.mark.gpu
 
 WT_RTOL = 1e-10
 
-CASES = [n for n in case_names() if not n.endswith("_cnvt")]
+CASES = case_names(convert=False)
 
 
 def engine_for(case):

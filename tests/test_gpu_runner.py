@@ -12,7 +12,7 @@ from golden_cases import Case, case_names
 
 pytestmark = pytest.mark.gpu
 
-CASES = [n for n in case_names() if not n.endswith("_cnvt")]
+CASES = case_names()
 
 
 def _write_conf(case, tmp):
@@ -38,6 +38,16 @@ def _write_conf(case, tmp):
         lines.append("WEIGHT = [%s]" % ", ".join(wts))
     if case.box:
         lines.append("BOX_SIZE = [%s]" % ", ".join(repr(v) for v in m["box"]))
+    if case.convert:
+        lines.append("COORD_CONVERT = [%s]" % ", ".join("T" for _ in m["labels"]))
+        if m.get("zfile"):
+            lines.append("Z_CMVDST_FILE = %s" % os.path.join(case.dir, m["zfile"]))
+        else:
+            lines.append("OMEGA_M = %r" % m.get("omega_m", 0.31))
+            for key, name in (("omega_l", "OMEGA_LAMBDA"), ("dew", "DE_EOS_W"),
+                              ("cmvdst_err", "CMVDST_ERR")):
+                if key in m:
+                    lines.append("%s = %r" % (name, m[key]))
     lines.append("BINNING_SCHEME = %d" % m["bintype"])
     lines.append("PAIR_COUNT = [%s]" % ", ".join(m["pairs"]))
     lines.append("PAIR_COUNT_FILE = [%s]" % ", ".join(
