@@ -72,6 +72,14 @@ def make_cosmo(omega_m=0.31, omega_l=None, dew=-1.0, cmvdst_err=0.0,
     return c, keep
 
 
+class Job(C.Structure):
+    """fcfcg_job: one periodic-box catalogue of a batch."""
+    _fields_ = [("n", C.c_size_t), ("x", _dp), ("y", _dp), ("z", _dp),
+                ("w", _dp), ("box", C.c_double * 3),
+                ("icnt", C.POINTER(C.c_int64)), ("wcnt", _dp),
+                ("sumw", C.c_double), ("status", C.c_int)]
+
+
 class Stats(C.Structure):
     _fields_ = [("candidates", C.c_uint64), ("in_range", C.c_uint64),
                 ("rechecked", C.c_uint64), ("recheck_inline", C.c_uint64),
@@ -108,6 +116,11 @@ PROTOTYPES = {
     "fcfcg_bins_tables": (C.c_int, [P, P, P, P, P]),
     "fcfcg_load_catalog": (C.c_int, [P, C.c_int, C.c_size_t, P, P, P, P]),
     "fcfcg_load_catalog_device": (C.c_int, [P, C.c_int, C.c_size_t, P, P, P, P]),
+    "fcfcg_count_batch": (C.c_int, [P, C.POINTER(Job), C.c_int, C.c_int,
+                                    C.c_int, C.c_int]),
+    "fcfcg_autotune_batch": (C.c_int, [P, C.POINTER(Job), C.c_int, C.c_int,
+                                       C.c_int, C.POINTER(C.c_int),
+                                       C.POINTER(C.c_double)]),
     "fcfcg_cnvt_coord": (C.c_int, [P, C.c_size_t, P, P, P, P, P, P,
                                    C.POINTER(Cosmo), C.POINTER(C.c_int)]),
     "fcfcg_load_catalog_radecz": (C.c_int, [P, C.c_int, C.c_size_t, P, P, P, P,

@@ -226,14 +226,14 @@ __device__ int ref_bin_survey(const fcfcg_launch &L, double x1, double y1,
  * image code of the cell pair (box).  The image shift goes to the A point,
  * or for auto counts to the point with the smaller input index. */
 __device__ int ref_bin_pair(const fcfcg_launch &L, uint32_t a, uint32_t b,
-    uint32_t code) {
+    uint32_t code, const double *box) {
   if (L.geometry == FCFCG_GEOM_SURVEY)
     return ref_bin_survey(L, L.A.x[a], L.A.y[a], L.A.z[a], L.A.s[a],
                           L.B.x[b], L.B.y[b], L.B.z[b], L.B.s[b]);
   const int wx = (int) (code & 3u) - 1, wy = (int) ((code >> 2) & 3u) - 1,
             wz = (int) ((code >> 4) & 3u) - 1;
-  const double shx = -wx * L.box[0], shy = -wy * L.box[1],
-               shz = -wz * L.box[2];
+  const double shx = -wx * box[0], shy = -wy * box[1],
+               shz = -wz * box[2];
   const double xa = L.A.x[a], ya = L.A.y[a], za = L.A.z[a];
   const double xb = L.B.x[b], yb = L.B.y[b], zb = L.B.z[b];
   double dx, dy, dz;
@@ -367,33 +367,66 @@ __device__ __forceinline__ int first_j(const WarpChunk &w, bool self,
   return t + r;
 }
 
+/* The catalogue a CTA of a batched launch is working on (shared memory):
+ * its grid, box and global histogram. */
+struct MockSh {
+  int nc[3];
+  uint32_t base;
+  double cw[3];
+  double box[3];
+  unsigned long long *g;     /* gcnt, or gwt when weighted */
+  uint32_t id;
+};
+
 /* Histogram of the FP32 kernel in shared memory: ntot u32 counts, or
- * ntot u32 low words followed by ntot s32 high words for weighted sums. */
-template <int WT>
-__device__ __forceinline__ void hist_add(const fcfcg_launch &L, uint32_t *h,
-    int bin, long long w) {
+ * ntot u32 low words followed by ntot s32 high words for weighted sums.
+ * Overflow goes to the global histogram of the current catalogue. */
+template <int WT, int BATCH>
+__device__ __forceinline__ void hist_add(const fcfcg_launch &L,
+    const MockSh *ms, uint32_t *h, int bin, long long w) {
+  unsigned long long *g = BATCH ? ms->g : (WT ? L.gwt : L.gcnt);
   if (WT) {
-    if (L.hist_smem) hist_add_fix32(h, (int *) (h + L.ntot), L.gwt, bin, w);
-    else add128(L.gwt + 2 * bin, w);
+    if (L.hist_smem) hist_add_fix32(h, (int *) (h + L.ntot), g, bin, w);
+    else add128(g + 2 * bin, w);
   } else {
-    if (L.hist_smem) hist_add_count(h, L.gcnt, bin);
-    else atomicAdd(L.gcnt + bin, 1ull);
+    if (L.hist_smem) hist_add_count(h, g, bin);
+    else atomicAdd(g + bin, 1ull);
   }
 }
 
 /* Queue a pair for the FP64 recheck; when the queue is full, bin it here. */
-template <int WT>
-__device__ __forceinline__ void enqueue(const fcfcg_launch &L, uint32_t a,
-    uint32_t b, uint32_t code, uint32_t *h, unsigned long long &n_inline) {
+template <int WT, int BATCH>
+__device__ __forceinline__ void enqueue(const fcfcg_launch &L,
+    const MockSh *ms, uint32_t a, uint32_t b, uint32_t code, uint32_t *h,
+    unsigned long long &n_inline) {
   uint32_t slot = atomicAdd(L.qcount, 1u);
   if (slot < L.qcap) {
-    *((uint4 *) L.queue + slot) = make_uint4(a, b, code, 0u);
+    *((uint4 *) L.queue + slot) = make_uint4(a, b, code, BATCH ? ms->id : 0u);
     return;
   }
   n_inline++;
-  int bin = ref_bin_pair(L, a, b, code);
+  int bin = ref_bin_pair(L, a, b, code, BATCH ? ms->box : L.box);
   if (bin < 0) return;
-  hist_add<WT>(L, h, bin, WT ? fix_prod_pair(L, a, b) : 0);
+  hist_add<WT, BATCH>(L, ms, h, bin, WT ? fix_prod_pair(L, a, b) : 0);
+}
+
+/* Add a CTA's shared histogram to a global one and clear it. */
+template <int WT>
+__device__ __forceinline__ void hist_flush(const fcfcg_launch &L,
+    uint32_t *h, unsigned long long *g) {
+  for (long i = threadIdx.x; i < L.ntot; i += blockDim.x) {
+    if (WT) {
+      const long long v = ((long long) ((int *) h)[L.ntot + i] << 32) +
+                          (long long) h[i];
+      if (v) add128(g + 2 * i, v);
+      h[i] = 0;
+      h[L.ntot + i] = 0;
+    } else {
+      const uint32_t v = h[i];
+      if (v) atomicAdd(g + i, (unsigned long long) v);
+      h[i] = 0;
+    }
+  }
 }
 
 #define CT32_THREADS 256
@@ -432,12 +465,12 @@ __host__ __device__ __forceinline__ size_t stage_bytes(int nsten, int wt) {
 }
 
 /* Image code of the neighbour cell of a stencil offset (box). */
-__device__ __forceinline__ uint32_t nb_code(const fcfcg_launch &L, int cx,
+__device__ __forceinline__ uint32_t nb_code(const int *ncell, int cx,
     int cy, int cz, int4 o) {
   int q[3] = {cx + o.x, cy + o.y, cz + o.z};
   uint32_t code = 0;
   for (int k = 0; k < 3; k++) {
-    const int n = L.ncell[k];
+    const int n = ncell[k];
     int w = 0;
     while (q[k] < 0) { q[k] += n; w--; }
     while (q[k] >= n) { q[k] -= n; w++; }
@@ -450,9 +483,10 @@ __device__ __forceinline__ uint32_t nb_code(const fcfcg_launch &L, int cx,
  * Bin one queued pair per lane.  FP32 windows decide; ambiguous pairs go to
  * the FP64 recheck queue.  c2 = twice the chunk cell's centre (survey).
  */
-template <int GEOM, int BIN, int WT>
+template <int GEOM, int BIN, int WT, int BATCH>
 __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
-    const Stage &S, uint32_t ent, uint32_t first, int cx, int cy, int cz,
+    const MockSh *ms, const Stage &S, uint32_t ent, uint32_t first, int cx,
+    int cy, int cz,
     float c2x, float c2y, float c2z, const uint16_t *fs, const uint16_t *fp,
     const float *fse, const float *fpe, uint32_t *h, uint32_t &n_in,
     uint32_t &n_q, unsigned long long &n_inline) {
@@ -532,8 +566,9 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
     n_q++;
     uint32_t code = 0;
     if (GEOM == FCFCG_GEOM_BOX)
-      code = nb_code(L, cx, cy, cz, __ldg((const int4 *) L.sten + S.bt[src]));
-    enqueue<WT>(L, ai, bj, code, h, n_inline);
+      code = nb_code(BATCH ? ms->nc : L.ncell, cx, cy, cz,
+                     __ldg((const int4 *) L.sten + S.bt[src]));
+    enqueue<WT, BATCH>(L, ms, ai, bj, code, h, n_inline);
     return;
   }
   n_in++;
@@ -544,7 +579,7 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
     w = fix_prod(wa.x, __int_as_float(wa.y), pa.w, __float_as_int(bw.y), bw.z,
                  bw.x);
   }
-  hist_add<WT>(L, h, bin, w);
+  hist_add<WT, BATCH>(L, ms, h, bin, w);
 }
 
 /* Compare a neighbour point (one per lane) with chunk points [i0, i1):
@@ -596,11 +631,13 @@ __device__ __forceinline__ uint32_t scan_chunk(const fcfcg_launch &L,
  * in-range pairs are then compacted into the warp queue and binned 32 at a
  * time, every lane busy.
  */
-template <int GEOM, int BIN, int WT>
+template <int GEOM, int BIN, int WT, int BATCH>
 __global__ void __launch_bounds__(CT32_THREADS, 4)
 k_count32(const fcfcg_launch L) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t sh_chunk;
+  __shared__ MockSh sh_mock;   /* batched launch: the current catalogue */
+  int cur = -1;
   uint16_t *fs = (uint16_t *) smem;
   uint16_t *fp = fs + L.nfs;
   float *fse = (float *) (smem + (((size_t) (L.nfs + L.nfp) * 2 + 3) & ~(size_t) 3));
@@ -653,11 +690,40 @@ k_count32(const fcfcg_launch L) {
     const uint32_t c = sh_chunk;
     if (c >= L.nchunk) break;
     const uint4 ch = __ldg(((const uint4 *) L.chunks) + c);
+    int ncl[3] = {L.ncell[0], L.ncell[1], L.ncell[2]};
+    uint32_t cbase = 0;
+    if (BATCH) {
+      /* chunks come in catalogue order: on a change of catalogue, hand the
+       * shared histogram to the previous one's global histogram */
+      const int mk = (int) ch.w;
+      if (mk != cur) {
+        if (cur >= 0 && L.hist_smem) hist_flush<WT>(L, h, sh_mock.g);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          const fcfcg_mock *M = L.mocks + mk;
+          for (int k = 0; k < 3; k++) {
+            sh_mock.nc[k] = M->ncell[k];
+            sh_mock.cw[k] = M->cw[k];
+            sh_mock.box[k] = M->box[k];
+          }
+          sh_mock.base = M->cell_base;
+          sh_mock.g = WT ? M->gwt : M->gcnt;
+          sh_mock.id = (uint32_t) mk;
+        }
+        __syncthreads();
+        cur = mk;
+      }
+      ncl[0] = sh_mock.nc[0];
+      ncl[1] = sh_mock.nc[1];
+      ncl[2] = sh_mock.nc[2];
+      cbase = sh_mock.base;
+    }
     const uint32_t cell = ch.x, first = ch.y;
+    const uint32_t lcell = cell - cbase;
     const int m = (int) ch.z;
-    const int cx = (int) (cell % (uint32_t) L.ncell[0]);
-    const int cy = (int) ((cell / (uint32_t) L.ncell[0]) % (uint32_t) L.ncell[1]);
-    const int cz = (int) (cell / ((uint32_t) L.ncell[0] * (uint32_t) L.ncell[1]));
+    const int cx = (int) (lcell % (uint32_t) ncl[0]);
+    const int cy = (int) ((lcell / (uint32_t) ncl[0]) % (uint32_t) ncl[1]);
+    const int cz = (int) (lcell / ((uint32_t) ncl[0] * (uint32_t) ncl[1]));
     const int aoff = (int) (first - __ldg(L.A.cstart + cell));
     float c2x = 0.f, c2y = 0.f, c2z = 0.f;
     if (GEOM == FCFCG_GEOM_SURVEY) {
@@ -681,7 +747,7 @@ k_count32(const fcfcg_launch L) {
           int q[3] = {cx + o.x, cy + o.y, cz + o.z};
           bool ok = true;
           for (int k = 0; k < 3; k++) {
-            const int n = L.ncell[k];
+            const int n = ncl[k];
             if (GEOM == FCFCG_GEOM_SURVEY) {
               ok &= (q[k] >= 0) & (q[k] < n);
             } else {
@@ -690,7 +756,8 @@ k_count32(const fcfcg_launch L) {
             }
           }
           if (ok) {
-            const uint32_t cb = ((uint32_t) q[2] * L.ncell[1] + q[1]) * L.ncell[0] + q[0];
+            const uint32_t cb = cbase +
+                ((uint32_t) q[2] * ncl[1] + q[1]) * ncl[0] + q[0];
             bs = __ldg(L.B.cstart + cb);
             nb = __ldg(L.B.cstart + cb + 1) - bs;
           }
@@ -730,7 +797,18 @@ k_count32(const fcfcg_launch L) {
         const uint32_t jc = p - S.pre[t];
         const uint32_t bj = S.bst[t] + jc;
         const float4 pb = Bl4[bj];
-        const float4 D = __ldg(stD + t);
+        float4 D;
+        if (BATCH) {
+          /* -offset * cell width of this catalogue, rounded as the stencil
+           * table of a single catalogue is */
+          const int4 o = __ldg(sten + t);
+          D = make_float4(__double2float_rn((double) (-o.x) * sh_mock.cw[0]),
+                          __double2float_rn((double) (-o.y) * sh_mock.cw[1]),
+                          __double2float_rn((double) (-o.z) * sh_mock.cw[2]),
+                          0.f);
+        } else {
+          D = __ldg(stD + t);
+        }
         bx = pb.x - D.x;
         by = pb.y - D.y;
         bz = pb.z - D.z;
@@ -789,9 +867,9 @@ k_count32(const fcfcg_launch L) {
         for (uint32_t k = 0; k < np; k++) {
           const uint32_t e = (uint32_t) lane * np + k;
           if (e < nr)
-            bin_pair<GEOM, BIN, WT>(L, S, S.q[e], first, cx, cy, cz, c2x, c2y,
-                                    c2z, fs, fp, fse, fpe, h, n_in, n_q,
-                                    n_inline);
+            bin_pair<GEOM, BIN, WT, BATCH>(L, &sh_mock, S, S.q[e], first, cx,
+                                           cy, cz, c2x, c2y, c2z, fs, fp,
+                                           fse, fpe, h, n_in, n_q, n_inline);
         }
         __syncwarp();
       }
@@ -813,18 +891,8 @@ k_count32(const fcfcg_launch L) {
     atomicAdd(L.stats + 3, n_inline);
   }
   __syncthreads();
-  if (L.hist_smem) {
-    for (long i = threadIdx.x; i < L.ntot; i += blockDim.x) {
-      if (WT) {
-        const long long v = ((long long) ((int *) h)[L.ntot + i] << 32) +
-                            (long long) h[i];
-        if (v) add128(L.gwt + 2 * i, v);
-      } else {
-        uint32_t v = h[i];
-        if (v) atomicAdd(L.gcnt + i, (unsigned long long) v);
-      }
-    }
-  }
+  if (L.hist_smem && (!BATCH || cur >= 0))
+    hist_flush<WT>(L, h, BATCH ? sh_mock.g : (WT ? L.gwt : L.gcnt));
 }
 
 /*
@@ -860,7 +928,7 @@ k_count64(const fcfcg_launch L) {
       for (int j = first_j(w, self, bstart); j < nb; j += w.G) {
         const uint32_t bj = bstart + (uint32_t) j;
         n_cand++;
-        int bin = ref_bin_pair(L, w.ai, bj, code);
+        int bin = ref_bin_pair(L, w.ai, bj, code, L.box);
         if (bin < 0) continue;
         n_in++;
         if (WT) {
@@ -903,11 +971,12 @@ __global__ void k_recheck(const fcfcg_launch L, uint32_t nq) {
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq;
        q += gridDim.x * blockDim.x) {
     const uint4 e = ((const uint4 *) L.queue)[q];
-    int bin = ref_bin_pair(L, e.x, e.y, e.z);
+    const fcfcg_mock *M = L.mocks ? L.mocks + e.w : NULL;
+    int bin = ref_bin_pair(L, e.x, e.y, e.z, M ? M->box : L.box);
     if (bin < 0) continue;
     n_in++;
-    if (WT) add128(L.gwt + 2 * bin, fix_prod_pair(L, e.x, e.y));
-    else atomicAdd(L.gcnt + bin, 1ull);
+    if (WT) add128((M ? M->gwt : L.gwt) + 2 * bin, fix_prod_pair(L, e.x, e.y));
+    else atomicAdd((M ? M->gcnt : L.gcnt) + bin, 1ull);
   }
   for (int o = 16; o > 0; o >>= 1)
     n_in += __shfl_xor_sync(FULLMASK, n_in, o);
@@ -918,10 +987,23 @@ __global__ void k_recheck(const fcfcg_launch L, uint32_t nq) {
 
 typedef void (*kfun_t)(const fcfcg_launch);
 
-static kfun_t pick32(int geom, int bin, int wt) {
+static kfun_t pick32(int geom, int bin, int wt, int batch) {
+  if (batch) {
+    if (geom != FCFCG_GEOM_BOX) return 0;
+#define K32B(B)                                                            \
+  if (bin == B)                                                            \
+    return wt ? (kfun_t) k_count32<FCFCG_GEOM_BOX, B, 1, 1>                \
+              : (kfun_t) k_count32<FCFCG_GEOM_BOX, B, 0, 1>;
+    K32B(FCFCG_BIN_ISO)
+    K32B(FCFCG_BIN_SMU)
+    K32B(FCFCG_BIN_SPI)
+#undef K32B
+    return 0;
+  }
 #define K32(G, B)                                                          \
   if (geom == G && bin == B)                                               \
-    return wt ? (kfun_t) k_count32<G, B, 1> : (kfun_t) k_count32<G, B, 0>;
+    return wt ? (kfun_t) k_count32<G, B, 1, 0>                             \
+              : (kfun_t) k_count32<G, B, 0, 0>;
   K32(FCFCG_GEOM_BOX, FCFCG_BIN_ISO)
   K32(FCFCG_GEOM_BOX, FCFCG_BIN_SMU)
   K32(FCFCG_GEOM_BOX, FCFCG_BIN_SPI)
@@ -950,7 +1032,7 @@ extern "C" int fcfcg_k_count(void *stream, const fcfcg_launch *L,
     smem = L->hist_smem ? (size_t) L->ntot * (L->withwt ? 8 : 4) : 0;
     threads = CT_THREADS;
   } else {
-    f = pick32(L->geometry, L->bintype, L->withwt);
+    f = pick32(L->geometry, L->bintype, L->withwt, L->mocks != NULL);
     size_t tab = fcfcg_k_count32_tab_bytes(L->nfs, L->nfp, L->nsb, L->npb);
     smem = tab + (L->hist_smem ? (size_t) L->ntot * (L->withwt ? 8 : 4) : 0);
     smem = ((smem + 15) & ~(size_t) 15) + stage_bytes(L->nsten, L->withwt);

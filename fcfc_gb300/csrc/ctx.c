@@ -42,7 +42,7 @@ struct fcfcg_ctx {
   cudaStream_t stream;
   char err[512];
   int kcell;
-  slot_t slot[FCFCG_MAX_SLOT];
+  slot_t slot[FCFCG_MAX_SLOT + 1];   /* the last one holds batches */
   /* shared scratch */
   uint32_t *cfill, *scan_tmp, *cchunk, *chunks;
   size_t cfill_cap, scan_cap, cchunk_cap, chunk_cap;
@@ -69,6 +69,16 @@ struct fcfcg_ctx {
   void *d_cnvt;
   size_t cnvt_cap;
   int cnvt_order;
+  /* batches */
+  int internal;                  /* the batch slot may be addressed */
+  fcfcg_mock *h_mock;
+  size_t h_mock_cap;
+  void *d_mock;
+  size_t d_mock_cap;
+  uint32_t *d_mbase;
+  size_t d_mbase_cap;
+  unsigned long long *d_bout, *d_bstat;
+  size_t d_bout_cap, d_bstat_cap;
 };
 
 static void set_err(fcfcg_ctx *c, const char *fmt, ...) {
@@ -162,12 +172,13 @@ void fcfcg_destroy(fcfcg_ctx *c) {
   if (!c->host_only) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
-    for (int i = 0; i < FCFCG_MAX_SLOT; i++) slot_free(c->slot + i);
+    for (int i = 0; i <= FCFCG_MAX_SLOT; i++) slot_free(c->slot + i);
     void *p[] = {c->cfill, c->scan_tmp, c->cchunk, c->chunks, c->d_fse,
                  c->d_fpe, c->d_fs,
                  c->d_fp, c->d_rs, c->d_rp, c->d_s2edge, c->d_pedge,
                  c->d_sten, c->d_stenD, c->d_cnt, c->d_wt, c->d_stats,
-                 c->d_bbox, c->d_wd, c->d_head, c->d_queue, c->d_cnvt};
+                 c->d_bbox, c->d_wd, c->d_head, c->d_queue, c->d_cnvt,
+                 c->d_mock, c->d_mbase, c->d_bout, c->d_bstat};
     for (size_t i = 0; i < sizeof p / sizeof p[0]; i++)
       if (p[i]) cudaFree(p[i]);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
@@ -176,6 +187,7 @@ void fcfcg_destroy(fcfcg_ctx *c) {
     if (c->stream) cudaStreamDestroy(c->stream);
   }
   fcfcg_bins_release(&c->bins);
+  free(c->h_mock);
   free(c);
 }
 
@@ -295,7 +307,7 @@ int fcfcg_bins_tables(const fcfcg_ctx *c, uint16_t *stab, uint16_t *ptab,
 int fcfcg_set_cells_per_smax(fcfcg_ctx *c, int k) {
   if (!c || k < 0 || k > 8) return FCFCG_ERR_ARG;
   c->kcell = k;
-  for (int i = 0; i < FCFCG_MAX_SLOT; i++) c->slot[i].grid_valid = 0;
+  for (int i = 0; i <= FCFCG_MAX_SLOT; i++) c->slot[i].grid_valid = 0;
   return FCFCG_OK;
 }
 
@@ -306,7 +318,7 @@ static int load_common(fcfcg_ctx *c, int slot, size_t n, const double *x,
     const double *y, const double *z, const double *w, int on_device,
     const fcfcg_cosmo *cosmo) {
   if (!c || c->host_only) return FCFCG_ERR_ARG;
-  if (slot < 0 || slot >= FCFCG_MAX_SLOT) {
+  if (slot < 0 || slot >= FCFCG_MAX_SLOT + c->internal) {
     set_err(c, "slot %d out of range", slot);
     return FCFCG_ERR_ARG;
   }
@@ -538,8 +550,8 @@ static int pick_k(double density, double reach) {
   return k;
 }
 
-static int grid_setup(fcfcg_ctx *c, grid_t *g, const slot_t *A,
-    const slot_t *B) {
+/* Largest separation that counts, per axis and in 3D (rescaled). */
+static void grid_reach(const fcfcg_ctx *c, grid_t *g) {
   const fcfcg_bins *b = &c->bins;
   const int box = (b->geometry == FCFCG_GEOM_BOX);
   double r3;
@@ -558,6 +570,14 @@ static int grid_setup(fcfcg_ctx *c, grid_t *g, const slot_t *A,
     g->reach[0] = g->reach[1] = g->reach[2] = r3;
   }
   g->reach3 = r3;
+}
+
+static int grid_setup(fcfcg_ctx *c, grid_t *g, const slot_t *A,
+    const slot_t *B) {
+  const fcfcg_bins *b = &c->bins;
+  const int box = (b->geometry == FCFCG_GEOM_BOX);
+  grid_reach(c, g);
+  const double r3 = g->reach3;
   double lo[3], hi[3];
   if (box) {
     for (int k = 0; k < 3; k++) {
@@ -797,6 +817,74 @@ static int fp32_bounds(const fcfcg_ctx *c, const grid_t *g, double dmax,
   return 0;
 }
 
+/* Launch fields of a sorted catalogue. */
+static void launch_cat(fcfcg_dcat *D, const slot_t *S) {
+  D->l4 = S->l4;
+  D->wq = S->wq;
+  D->x = S->sx;
+  D->y = S->sy;
+  D->z = S->sz;
+  D->s = S->ss;
+  D->w = S->sw;
+  D->id = S->sid;
+  D->cstart = S->cstart;
+  D->wexp = S->wexp;
+}
+
+/* Launch fields of the bins (FP64 reference binning), the outputs and the
+ * recheck queue. */
+static void launch_bins(const fcfcg_ctx *c, fcfcg_launch *L) {
+  const fcfcg_bins *b = &c->bins;
+  L->ns = b->ns;
+  L->nmu = b->nmu;
+  L->np = b->np;
+  L->ntot = b->ntot;
+  L->rs = c->d_rs;
+  L->rp = c->d_rp;
+  L->rsoff = b->s.roff;
+  L->rpoff = b->p.roff;
+  L->nrs = b->s.nrtab;
+  L->nrp = b->p.nrtab;
+  L->tabtype = b->s.tabtype;
+  L->s2edge = c->d_s2edge;
+  L->pedge = c->d_pedge;
+  L->s2min = b->s.vmin;
+  L->s2max = b->s.vmax;
+  L->smin0 = b->s.min0;
+  if (b->bintype == FCFCG_BIN_SPI) {
+    L->pmin = b->p.vmin;
+    L->pmax = b->p.vmax;
+    L->pmin0 = b->p.min0;
+  }
+  L->fixF = 42;
+  L->gcnt = c->d_cnt;
+  L->gwt = c->d_wt;
+  L->gwd = c->d_wd;
+  L->queue = c->d_queue;
+  L->qcount = c->d_qcount;
+  L->qcap = (uint32_t) c->qcap;
+  L->stats = c->d_stats;
+}
+
+/* Launch fields of the FP32 edge-window tables. */
+static void launch_fp32_tables(const fcfcg_ctx *c, fcfcg_launch *L) {
+  const fcfcg_bins *b = &c->bins;
+  L->fs = c->d_fs;
+  L->nfs = (int) b->s.nftab;
+  L->fsoff = (int) b->s.foff;
+  L->fsinv = (float) ldexp(1.0, -b->s.fshift);
+  L->fse = c->d_fse;
+  L->nsb = b->s.nbin;
+  if (b->bintype == FCFCG_BIN_SPI) {
+    L->fp = c->d_fp;
+    L->nfp = (int) b->p.nftab;
+    L->fpoff = (int) b->p.foff;
+    L->fpinv = (float) ldexp(1.0, -b->p.fshift);
+    L->fpe = c->d_fpe;
+    L->npb = b->p.nbin;
+  }
+}
+
 static int ensure_pinned(fcfcg_ctx *c, size_t bytes) {
   if (c->h_pinned_cap >= bytes) return FCFCG_OK;
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
@@ -810,7 +898,8 @@ static int ensure_pinned(fcfcg_ctx *c, size_t bytes) {
 int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
     int precision, int64_t *icnt, double *wcnt) {
   if (!c || c->host_only) return FCFCG_ERR_ARG;
-  if (sa < 0 || sa >= FCFCG_MAX_SLOT || sb < 0 || sb >= FCFCG_MAX_SLOT) {
+  const int nslot = FCFCG_MAX_SLOT + c->internal;
+  if (sa < 0 || sa >= nslot || sb < 0 || sb >= nslot) {
     set_err(c, "slot out of range");
     return FCFCG_ERR_ARG;
   }
@@ -878,68 +967,13 @@ int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
   L.stenD = c->d_stenD;
   L.chunks = c->chunks;
   L.chunk_head = c->d_head;
-  const slot_t *S[2] = {A, B};
-  fcfcg_dcat *D[2] = {&L.A, &L.B};
-  for (int q = 0; q < 2; q++) {
-    D[q]->l4 = S[q]->l4;
-    D[q]->wq = S[q]->wq;
-    D[q]->x = S[q]->sx;
-    D[q]->y = S[q]->sy;
-    D[q]->z = S[q]->sz;
-    D[q]->s = S[q]->ss;
-    D[q]->w = S[q]->sw;
-    D[q]->id = S[q]->sid;
-    D[q]->cstart = S[q]->cstart;
-    D[q]->wexp = S[q]->wexp;
-  }
-  L.ns = b->ns;
-  L.nmu = b->nmu;
-  L.np = b->np;
-  L.ntot = b->ntot;
-  L.rs = c->d_rs;
-  L.rp = c->d_rp;
-  L.rsoff = b->s.roff;
-  L.rpoff = b->p.roff;
-  L.nrs = b->s.nrtab;
-  L.nrp = b->p.nrtab;
-  L.tabtype = b->s.tabtype;
-  L.s2edge = c->d_s2edge;
-  L.pedge = c->d_pedge;
-  L.s2min = b->s.vmin;
-  L.s2max = b->s.vmax;
-  L.smin0 = b->s.min0;
-  if (b->bintype == FCFCG_BIN_SPI) {
-    L.pmin = b->p.vmin;
-    L.pmax = b->p.vmax;
-    L.pmin0 = b->p.min0;
-  }
-  L.fixF = 42;
-  L.gcnt = c->d_cnt;
-  L.gwt = c->d_wt;
-  L.gwd = c->d_wd;
-  L.queue = c->d_queue;
-  L.qcount = c->d_qcount;
-  L.qcap = (uint32_t) c->qcap;
-  L.stats = c->d_stats;
+  launch_cat(&L.A, A);
+  launch_cat(&L.B, B);
+  launch_bins(c, &L);
   int prec = precision;
   if (prec == FCFCG_PREC_FP32_RECHECK && fp32_bounds(c, &g, dmax, A, B, &L))
     prec = FCFCG_PREC_FP64;
-  if (prec == FCFCG_PREC_FP32_RECHECK) {
-    L.fs = c->d_fs;
-    L.nfs = (int) b->s.nftab;
-    L.fsoff = (int) b->s.foff;
-    L.fsinv = (float) ldexp(1.0, -b->s.fshift);
-    L.fse = c->d_fse;
-    L.nsb = b->s.nbin;
-    if (b->bintype == FCFCG_BIN_SPI) {
-      L.fp = c->d_fp;
-      L.nfp = (int) b->p.nftab;
-      L.fpoff = (int) b->p.foff;
-      L.fpinv = (float) ldexp(1.0, -b->p.fshift);
-      L.fpe = c->d_fpe;
-      L.npb = b->p.nbin;
-    }
-  }
+  if (prec == FCFCG_PREC_FP32_RECHECK) launch_fp32_tables(c, &L);
   size_t tabbytes = (prec == FCFCG_PREC_FP32_RECHECK)
       ? fcfcg_k_count32_tab_bytes(L.nfs, L.nfp, L.nsb, L.npb) : 0;
   size_t hbytes = (size_t) b->ntot * (withwt ? 8 : 4);
@@ -958,7 +992,7 @@ int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
   const uint32_t clen = (prec == FCFCG_PREC_FP32_RECHECK) ? FCFCG_CHUNK32
                                                           : FCFCG_CHUNK;
   CKK(fcfcg_k_chunks(c->stream, A->cstart, ncell, clen, c->cchunk,
-                     c->scan_tmp, st, c->chunks, &nchunk));
+                     c->scan_tmp, st, c->chunks, &nchunk, NULL, 0));
   c->launches += 5;
   CK(cudaEventRecord(c->ev[1], c->stream));
   CK(cudaStreamSynchronize(c->stream));
@@ -1099,4 +1133,649 @@ int fcfcg_stats_get(const fcfcg_ctx *c, fcfcg_stats *out) {
   if (!c || !out) return FCFCG_ERR_ARG;
   *out = c->stats;
   return FCFCG_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Batches of periodic-box catalogues.                                       */
+
+/* The all-FP64 comparison path: the catalogues one after the other through
+ * the internal slot, each with its own box. */
+static int batch_fp64(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
+    int on_device) {
+  fcfcg_bins *b = &c->bins;
+  double box0[3], raw0[3];
+  memcpy(box0, b->box, sizeof box0);
+  memcpy(raw0, b->box_raw, sizeof raw0);
+  fcfcg_stats tot;
+  memset(&tot, 0, sizeof tot);
+  int rc = FCFCG_OK;
+  c->internal = 1;
+  for (int j = 0; j < njobs && rc == FCFCG_OK; j++) {
+    fcfcg_job *J = jobs + j;
+    if (J->status) continue;
+    for (int k = 0; k < 3; k++) {
+      b->box_raw[k] = J->box[k];
+      b->box[k] = J->box[k] * b->rescale;
+    }
+    int e = load_common(c, FCFCG_MAX_SLOT, J->n, J->x, J->y, J->z,
+                        withwt ? J->w : NULL, on_device, NULL);
+    if (e == FCFCG_ERR_DATA) {
+      J->status = e;
+      continue;
+    }
+    if (e) {
+      rc = e;
+      break;
+    }
+    J->sumw = c->slot[FCFCG_MAX_SLOT].sumw;
+    e = fcfcg_count(c, FCFCG_MAX_SLOT, FCFCG_MAX_SLOT, 1, withwt,
+                    FCFCG_PREC_FP64, J->icnt, J->wcnt);
+    if (e) {
+      rc = e;
+      break;
+    }
+    tot.candidates += c->stats.candidates;
+    tot.in_range += c->stats.in_range;
+    tot.ms_grid += c->stats.ms_grid;
+    tot.ms_count += c->stats.ms_count;
+    tot.ms_total += c->stats.ms_total;
+  }
+  c->internal = 0;
+  c->slot[FCFCG_MAX_SLOT].grid_valid = 0;
+  memcpy(b->box, box0, sizeof box0);
+  memcpy(b->box_raw, raw0, sizeof raw0);
+  tot.precision_used = FCFCG_PREC_FP64;
+  tot.launches = c->launches;
+  c->stats = tot;
+  return rc;
+}
+
+int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
+    int precision, int on_device) {
+  if (!c || c->host_only || njobs < 0 || (njobs && !jobs))
+    return FCFCG_ERR_ARG;
+  fcfcg_bins *b = &c->bins;
+  if (b->geometry != FCFCG_GEOM_BOX) {
+    set_err(c, "batches are periodic boxes: use a box context");
+    return FCFCG_ERR_ARG;
+  }
+  if (precision != FCFCG_PREC_FP32_RECHECK && precision != FCFCG_PREC_FP64)
+    return FCFCG_ERR_ARG;
+  CK(cudaSetDevice(c->device));
+  memset(&c->stats, 0, sizeof c->stats);
+  /* per-catalogue checks of conf_verify: s_max (and pi_max) below half the
+   * box (src/fcfc/2pt_box/load_conf.c:1000-1003) */
+  const double smax_raw = b->sbin_raw[b->ns];
+  const double pmax_raw = (b->bintype == FCFCG_BIN_SPI) ? b->pbin_raw[b->np] : 0;
+  for (int j = 0; j < njobs; j++) {
+    fcfcg_job *J = jobs + j;
+    J->status = FCFCG_OK;
+    J->sumw = 0;
+    if ((withwt && !J->wcnt) || (!withwt && !J->icnt) ||
+        (J->n && (!J->x || !J->y || !J->z)) || (withwt && J->n && !J->w)) {
+      J->status = FCFCG_ERR_ARG;
+      continue;
+    }
+    for (int k = 0; k < 3; k++) {
+      if (!(J->box[k] > 0) || !isfinite(J->box[k]) ||
+          smax_raw >= J->box[k] * 0.5 ||
+          (b->bintype == FCFCG_BIN_SPI && pmax_raw >= J->box[k] * 0.5))
+        J->status = FCFCG_ERR_CFG;
+    }
+    if (!J->status) {
+      if (withwt) memset(J->wcnt, 0, sizeof(double) * b->ntot);
+      else memset(J->icnt, 0, sizeof(int64_t) * b->ntot);
+    }
+  }
+  if (precision == FCFCG_PREC_FP64)
+    return batch_fp64(c, jobs, njobs, withwt, on_device);
+
+  /* 1. catalogues side by side in the batch slot, rescaled */
+  int *acc = malloc(sizeof(int) * (njobs ? njobs : 1));
+  size_t *base = malloc(sizeof(size_t) * (njobs ? njobs + 1 : 1));
+  if (!acc || !base) {
+    free(acc);
+    free(base);
+    return FCFCG_ERR_MEMORY;
+  }
+  int rc = FCFCG_OK;
+  int na = 0;
+  size_t N = 0;
+  for (int j = 0; j < njobs; j++) {
+    if (jobs[j].status || !jobs[j].n) continue;
+    acc[na] = j;
+    base[na++] = N;
+    N += jobs[j].n;
+  }
+  base[na] = N;
+#define BFAIL(code)                                                       \
+  do {                                                                    \
+    rc = (code);                                                          \
+    goto out;                                                             \
+  } while (0)
+#define BCK(call)                                                         \
+  do {                                                                    \
+    cudaError_t e_ = (call);                                              \
+    if (e_ != cudaSuccess) {                                              \
+      set_err(c, "%s: %s", #call, cudaGetErrorString(e_));                \
+      BFAIL(FCFCG_ERR_CUDA);                                              \
+    }                                                                     \
+  } while (0)
+#define BCKK(call)                                                        \
+  do {                                                                    \
+    int e_ = (call);                                                      \
+    if (e_) {                                                             \
+      set_err(c, "%s: %s", #call, fcfcg_cuda_errstr(e_));                 \
+      BFAIL(FCFCG_ERR_CUDA);                                              \
+    }                                                                     \
+  } while (0)
+#define BGROW(ptr, capv, bytes)                                           \
+  do {                                                                    \
+    size_t cap_ = (capv);                                                 \
+    int r_ = grow(c, (void **) &(ptr), &cap_, (bytes));                   \
+    if (r_) BFAIL(r_);                                                    \
+    (capv) = cap_;                                                        \
+  } while (0)
+  if (N > 0xFFFFFFF0u) {
+    set_err(c, "batch too large (%zu objects)", N);
+    BFAIL(FCFCG_ERR_ARG);
+  }
+  if (na == 0) goto out;
+  BCK(cudaEventRecord(c->ev[0], c->stream));
+  slot_t *S = c->slot + FCFCG_MAX_SLOT;
+  S->grid_valid = 0;
+  if (S->cap < N || !S->x) {
+    slot_free(S);
+    BCK(cudaMalloc((void **) &S->x, sizeof(double) * N));
+    BCK(cudaMalloc((void **) &S->y, sizeof(double) * N));
+    BCK(cudaMalloc((void **) &S->z, sizeof(double) * N));
+    BCK(cudaMalloc((void **) &S->s, sizeof(double) * N));
+    BCK(cudaMalloc((void **) &S->w, sizeof(double) * N));
+    S->cap = N;
+  }
+  S->n = N;
+  S->has_w = withwt;
+  BGROW(c->d_bstat, c->d_bstat_cap, sizeof(unsigned long long) * 7 * na);
+  {
+    unsigned long long *init = malloc(sizeof(unsigned long long) * 7 * na);
+    if (!init) BFAIL(FCFCG_ERR_MEMORY);
+    for (int a = 0; a < na; a++) {
+      for (int k = 0; k < 3; k++) {
+        init[7 * a + k] = ~0ull;
+        init[7 * a + 3 + k] = 0;
+      }
+      init[7 * a + 6] = 0;
+    }
+    cudaError_t e = cudaMemcpy(c->d_bstat, init,
+                               sizeof(unsigned long long) * 7 * na,
+                               cudaMemcpyHostToDevice);
+    free(init);
+    BCK(e);
+  }
+  for (int a = 0; a < na; a++) {
+    const fcfcg_job *J = jobs + acc[a];
+    const size_t o = base[a], n = J->n;
+    const double *ix = J->x, *iy = J->y, *iz = J->z;
+    const double *iw = withwt ? J->w : NULL;
+    if (!on_device) {
+      BCK(cudaMemcpyAsync(S->x + o, J->x, sizeof(double) * n,
+                          cudaMemcpyHostToDevice, c->stream));
+      BCK(cudaMemcpyAsync(S->y + o, J->y, sizeof(double) * n,
+                          cudaMemcpyHostToDevice, c->stream));
+      BCK(cudaMemcpyAsync(S->z + o, J->z, sizeof(double) * n,
+                          cudaMemcpyHostToDevice, c->stream));
+      if (iw)
+        BCK(cudaMemcpyAsync(S->w + o, J->w, sizeof(double) * n,
+                            cudaMemcpyHostToDevice, c->stream));
+      ix = S->x + o;
+      iy = S->y + o;
+      iz = S->z + o;
+      iw = iw ? S->w + o : NULL;
+    }
+    BCKK(fcfcg_k_prep(c->stream, n, ix, iy, iz, iw, b->rescale, 0, S->x + o,
+                      S->y + o, S->z + o, NULL, S->w + o,
+                      c->d_bstat + 7 * a + 6));
+    BCKK(fcfcg_k_bbox(c->stream, n, S->x + o, S->y + o, S->z + o,
+                      c->d_bstat + 7 * a));
+    c->launches += 2;
+  }
+  /* 2. per-catalogue range checks, weight scales and sums */
+  unsigned long long *hb = malloc(sizeof(unsigned long long) * 7 * na);
+  if (!hb) BFAIL(FCFCG_ERR_MEMORY);
+  {
+    cudaError_t e = cudaMemcpyAsync(hb, c->d_bstat,
+                                    sizeof(unsigned long long) * 7 * na,
+                                    cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaStreamSynchronize(c->stream);
+    if (e) {
+      free(hb);
+      BCK(e);
+    }
+  }
+  int *wexp = malloc(sizeof(int) * na);
+  double *hw = NULL;
+  size_t hwcap = 0;
+  if (!wexp) {
+    free(hb);
+    BFAIL(FCFCG_ERR_MEMORY);
+  }
+  for (int a = 0; a < na; a++) {
+    fcfcg_job *J = jobs + acc[a];
+    for (int k = 0; k < 3; k++) {
+      unsigned long long lo = hb[7 * a + k], hi = hb[7 * a + 3 + k];
+      lo = (lo >> 63) ? (lo & 0x7FFFFFFFFFFFFFFFull) : ~lo;
+      hi = (hi >> 63) ? (hi & 0x7FFFFFFFFFFFFFFFull) : ~hi;
+      double mn, mx;
+      memcpy(&mn, &lo, 8);
+      memcpy(&mx, &hi, 8);
+      const double L = J->box[k] * b->rescale, tol = L * 1e-9;
+      if (!isfinite(mn) || !isfinite(mx) || mn < -tol || mx > L + tol)
+        J->status = FCFCG_ERR_DATA;
+    }
+    double wmax = 1;
+    if (withwt) memcpy(&wmax, hb + 7 * a + 6, 8);
+    if (!isfinite(wmax)) J->status = FCFCG_ERR_DATA;
+    int we = (wmax > 0) ? (int) ceil(log2(wmax)) : 0;
+    if (ldexp(1.0, we) < wmax) we++;
+    wexp[a] = we;
+    if (J->status) continue;
+    if (withwt) {
+      const double *wv = J->w;
+      if (on_device) {
+        if (hwcap < J->n) {
+          free(hw);
+          hw = malloc(sizeof(double) * J->n);
+          hwcap = hw ? J->n : 0;
+        }
+        if (!hw) {
+          free(hb);
+          free(wexp);
+          BFAIL(FCFCG_ERR_MEMORY);
+        }
+        cudaError_t e = cudaMemcpy(hw, J->w, sizeof(double) * J->n,
+                                   cudaMemcpyDeviceToHost);
+        if (e) {
+          free(hb);
+          free(wexp);
+          free(hw);
+          BCK(e);
+        }
+        wv = hw;
+      }
+      double sum = 0;
+      for (size_t i = 0; i < J->n; i++) sum += wv[i];
+      J->sumw = sum;
+    } else {
+      J->sumw = (double) J->n;
+    }
+  }
+  free(hb);
+  free(hw);
+  /* 3. grids: one refinement k for the batch, each catalogue's cells tile
+   * its own box */
+  grid_t gr;
+  memset(&gr, 0, sizeof gr);
+  grid_reach(c, &gr);
+  double vol = 0, nsum = 0;
+  for (int a = 0; a < na; a++) {
+    const fcfcg_job *J = jobs + acc[a];
+    if (J->status) continue;
+    vol += J->box[0] * J->box[1] * J->box[2] * b->rescale * b->rescale *
+           b->rescale;
+    nsum += (double) J->n;
+  }
+  const double density = nsum / (vol > 0 ? vol : 1);
+  const int key = tune_key(density, gr.reach) + 1000;   /* batch keys */
+  int k = c->kcell;
+  if (!k) k = (c->tuned_k && c->tuned_key == key) ? c->tuned_k
+                                                  : pick_k(density, gr.reach3);
+  BGROW(c->d_mbase, c->d_mbase_cap, sizeof(uint32_t) * (na + 1));
+  if (c->h_mock_cap < (size_t) na) {
+    free(c->h_mock);
+    c->h_mock = malloc(sizeof(fcfcg_mock) * na);
+    c->h_mock_cap = c->h_mock ? (size_t) na : 0;
+    if (!c->h_mock) {
+      free(wexp);
+      BFAIL(FCFCG_ERR_MEMORY);
+    }
+  }
+  uint32_t *hbase = malloc(sizeof(uint32_t) * (na + 1));
+  if (!hbase) {
+    free(wexp);
+    BFAIL(FCFCG_ERR_MEMORY);
+  }
+  grid_t gmin = gr, gmax = gr;
+  for (int d = 0; d < 3; d++) {
+    gmin.cw[d] = 1e300;
+    gmax.cw[d] = 0;
+  }
+  size_t cells = 0;
+  double xabs = 0;
+  for (int a = 0; a < na; a++) {
+    const fcfcg_job *J = jobs + acc[a];
+    fcfcg_mock *M = c->h_mock + a;
+    memset(M, 0, sizeof *M);
+    hbase[a] = (uint32_t) cells;
+    if (J->status) continue;     /* no cells: never visited */
+    size_t nc = 1;
+    for (int d = 0; d < 3; d++) {
+      const double L = J->box[d] * b->rescale;
+      const double cwt = gr.reach[d] / k * (1 + 1e-6);
+      int n = (int) floor(L / cwt);
+      if (n < 1) n = 1;
+      if (n > 4096) n = 4096;
+      M->ncell[d] = n;
+      M->cw[d] = L / n;
+      M->box[d] = L;
+      nc *= (size_t) n;
+      gmin.cw[d] = fmin(gmin.cw[d], M->cw[d]);
+      gmax.cw[d] = fmax(gmax.cw[d], M->cw[d]);
+      xabs = fmax(xabs, L);
+    }
+    M->cell_base = (uint32_t) cells;
+    cells += nc;
+    if (cells > 0x7FFFFFF0u) {
+      free(wexp);
+      free(hbase);
+      set_err(c, "batch grid too large");
+      BFAIL(FCFCG_ERR_UNSUPPORTED);
+    }
+  }
+  hbase[na] = (uint32_t) cells;
+  /* 4. one stencil for all: built for the narrowest cells (a superset of
+   * every catalogue's own); bounds for the widest */
+  int nsten = 0;
+  double dmin = 0;
+  gmin.k = gmax.k = k;
+  if (gmin.cw[0] > 1e299) {        /* every catalogue failed its checks */
+    free(wexp);
+    free(hbase);
+    goto out;
+  }
+  if ((rc = stencil_build(c, &gmin, 1, c->sten, c->stD, &nsten, &dmin))) {
+    free(wexp);
+    free(hbase);
+    goto out;
+  }
+  double dmax = 0;
+  for (int t = 0; t < nsten; t++)
+    for (int d = 0; d < 3; d++)
+      dmax = fmax(dmax, fabs((double) c->sten[4 * t + d]) * gmax.cw[d]);
+  /* 5. cell sort of every catalogue into the shared sorted arrays */
+  const size_t m = N;
+  if (S->scap < m) {
+    void *pp[] = {S->l4, S->wq, S->sx, S->sy, S->sz, S->ss, S->sw, S->sid,
+                  S->cell_of};
+    for (size_t i = 0; i < sizeof pp / sizeof pp[0]; i++)
+      if (pp[i]) cudaFree(pp[i]);
+    S->l4 = NULL;
+    S->scap = 0;
+    cudaError_t e = cudaMalloc((void **) &S->l4, sizeof(float) * 4 * m);
+    if (!e) e = cudaMalloc((void **) &S->wq, sizeof(int) * 2 * m);
+    if (!e) e = cudaMalloc((void **) &S->sx, sizeof(double) * m);
+    if (!e) e = cudaMalloc((void **) &S->sy, sizeof(double) * m);
+    if (!e) e = cudaMalloc((void **) &S->sz, sizeof(double) * m);
+    if (!e) e = cudaMalloc((void **) &S->ss, sizeof(double) * 1);
+    if (!e) e = cudaMalloc((void **) &S->sw, sizeof(double) * m);
+    if (!e) e = cudaMalloc((void **) &S->sid, sizeof(uint32_t) * m);
+    if (!e) e = cudaMalloc((void **) &S->cell_of, sizeof(uint32_t) * m);
+    if (e) {
+      free(wexp);
+      free(hbase);
+      BCK(e);
+    }
+    S->scap = m;
+  }
+  if (S->ccap < cells + 1) {
+    if (S->cstart) cudaFree(S->cstart);
+    S->cstart = NULL;
+    S->ccap = 0;
+    cudaError_t e = cudaMalloc((void **) &S->cstart,
+                               sizeof(uint32_t) * (cells + 1));
+    if (e) {
+      free(wexp);
+      free(hbase);
+      BCK(e);
+    }
+    S->ccap = cells + 1;
+  }
+  BGROW(c->cfill, c->cfill_cap, sizeof(uint32_t) * (cells + 1));
+  const size_t stl = fcfcg_scan_tmp_len(cells + 1) + 16;
+  BGROW(c->scan_tmp, c->scan_cap, sizeof(uint32_t) * stl);
+  BCK(cudaMemsetAsync(c->cfill, 0, sizeof(uint32_t) * (cells + 1), c->stream));
+  for (int a = 0; a < na; a++) {
+    const fcfcg_job *J = jobs + acc[a];
+    if (J->status) continue;
+    const fcfcg_mock *M = c->h_mock + a;
+    const size_t o = base[a];
+    BCKK(fcfcg_k_cell_batch(c->stream, J->n, S->x + o, S->y + o, S->z + o,
+                            M->ncell, M->cw, M->cell_base, S->cell_of + o,
+                            c->cfill));
+    c->launches++;
+  }
+  BCKK(fcfcg_scan(c->stream, c->cfill, cells, S->cstart, c->scan_tmp));
+  c->launches += 3;
+  BCK(cudaMemsetAsync(c->cfill, 0, sizeof(uint32_t) * (cells + 1), c->stream));
+  for (int a = 0; a < na; a++) {
+    const fcfcg_job *J = jobs + acc[a];
+    if (J->status) continue;
+    const fcfcg_mock *M = c->h_mock + a;
+    const size_t o = base[a];
+    BCKK(fcfcg_k_scatter_batch(c->stream, J->n, S->x + o, S->y + o, S->z + o,
+                               withwt ? S->w + o : NULL, withwt, wexp[a],
+                               M->ncell, M->cw, M->cell_base, (uint32_t) o,
+                               S->cell_of + o, S->cstart, c->cfill, S->l4,
+                               S->wq, S->sx, S->sy, S->sz, S->sw, S->sid));
+    c->launches++;
+  }
+  /* 6. per-catalogue histograms and the catalogue table */
+  const size_t per = (size_t) b->ntot * (withwt ? 2 : 1);
+  BGROW(c->d_bout, c->d_bout_cap, sizeof(unsigned long long) * per * na);
+  BCK(cudaMemsetAsync(c->d_bout, 0, sizeof(unsigned long long) * per * na,
+                      c->stream));
+  for (int a = 0; a < na; a++) {
+    c->h_mock[a].gcnt = withwt ? NULL : c->d_bout + per * a;
+    c->h_mock[a].gwt = withwt ? c->d_bout + per * a : NULL;
+  }
+  BGROW(c->d_mock, c->d_mock_cap, sizeof(fcfcg_mock) * na);
+  BCK(cudaMemcpyAsync(c->d_mock, c->h_mock, sizeof(fcfcg_mock) * na,
+                      cudaMemcpyHostToDevice, c->stream));
+  BCK(cudaMemcpyAsync(c->d_mbase, hbase, sizeof(uint32_t) * (na + 1),
+                      cudaMemcpyHostToDevice, c->stream));
+  /* the copies read host memory that is freed below */
+  BCK(cudaStreamSynchronize(c->stream));
+  free(hbase);
+  /* 7. launch parameters */
+  fcfcg_launch L;
+  memset(&L, 0, sizeof L);
+  L.geometry = FCFCG_GEOM_BOX;
+  L.bintype = b->bintype;
+  L.isauto = 1;
+  L.withwt = withwt;
+  for (int d = 0; d < 3; d++) {
+    L.ncell[d] = 1;
+    L.box[d] = b->box[d];
+  }
+  S->xabs = xabs;
+  S->s2abs = 0;
+  S->wexp = 0;
+  launch_cat(&L.A, S);
+  launch_cat(&L.B, S);
+  launch_bins(c, &L);
+  L.mocks = (const fcfcg_mock *) c->d_mock;
+  L.nmock = na;
+  int prec = FCFCG_PREC_FP32_RECHECK;
+  if (fp32_bounds(c, &gmax, dmax, S, S, &L)) prec = FCFCG_PREC_FP64;
+  size_t tabbytes = 0, stage = 0;
+  if (prec == FCFCG_PREC_FP32_RECHECK) {
+    launch_fp32_tables(c, &L);
+    tabbytes = fcfcg_k_count32_tab_bytes(L.nfs, L.nfp, L.nsb, L.npb);
+    stage = fcfcg_k_count32_stage(nsten, withwt);
+    if (tabbytes + stage > 200 * 1024) prec = FCFCG_PREC_FP64;
+  }
+  if (prec != FCFCG_PREC_FP32_RECHECK) {
+    /* FP32 windows too wide for these boxes: count them in FP64 */
+    free(wexp);
+    free(acc);
+    free(base);
+    return batch_fp64(c, jobs, njobs, withwt, on_device);
+  }
+  const size_t hbytes = (size_t) b->ntot * (withwt ? 8 : 4);
+  L.hist_smem = (tabbytes + stage + hbytes <= 200 * 1024);
+  L.nsten = nsten;
+  L.tzero = -1;
+  for (int t = 0; t < nsten; t++)
+    if (!c->sten[4 * t] && !c->sten[4 * t + 1] && !c->sten[4 * t + 2])
+      L.tzero = t;
+  if ((rc = upload(c, (void **) &c->d_sten, c->sten,
+                   sizeof(int) * 4 * nsten))) {
+    free(wexp);
+    goto out;
+  }
+  if ((rc = upload(c, (void **) &c->d_stenD, c->stD,
+                   sizeof(float) * 4 * nsten))) {
+    free(wexp);
+    goto out;
+  }
+  L.sten = c->d_sten;
+  L.stenD = c->d_stenD;
+  /* 8. work chunks of every catalogue, in catalogue order */
+  BGROW(c->cchunk, c->cchunk_cap, sizeof(uint32_t) * 2 * (cells + 1));
+  const size_t maxchunk = N / FCFCG_CHUNK + cells + 1;
+  BGROW(c->chunks, c->chunk_cap, sizeof(uint32_t) * 4 * maxchunk);
+  uint32_t nchunk = 0;
+  BCKK(fcfcg_k_chunks(c->stream, S->cstart, (uint32_t) cells, FCFCG_CHUNK32,
+                      c->cchunk, c->scan_tmp, stl, c->chunks, &nchunk,
+                      c->d_mbase, na));
+  c->launches += 5;
+  BCK(cudaEventRecord(c->ev[1], c->stream));
+  BCK(cudaStreamSynchronize(c->stream));
+  L.nchunk = nchunk;
+  L.chunks = c->chunks;
+  L.chunk_head = c->d_head;
+  BCK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * 4,
+                      c->stream));
+  BCK(cudaMemsetAsync(c->d_head, 0, sizeof(uint32_t) * 2, c->stream));
+  BCK(cudaEventRecord(c->ev[2], c->stream));
+  size_t smem = 0;
+  BCKK(fcfcg_k_count(c->stream, &L, prec, c->nsm, &smem));
+  c->launches += 1;
+  BCK(cudaEventRecord(c->ev[3], c->stream));
+  uint32_t nq = 0;
+  BCK(cudaMemcpyAsync(&nq, c->d_qcount, sizeof nq, cudaMemcpyDeviceToHost,
+                      c->stream));
+  BCK(cudaStreamSynchronize(c->stream));
+  if (nq > c->qcap) nq = (uint32_t) c->qcap;
+  BCKK(fcfcg_k_recheck(c->stream, &L, nq));
+  c->launches += nq ? 1 : 0;
+  BCK(cudaEventRecord(c->ev[4], c->stream));
+  /* 9. results */
+  {
+    unsigned long long *hres = malloc(sizeof(unsigned long long) * per * na);
+    unsigned long long hstats[4];
+    if (!hres) {
+      free(wexp);
+      BFAIL(FCFCG_ERR_MEMORY);
+    }
+    cudaError_t e = cudaMemcpyAsync(hres, c->d_bout,
+                                    sizeof(unsigned long long) * per * na,
+                                    cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaMemcpyAsync(hstats, c->d_stats, sizeof hstats,
+                                cudaMemcpyDeviceToHost, c->stream);
+    if (!e) e = cudaStreamSynchronize(c->stream);
+    if (e) {
+      free(hres);
+      free(wexp);
+      BCK(e);
+    }
+    for (int a = 0; a < na; a++) {
+      fcfcg_job *J = jobs + acc[a];
+      if (J->status) continue;
+      const unsigned long long *r = hres + per * a;
+      if (withwt) {
+        const int ex = 2 * wexp[a] - L.fixF;
+        for (long i = 0; i < b->ntot; i++) {
+          __int128 v = (__int128) (((unsigned __int128) r[2 * i + 1] << 64) |
+                                   (unsigned __int128) r[2 * i]);
+          J->wcnt[i] = ldexp((double) v, ex);
+        }
+      } else {
+        for (long i = 0; i < b->ntot; i++) J->icnt[i] = (int64_t) r[i];
+      }
+    }
+    free(hres);
+    fcfcg_stats *o = &c->stats;
+    o->candidates = hstats[0];
+    o->in_range = hstats[1];
+    o->rechecked = hstats[2];
+    o->recheck_inline = hstats[3];
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+    o->ms_grid = ms;
+    cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+    o->ms_count = ms;
+    cudaEventElapsedTime(&ms, c->ev[3], c->ev[4]);
+    o->ms_recheck = ms;
+    cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]);
+    o->ms_total = ms;
+    o->cells_per_smax = k;
+    o->nstencil = nsten;
+    o->nchunks = nchunk;
+    o->precision_used = prec;
+    o->launches = c->launches;
+  }
+  free(wexp);
+out:
+  free(acc);
+  free(base);
+  return rc;
+#undef BFAIL
+#undef BCK
+#undef BCKK
+#undef BGROW
+}
+
+int fcfcg_autotune_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs,
+    int withwt, int on_device, int *best_k, double *best_ms) {
+  if (!c || c->host_only) return FCFCG_ERR_ARG;
+  const int saved = c->kcell;
+  int bk = 0, rc = FCFCG_OK;
+  double bms = 1e300;
+  for (int k = 1; k <= 5 && rc == FCFCG_OK; k++) {
+    c->kcell = k;
+    double ms = 0;
+    for (int rep = 0; rep < 2 && rc == FCFCG_OK; rep++) {
+      rc = fcfcg_count_batch(c, jobs, njobs, withwt, FCFCG_PREC_FP32_RECHECK,
+                             on_device);
+      ms = c->stats.ms_count + c->stats.ms_recheck;
+    }
+    if (rc == FCFCG_ERR_UNSUPPORTED) {
+      rc = FCFCG_OK;
+      break;
+    }
+    if (rc == FCFCG_OK && ms > 0 && ms < bms) {
+      bms = ms;
+      bk = k;
+    }
+  }
+  c->kcell = saved;
+  if (rc == FCFCG_OK && bk) {
+    /* the key fcfcg_count_batch computes for this batch */
+    grid_t gr;
+    memset(&gr, 0, sizeof gr);
+    grid_reach(c, &gr);
+    const fcfcg_bins *b = &c->bins;
+    double vol = 0, nsum = 0;
+    for (int j = 0; j < njobs; j++) {
+      if (jobs[j].status || !jobs[j].n) continue;
+      vol += jobs[j].box[0] * jobs[j].box[1] * jobs[j].box[2] * b->rescale *
+             b->rescale * b->rescale;
+      nsum += (double) jobs[j].n;
+    }
+    c->tuned_k = bk;
+    c->tuned_key = tune_key(nsum / (vol > 0 ? vol : 1), gr.reach) + 1000;
+  }
+  if (best_k) *best_k = bk;
+  if (best_ms) *best_ms = bms;
+  return rc;
 }

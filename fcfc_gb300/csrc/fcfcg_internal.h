@@ -82,6 +82,17 @@ typedef struct {
   int wexp;              /* weights scaled by 2^-wexp */
 } fcfcg_dcat;
 
+/* One catalogue of a batch (periodic boxes; all share the bins and the
+ * cell stencil, each has its own box, grid and histogram). */
+typedef struct {
+  int ncell[3];
+  uint32_t cell_base;    /* global index of the catalogue's first cell */
+  double cw[3];          /* cell widths (rescaled units) */
+  double box[3];         /* rescaled box */
+  unsigned long long *gcnt;    /* ntot counts */
+  unsigned long long *gwt;     /* 2 * ntot: lo, hi words of int128 */
+} fcfcg_mock;
+
 typedef struct {
   int geometry, bintype, isauto, withwt;
   int ncell[3];
@@ -133,6 +144,10 @@ typedef struct {
   unsigned long long *stats;   /* [0] candidates [1] in-range [2] recheck
                                   [3] inline rechecks */
   int hist_smem;               /* histogram in shared memory */
+  /* batch of catalogues (NULL: one catalogue pair): chunk .w is the
+   * catalogue, queue entries carry it too */
+  const fcfcg_mock *mocks;
+  int nmock;
 } fcfcg_launch;
 
 /* Launchers implemented in the .cu files; return 0 or a CUDA error code. */
@@ -148,7 +163,22 @@ int fcfcg_k_grid(void *stream, size_t n, const double *x, const double *y,
     double *sz, double *ss, double *sw, uint32_t *sid);
 int fcfcg_k_chunks(void *stream, const uint32_t *cstart, uint32_t ncell,
     uint32_t clen, uint32_t *cchunk, uint32_t *scan_tmp, size_t scan_tmp_len,
-    uint32_t *chunks, uint32_t *nchunk_out);
+    uint32_t *chunks, uint32_t *nchunk_out, const uint32_t *mock_cell_base,
+    int nmock);
+/* Batch grid: cells of one catalogue numbered from cell_base into a shared
+ * cell-count array (k_cell), and its points scattered into the shared
+ * sorted arrays after the global scan (k_scatter); sid = id_base + i. */
+int fcfcg_k_cell_batch(void *stream, size_t n, const double *x,
+    const double *y, const double *z, const int ncell[3], const double cw[3],
+    uint32_t cell_base, uint32_t *cell_of, uint32_t *count);
+int fcfcg_k_scatter_batch(void *stream, size_t n, const double *x,
+    const double *y, const double *z, const double *w, int has_w, int wexp,
+    const int ncell[3], const double cw[3], uint32_t cell_base,
+    uint32_t id_base, const uint32_t *cell_of, const uint32_t *cstart,
+    uint32_t *cfill, float *l4, int *wq, double *sx, double *sy, double *sz,
+    double *sw, uint32_t *sid);
+int fcfcg_scan(void *stream, const uint32_t *in, size_t n, uint32_t *out,
+    uint32_t *tmp);
 size_t fcfcg_k_count32_stage(int nsten, int withwt);
 size_t fcfcg_k_count32_tab_bytes(int nfs, int nfp, int nsb, int npb);
 int fcfcg_k_bbox(void *stream, size_t n, const double *x, const double *y,

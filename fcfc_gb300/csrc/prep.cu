@@ -222,14 +222,14 @@ __device__ __forceinline__ int cell_axis(double v, double lo, double cw,
 __global__ void k_cell(size_t n, const double *__restrict__ x,
     const double *__restrict__ y, const double *__restrict__ z, int nx,
     int ny, int nz, double cwx, double cwy, double cwz, double lox,
-    double loy, double loz, uint32_t *__restrict__ cell_of,
+    double loy, double loz, uint32_t cell_base, uint32_t *__restrict__ cell_of,
     uint32_t *__restrict__ count) {
   for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n;
        i += (size_t) gridDim.x * blockDim.x) {
     int cx = cell_axis(x[i], lox, cwx, nx);
     int cy = cell_axis(y[i], loy, cwy, ny);
     int cz = cell_axis(z[i], loz, cwz, nz);
-    uint32_t c = ((uint32_t) cz * ny + cy) * nx + cx;
+    uint32_t c = cell_base + ((uint32_t) cz * ny + cy) * nx + cx;
     cell_of[i] = c;
     atomicAdd(count + c, 1u);
   }
@@ -239,7 +239,8 @@ __global__ void k_scatter(size_t n, const double *__restrict__ x,
     const double *__restrict__ y, const double *__restrict__ z,
     const double *__restrict__ s, const double *__restrict__ w, int has_w,
     int wexp, int nx, int ny, double cwx, double cwy, double cwz, double lox,
-    double loy, double loz, const uint32_t *__restrict__ cell_of,
+    double loy, double loz, uint32_t cell_base, uint32_t id_base,
+    const uint32_t *__restrict__ cell_of,
     const uint32_t *__restrict__ cstart, uint32_t *__restrict__ cfill,
     float4 *__restrict__ l4, int2 *__restrict__ wq, double *__restrict__ sx,
     double *__restrict__ sy, double *__restrict__ sz, double *__restrict__ ss,
@@ -248,9 +249,10 @@ __global__ void k_scatter(size_t n, const double *__restrict__ x,
        i += (size_t) gridDim.x * blockDim.x) {
     uint32_t c = cell_of[i];
     uint32_t pos = cstart[c] + atomicAdd(cfill + c, 1u);
-    int cx = (int) (c % (uint32_t) nx);
-    int cy = (int) ((c / (uint32_t) nx) % (uint32_t) ny);
-    int cz = (int) (c / ((uint32_t) nx * (uint32_t) ny));
+    const uint32_t cl = c - cell_base;
+    int cx = (int) (cl % (uint32_t) nx);
+    int cy = (int) ((cl / (uint32_t) nx) % (uint32_t) ny);
+    int cz = (int) (cl / ((uint32_t) nx * (uint32_t) ny));
     double a = x[i], b = y[i], d = z[i];
     double ccx = lox + (cx + 0.5) * cwx;
     double ccy = loy + (cy + 0.5) * cwy;
@@ -271,7 +273,7 @@ __global__ void k_scatter(size_t n, const double *__restrict__ x,
     sz[pos] = d;
     if (ss) ss[pos] = s[i];
     sw[pos] = wv;
-    sid[pos] = (uint32_t) i;
+    sid[pos] = id_base + (uint32_t) i;
   }
 }
 
@@ -290,7 +292,7 @@ extern "C" int fcfcg_k_grid(void *stream, size_t n, const double *x,
   if (n) {
     k_cell<<<grid_for(n, PREP_THREADS), PREP_THREADS, 0, st>>>(
         n, x, y, z, ncell[0], ncell[1], ncell[2], cw[0], cw[1], cw[2], lo[0],
-        lo[1], lo[2], cell_of, cfill);
+        lo[1], lo[2], 0u, cell_of, cfill);
     if ((e = cudaGetLastError())) return (int) e;
   }
   int r = scan_u32(st, cfill, nc, cstart, scan_tmp);
@@ -299,11 +301,42 @@ extern "C" int fcfcg_k_grid(void *stream, size_t n, const double *x,
   if (n) {
     k_scatter<<<grid_for(n, PREP_THREADS), PREP_THREADS, 0, st>>>(
         n, x, y, z, s, w, has_w, wexp, ncell[0], ncell[1], cw[0], cw[1],
-        cw[2], lo[0], lo[1], lo[2], cell_of, cstart, cfill, (float4 *) l4,
-        (int2 *) wq, sx, sy, sz, ss, sw, sid);
+        cw[2], lo[0], lo[1], lo[2], 0u, 0u, cell_of, cstart, cfill,
+        (float4 *) l4, (int2 *) wq, sx, sy, sz, ss, sw, sid);
     if ((e = cudaGetLastError())) return (int) e;
   }
   return 0;
+}
+
+extern "C" int fcfcg_scan(void *stream, const uint32_t *in, size_t n,
+    uint32_t *out, uint32_t *tmp) {
+  return scan_u32((cudaStream_t) stream, in, n, out, tmp);
+}
+
+extern "C" int fcfcg_k_cell_batch(void *stream, size_t n, const double *x,
+    const double *y, const double *z, const int ncell[3], const double cw[3],
+    uint32_t cell_base, uint32_t *cell_of, uint32_t *count) {
+  if (!n) return 0;
+  k_cell<<<grid_for(n, PREP_THREADS), PREP_THREADS, 0,
+           (cudaStream_t) stream>>>(n, x, y, z, ncell[0], ncell[1], ncell[2],
+                                    cw[0], cw[1], cw[2], 0.0, 0.0, 0.0,
+                                    cell_base, cell_of, count);
+  return (int) cudaGetLastError();
+}
+
+extern "C" int fcfcg_k_scatter_batch(void *stream, size_t n, const double *x,
+    const double *y, const double *z, const double *w, int has_w, int wexp,
+    const int ncell[3], const double cw[3], uint32_t cell_base,
+    uint32_t id_base, const uint32_t *cell_of, const uint32_t *cstart,
+    uint32_t *cfill, float *l4, int *wq, double *sx, double *sy, double *sz,
+    double *sw, uint32_t *sid) {
+  if (!n) return 0;
+  k_scatter<<<grid_for(n, PREP_THREADS), PREP_THREADS, 0,
+              (cudaStream_t) stream>>>(
+      n, x, y, z, NULL, w, has_w, wexp, ncell[0], ncell[1], cw[0], cw[1],
+      cw[2], 0.0, 0.0, 0.0, cell_base, id_base, cell_of, cstart, cfill,
+      (float4 *) l4, (int2 *) wq, sx, sy, sz, NULL, sw, sid);
+  return (int) cudaGetLastError();
 }
 
 /* Work chunks: every cell is cut into pieces of at most clen points, as
@@ -317,25 +350,39 @@ __global__ void k_chunk_count(const uint32_t *__restrict__ cstart,
   }
 }
 
+/* mbase (nmock + 1 entries, may be NULL): first cell of each catalogue of a
+ * batch; the chunk's .w is the catalogue holding its cell. */
 __global__ void k_chunk_emit(const uint32_t *__restrict__ cstart,
     uint32_t ncell, uint32_t clen, const uint32_t *__restrict__ coff,
-    uint4 *__restrict__ chunks) {
+    uint4 *__restrict__ chunks, const uint32_t *__restrict__ mbase,
+    int nmock) {
   for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
        c += gridDim.x * blockDim.x) {
     uint32_t a = cstart[c], m = cstart[c + 1] - a;
     uint32_t k = coff[c];
     uint32_t nch = (m + clen - 1) / clen;
+    uint32_t mk = 0;
+    if (mbase) {
+      int lo = 0, hi = nmock;   /* last lo with mbase[lo] <= c */
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (mbase[mid] <= c) lo = mid;
+        else hi = mid;
+      }
+      mk = (uint32_t) lo;
+    }
     for (uint32_t q = 0; q < nch; q++) {
       uint32_t b0 = (uint32_t) (((unsigned long long) m * q) / nch);
       uint32_t b1 = (uint32_t) (((unsigned long long) m * (q + 1)) / nch);
-      chunks[k++] = make_uint4(c, a + b0, b1 - b0, 0);
+      chunks[k++] = make_uint4(c, a + b0, b1 - b0, mk);
     }
   }
 }
 
 extern "C" int fcfcg_k_chunks(void *stream, const uint32_t *cstart,
     uint32_t ncell, uint32_t clen, uint32_t *cchunk, uint32_t *scan_tmp,
-    size_t scan_tmp_len, uint32_t *chunks, uint32_t *nchunk_out) {
+    size_t scan_tmp_len, uint32_t *chunks, uint32_t *nchunk_out,
+    const uint32_t *mock_cell_base, int nmock) {
   cudaStream_t st = (cudaStream_t) stream;
   (void) scan_tmp_len;
   k_chunk_count<<<grid_for(ncell, PREP_THREADS), PREP_THREADS, 0, st>>>(
@@ -348,7 +395,7 @@ extern "C" int fcfcg_k_chunks(void *stream, const uint32_t *cstart,
   if (r) return r;
   if (chunks) {
     k_chunk_emit<<<grid_for(ncell, PREP_THREADS), PREP_THREADS, 0, st>>>(
-        cstart, ncell, clen, coff, (uint4 *) chunks);
+        cstart, ncell, clen, coff, (uint4 *) chunks, mock_cell_base, nmock);
     if ((e = cudaGetLastError())) return (int) e;
   }
   if (nchunk_out)

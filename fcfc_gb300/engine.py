@@ -190,6 +190,69 @@ class PairCounter:
                                              None))
         return res
 
+    # -- batches of periodic boxes -----------------------------------------
+    def _jobs(self, cats, boxes, weights, weighted, on_device):
+        n = len(cats)
+        jobs = (capi.Job * max(n, 1))()
+        keep = []
+        outs = []
+        for j in range(n):
+            J = jobs[j]
+            b = np.broadcast_to(np.asarray(boxes[j], np.float64), (3,))
+            for k in range(3):
+                J.box[k] = float(b[k])
+            if on_device:
+                x, y, z = cats[j][:3]
+                J.n = int(cats[j][3])
+                J.x, J.y, J.z = (C.cast(C.c_void_p(p), capi._dp) for p in (x, y, z))
+                if weighted:
+                    J.w = C.cast(C.c_void_p(weights[j]), capi._dp)
+            else:
+                a = np.asarray(cats[j], np.float64)
+                cols = [np.ascontiguousarray(a[:, k]) for k in range(3)]
+                keep += cols
+                J.n = len(a)
+                J.x, J.y, J.z = (c.ctypes.data_as(capi._dp) for c in cols)
+                if weighted:
+                    w = np.ascontiguousarray(weights[j], np.float64)
+                    keep.append(w)
+                    J.w = w.ctypes.data_as(capi._dp)
+            if weighted:
+                o = np.zeros(self.ntot)
+                J.wcnt = o.ctypes.data_as(capi._dp)
+            else:
+                o = np.zeros(self.ntot, np.int64)
+                J.icnt = o.ctypes.data_as(C.POINTER(C.c_int64))
+            outs.append(o)
+        return jobs, keep, outs
+
+    def count_batch(self, cats, boxes, weights=None, weighted=False,
+                    precision=PREC_FP32_RECHECK, on_device=False):
+        """DD counts (undoubled) of many periodic boxes in one launch.
+
+        cats: N_j x 3 host arrays, or with on_device (x_ptr, y_ptr, z_ptr, n)
+        tuples of device FP64 pointers; boxes: BOX_SIZE per catalogue;
+        weights: per-catalogue arrays (device pointers with on_device).
+        Returns (counts, status, sumw) lists."""
+        jobs, keep, outs = self._jobs(cats, boxes, weights, weighted, on_device)
+        self._check(self.lib.fcfcg_count_batch(self.h, jobs, len(cats),
+                                               int(bool(weighted)),
+                                               int(precision), int(bool(on_device))))
+        del keep
+        return (outs, [jobs[j].status for j in range(len(cats))],
+                [jobs[j].sumw for j in range(len(cats))])
+
+    def autotune_batch(self, cats, boxes, weights=None, weighted=False,
+                       on_device=False):
+        jobs, keep, outs = self._jobs(cats, boxes, weights, weighted, on_device)
+        k = C.c_int()
+        ms = C.c_double()
+        self._check(self.lib.fcfcg_autotune_batch(
+            self.h, jobs, len(cats), int(bool(weighted)), int(bool(on_device)),
+            C.byref(k), C.byref(ms)))
+        del keep, outs
+        return k.value, ms.value
+
     def stats(self) -> dict:
         s = capi.Stats()
         self._check(self.lib.fcfcg_stats_get(self.h, C.byref(s)))

@@ -163,6 +163,50 @@ int fcfcg_load_catalog_device(fcfcg_ctx *ctx, int slot, size_t n,
     const double *x, const double *y, const double *z, const double *w);
 
 /*
+ * One catalogue of a batch (fcfcg_count_batch): a periodic box with its own
+ * size, counted for DD with the context's bins.  No reference counterpart as
+ * one call: FCFC counts one catalogue per run, so a batch replaces a loop of
+ * FCFC_2PT_BOX runs (src/fcfc/2pt_box/fcfc.c:19-82) over mock boxes.
+ *   n, x, y, z, w   coordinates as read (FP64) and optional weights; host or
+ *                   device pointers (the on_device argument).
+ *   box             BOX_SIZE of this catalogue.
+ *   icnt / wcnt     host outputs, ntot each: undoubled auto counts (icnt,
+ *                   unweighted) or weighted sums (wcnt), as fcfcg_count.
+ *   sumw            out: the sum of weights (n when unweighted).
+ *   status          out: FCFCG_OK, or this catalogue's error
+ *                   (FCFCG_ERR_CFG: s_max or pi_max not below half the box,
+ *                   as FCFC's conf_verify rejects it; FCFCG_ERR_DATA:
+ *                   points outside the box or non-finite values).
+ */
+typedef struct {
+  size_t n;
+  const double *x, *y, *z, *w;
+  double box[3];
+  int64_t *icnt;
+  double *wcnt;
+  double sumw;
+  int status;
+} fcfcg_job;
+
+/*
+ * Count DD pairs of many periodic-box catalogues (mocks) with one set of bins
+ * in a single persistent FP32 launch: all catalogues are cell-sorted into one
+ * array with per-catalogue grids, and the CTAs draw (catalogue, cell chunk)
+ * items from one device work counter; ambiguous pairs of every catalogue go
+ * through one FP64 recheck.  Box contexts only.  precision FCFCG_PREC_FP64
+ * counts the catalogues one after the other with the all-FP64 kernel (the
+ * comparison path).  Returns FCFCG_OK when the batch ran (per-catalogue
+ * errors are in jobs[i].status), or an error of the whole call.
+ */
+int fcfcg_count_batch(fcfcg_ctx *ctx, fcfcg_job *jobs, int njobs,
+    int withwt, int precision, int on_device);
+
+/* Time fcfcg_count_batch at 1..5 cells per maximum separation and keep the
+ * fastest for batches of this mean density (as fcfcg_autotune). */
+int fcfcg_autotune_batch(fcfcg_ctx *ctx, fcfcg_job *jobs, int njobs,
+    int withwt, int on_device, int *best_k, double *best_ms);
+
+/*
  * Fiducial cosmology of FCFC_2PT's coordinate conversion (COORD_CONVERT = T):
  * the keys OMEGA_M, OMEGA_LAMBDA, DE_EOS_W, CMVDST_ERR and Z_CMVDST_FILE
  * (src/fcfc/2pt/load_conf.c:532-536), checked as check_cosmo and conf_verify
