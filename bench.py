@@ -205,6 +205,150 @@ def run_reference(args, rank, world):
     return 0
 
 
+def mocks_workload(nmock=256, seed=7, density=2.5e-4, nmin=1e4, nmax=1e6):
+    """Neyman-Scott boxes (the generator of the clustered-box workload:
+    Poisson(100) children, sigma = 5 Mpc/h), N log-uniform in [nmin, nmax],
+    box side (N / density)^(1/3)."""
+    from fcfc_gb300 import synth
+    rng = np.random.default_rng(seed)
+    cats, boxes = [], []
+    for j in range(nmock):
+        n = float(np.exp(rng.uniform(np.log(nmin), np.log(nmax))))
+        L = (n / density) ** (1.0 / 3.0)
+        cats.append(synth.neyman_scott(max(1, int(round(n / 100))), L, 100.0,
+                                       5.0, seed=seed * 100003 + j))
+        boxes.append(L)
+    return cats, boxes
+
+
+def run_mocks(args, rank, world, local, dist):
+    """256 mock boxes, unweighted DD (s, mu) 40 x 100, one persistent launch
+    per step (fcfcg_count_batch)."""
+    import torch
+    import fcfc_gb300 as fg
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    nmock = 32 if args.small else 256
+    cats, boxes = mocks_workload(nmock=nmock, seed=7 + rank)
+    ntot_pts = sum(len(c) for c in cats)
+    tens = []
+    dcats = []
+    for x in cats:
+        cols = [torch.from_numpy(np.ascontiguousarray(x[:, k])).to(dev)
+                for k in range(3)]
+        tens += cols
+        dcats.append((cols[0].data_ptr(), cols[1].data_ptr(),
+                      cols[2].data_ptr(), len(x)))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    pc = fg.PairCounter("box", fg.BIN_SMU, box=max(boxes), smin=0, smax=200,
+                        ds=5, nmu=100, device=local)
+
+    def step(on_device=True, cat=None):
+        return pc.count_batch(cat if cat is not None else dcats, boxes,
+                              on_device=on_device)
+
+    counts, status, _ = step()
+    accepted = [j for j in range(nmock) if status[j] == 0]
+    pairs = int(sum(int(counts[j].sum()) for j in accepted))
+    # fixed s_max / 3 cells against the autotuned refinement
+    pc.set_cells_per_smax(3)
+    step()
+    t0 = time.perf_counter()
+    step()
+    ms_fixed3 = (time.perf_counter() - t0) * 1e3
+    pc.set_cells_per_smax(0)
+    k_tuned, _ = pc.autotune_batch(dcats, boxes, on_device=True)
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    launches0 = pc.stats()["launches"]
+    tt, tk = 0.0, 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step()
+        tt += time.perf_counter() - t0
+        tk += pc.stats()["ms_count"]
+    clocks = clk.stop()
+    st = pc.stats()
+    launches = pc.stats()["launches"] - launches0
+    ms_step = max_over_ranks(tt / args.steps * 1e3, dist)
+    value = pairs * world / (ms_step * 1e-3)
+    k_ms = tk / args.steps
+    # all-FP64 path on every 8th accepted catalogue (the same catalogues)
+    sub = accepted[::8]
+    sub_cats = [dcats[j] for j in sub]
+    sub_boxes = [boxes[j] for j in sub]
+    c64, _, _ = pc.count_batch(sub_cats, sub_boxes, on_device=True,
+                               precision=fg.PREC_FP64)
+    t0 = time.perf_counter()
+    c64, _, _ = pc.count_batch(sub_cats, sub_boxes, on_device=True,
+                               precision=fg.PREC_FP64)
+    ms64 = (time.perf_counter() - t0) * 1e3
+    pairs64 = int(sum(int(c.sum()) for c in c64))
+    t0 = time.perf_counter()
+    c32, _, _ = pc.count_batch(sub_cats, sub_boxes, on_device=True)
+    ms32_sub = (time.perf_counter() - t0) * 1e3
+    exact = all(np.array_equal(a, b) for a, b in zip(c64, c32))
+    # end to end from host arrays
+    step(on_device=False, cat=cats)
+    te = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step(on_device=False, cat=cats)
+        te += time.perf_counter() - t0
+    e2e_ms = te / args.steps * 1e3
+    peak = fp32_peak_tflops(dev)
+    achieved = pairs * FLOPS_PER_PAIR["smu"] / (k_ms * 1e-3) / 1e12
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64-recheck", "data": "synthetic",
+        "config": {"workload": "mocks%d" % nmock, "n_catalogues": nmock,
+                   "n_points": ntot_pts, "accepted": len(accepted),
+                   "rejected_smax_ge_half_box": nmock - len(accepted),
+                   "bins": "(s,mu) 40x100 s<200", "weighted": False,
+                   "pairs_per_step": pairs,
+                   "density": 2.5e-4, "n_range": [1e4, 1e6],
+                   "l2": "flushed between steps (256 MiB write)",
+                   "cells_per_smax_autotuned": k_tuned,
+                   "ms_per_step_fixed_smax_over_3": ms_fixed3,
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "fp64": {"value": pairs64 / (ms64 * 1e-3), "unit": UNIT,
+                 "catalogues": len(sub), "pairs": pairs64, "ms": ms64,
+                 "fp32_recheck_ms_same_catalogues": ms32_sub,
+                 "speedup_fp32_recheck_over_fp64": ms64 / ms32_sub,
+                 "counts_identical": exact},
+        "e2e": {"value": pairs / (e2e_ms * 1e-3), "unit": UNIT,
+                "ms_per_step": e2e_ms, "h2d_bytes_per_step": ntot_pts * 24,
+                "d2h_bytes_per_step": len(accepted) * pc.ntot * 8},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak,
+                     "traffic": None, "kernel": "k_count32<box,smu,unweighted,batch>",
+                     "kernel_ms": k_ms,
+                     "peak_source": "measured cuBLAS SGEMM (TF32 off) on this GPU",
+                     "flops_per_pair": FLOPS_PER_PAIR["smu"]},
+        "counters": {"candidates": st["candidates"], "rechecked": st["rechecked"],
+                     "nchunks": st["nchunks"], "ms_grid": st["ms_grid"],
+                     "ms_recheck": st["ms_recheck"]},
+        "clocks": clocks,
+        "gpu_launches": int(launches),
+    }
+    if dist:
+        dist.barrier()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    return 0
+
+
 def cpu_baseline_sample(x, w, box):
     """The CPU restatement of FCFC's counter (oracle/, OpenMP on every host
     core) on the whole workload, one weighted step: 10-30 s of CPU work."""
@@ -232,6 +376,9 @@ def main():
     ap.add_argument("--small", action="store_true",
                     help="quarter-size box (for profiler captures)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="ns_box_2e6",
+                    choices=["ns_box_2e6", "mocks256"],
+                    help="mocks256: 256 mock boxes in one persistent launch")
     args = ap.parse_args()
     rank, world, local = env_rank()
     dist = None
@@ -244,6 +391,8 @@ def main():
             dist.barrier()
         return rc
 
+    if args.workload == "mocks256":
+        return run_mocks(args, rank, world, local, dist)
     import torch
     import fcfc_gb300 as fg
     torch.cuda.set_device(local)
