@@ -116,6 +116,7 @@ PROTOTYPES = {
     "fcfcg_bins_tables": (C.c_int, [P, P, P, P, P]),
     "fcfcg_load_catalog": (C.c_int, [P, C.c_int, C.c_size_t, P, P, P, P]),
     "fcfcg_load_catalog_device": (C.c_int, [P, C.c_int, C.c_size_t, P, P, P, P]),
+    "fcfcg_adjoint": (C.c_int, [P, C.c_int, C.c_int, C.c_int, P, P, P]),
     "fcfcg_count_batch": (C.c_int, [P, C.POINTER(Job), C.c_int, C.c_int,
                                     C.c_int, C.c_int]),
     "fcfcg_autotune_batch": (C.c_int, [P, C.POINTER(Job), C.c_int, C.c_int,

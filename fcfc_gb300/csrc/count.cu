@@ -45,21 +45,21 @@ __device__ __forceinline__ void add128(unsigned long long *lohi, long long v) {
 }
 
 /*
- * Fixed-point product of two weights scaled to |w| <= 1, with F = 42
- * fractional bits.  A weight is held as an integer part wi = round(w 2^30)
- * and a float remainder wr = w - wi 2^-30:
- *   w_a w_b 2^42 = wi_a wi_b 2^-18 + (w_a wr_b + wr_a w_b) 2^42 (+ wr wr).
- * The first term is an exact 64-bit product rounded by a shift, the cross
- * term (|.| <= 2^13) is rounded with the 1.5 * 2^23 float trick.  No 64-bit
- * float conversions.  Every path uses this function, so a pair always adds
- * the same integer.
+ * Fixed-point product of two weights scaled to |w| <= 1, with F = 51
+ * fractional bits (FCFCG_FIX_F).  A weight is held as an integer part
+ * wi = round(w 2^30) and a float remainder wr = w - wi 2^-30 (|wr| <= 2^-31):
+ *   w_a w_b 2^51 = wi_a wi_b 2^-9 + (w_a wr_b + wr_a w_b) 2^51 (+ wr wr).
+ * The first term is an exact 64-bit product rounded by a shift; the cross
+ * term (|.| <= 2^21) is rounded with the 1.5 * 2^23 float trick; wr wr
+ * (<= 2^-11 of a unit) is dropped.  No 64-bit float conversions.  Every
+ * path uses this function, so a pair always adds the same integer.
  */
 __device__ __forceinline__ long long fix_prod(int ia, float ra, float fa,
     int ib, float rb, float fb) {
   const long long p = (long long) ia * (long long) ib;
-  const long long main = (p + (1ll << 17)) >> 18;
+  const long long main = (p + (1ll << 8)) >> 9;
   const float c = __fmaf_rn(fa, rb, __fmul_rn(ra, fb));
-  const float t = __fmaf_rn(c, 4398046511104.0f /* 2^42 */, 12582912.0f);
+  const float t = __fmaf_rn(c, 2251799813685248.0f /* 2^51 */, 12582912.0f);
   return main + (long long) (__float_as_int(t) - 0x4B400000);
 }
 
@@ -410,6 +410,28 @@ __device__ __forceinline__ void enqueue(const fcfcg_launch &L,
   hist_add<WT, BATCH>(L, ms, h, bin, WT ? fix_prod_pair(L, a, b) : 0);
 }
 
+/* Adjoint: FP64 gradient contributions of one pair with a known bin. */
+__device__ __forceinline__ void adj_pair(const fcfcg_launch &L, uint32_t a,
+    uint32_t b, int bin) {
+  const double g = __ldg(L.gadj + bin);
+  atomicAdd(L.dA + a, __dmul_rn(L.B.w[b], g));
+  atomicAdd(L.dB + b, __dmul_rn(L.A.w[a], g));
+}
+
+/* Adjoint: queue an ambiguous pair for the FP64 recheck, or bin it here
+ * when the queue is full. */
+__device__ __forceinline__ void enqueue_adj(const fcfcg_launch &L,
+    uint32_t a, uint32_t b, uint32_t code, unsigned long long &n_inline) {
+  uint32_t slot = atomicAdd(L.qcount, 1u);
+  if (slot < L.qcap) {
+    *((uint4 *) L.queue + slot) = make_uint4(a, b, code, 0u);
+    return;
+  }
+  n_inline++;
+  int bin = ref_bin_pair(L, a, b, code, L.box);
+  if (bin >= 0) adj_pair(L, a, b, bin);
+}
+
 /* Add a CTA's shared histogram to a global one and clear it. */
 template <int WT>
 __device__ __forceinline__ void hist_flush(const fcfcg_launch &L,
@@ -446,17 +468,23 @@ struct Stage {
   float4 *bw;       /* per warp, 32: weight, integer weight, remainder */
   uint16_t *bt;     /* per warp, 32: stencil entry */
   uint16_t *q;      /* per warp, QCAP: queued pairs */
+  /* adjoint only */
+  double *ga, *wa;  /* FCHUNK: gradient accumulators, FP64 weights */
+  double *gb, *wb;  /* per warp, 32: the same for the neighbour points */
 };
 
+/* wt: 0 unweighted, 1 weighted, 2 adjoint (weighted + FP64 gradients) */
 __host__ __device__ __forceinline__ size_t stage_cta_bytes(int nsten, int wt) {
   size_t n = (size_t) FCHUNK * 16 + (wt ? (size_t) FCHUNK * 8 : 0);
   n += (((size_t) nsten + 1) * 4 + 15) & ~(size_t) 15;
   n += (((size_t) nsten) * 4 + 15) & ~(size_t) 15;
+  if (wt == 2) n += (size_t) FCHUNK * 16;
   return n;
 }
 
 __host__ __device__ __forceinline__ size_t stage_warp_bytes(int wt) {
-  return 32 * 16 + (wt ? 32 * 16 : 0) + 32 * 2 + QCAP * 2;
+  return 32 * 16 + (wt ? 32 * 16 : 0) + 32 * 2 + QCAP * 2 +
+         (wt == 2 ? 32 * 16 : 0);
 }
 
 __host__ __device__ __forceinline__ size_t stage_bytes(int nsten, int wt) {
@@ -483,7 +511,7 @@ __device__ __forceinline__ uint32_t nb_code(const int *ncell, int cx,
  * Bin one queued pair per lane.  FP32 windows decide; ambiguous pairs go to
  * the FP64 recheck queue.  c2 = twice the chunk cell's centre (survey).
  */
-template <int GEOM, int BIN, int WT, int BATCH>
+template <int GEOM, int BIN, int WT, int BATCH, int ADJ>
 __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
     const MockSh *ms, const Stage &S, uint32_t ent, uint32_t first, int cx,
     int cy, int cz,
@@ -568,10 +596,18 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
     if (GEOM == FCFCG_GEOM_BOX)
       code = nb_code(BATCH ? ms->nc : L.ncell, cx, cy, cz,
                      __ldg((const int4 *) L.sten + S.bt[src]));
-    enqueue<WT, BATCH>(L, ms, ai, bj, code, h, n_inline);
+    if (ADJ) enqueue_adj(L, ai, bj, code, n_inline);
+    else enqueue<WT, BATCH>(L, ms, ai, bj, code, h, n_inline);
     return;
   }
   n_in++;
+  if (ADJ) {
+    /* d/dw_a of w_a w_b g[bin] is w_b g[bin], and the other way round */
+    const double g = L.hist_smem ? ((const double *) h)[bin] : __ldg(L.gadj + bin);
+    atomicAdd(S.ga + i, __dmul_rn(S.wb[src], g));
+    atomicAdd(S.gb + src, __dmul_rn(S.wa[i], g));
+    return;
+  }
   long long w = 0;
   if (WT) {
     const int2 wa = S.aw[i];
@@ -631,7 +667,7 @@ __device__ __forceinline__ uint32_t scan_chunk(const fcfcg_launch &L,
  * in-range pairs are then compacted into the warp queue and binned 32 at a
  * time, every lane busy.
  */
-template <int GEOM, int BIN, int WT, int BATCH>
+template <int GEOM, int BIN, int WT, int BATCH, int ADJ>
 __global__ void __launch_bounds__(CT32_THREADS, 4)
 k_count32(const fcfcg_launch L) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -659,7 +695,13 @@ k_count32(const fcfcg_launch L) {
     b += (((size_t) L.nsten + 1) * 4 + 15) & ~(size_t) 15;
     S.bst = (uint32_t *) b;
     b += (((size_t) L.nsten) * 4 + 15) & ~(size_t) 15;
-    b += (size_t) warp * stage_warp_bytes(WT);
+    if (ADJ) {
+      S.ga = (double *) b;
+      b += (size_t) FCHUNK * 8;
+      S.wa = (double *) b;
+      b += (size_t) FCHUNK * 8;
+    }
+    b += (size_t) warp * stage_warp_bytes(WT + ADJ);
     S.b = (float4 *) b;
     b += 32 * 16;
     S.bw = (float4 *) b;
@@ -667,14 +709,28 @@ k_count32(const fcfcg_launch L) {
     S.bt = (uint16_t *) b;
     b += 32 * 2;
     S.q = (uint16_t *) b;
+    if (ADJ) {
+      b += QCAP * 2;
+      S.gb = (double *) b;
+      b += 32 * 8;
+      S.wb = (double *) b;
+    }
   }
   for (int i = threadIdx.x; i < L.nfs; i += blockDim.x) fs[i] = L.fs[i];
   for (int i = threadIdx.x; i < L.nfp; i += blockDim.x) fp[i] = L.fp[i];
   for (int i = threadIdx.x; i <= L.nsb; i += blockDim.x) fse[i] = L.fse[i];
   if (L.npb)
     for (int i = threadIdx.x; i <= L.npb; i += blockDim.x) fpe[i] = L.fpe[i];
-  if (L.hist_smem)
+  if (ADJ) {
+    /* the cotangent of the counts takes the histogram's place */
+    if (L.hist_smem)
+      for (long i = threadIdx.x; i < L.ntot; i += blockDim.x)
+        ((double *) h)[i] = L.gadj[i];
+    for (int i = threadIdx.x; i < FCHUNK; i += blockDim.x) S.ga[i] = 0;
+    if (lane < 32) S.gb[lane] = 0;
+  } else if (L.hist_smem) {
     for (long i = threadIdx.x; i < L.ntot * (WT ? 2 : 1); i += blockDim.x) h[i] = 0;
+  }
 
   const float4 *__restrict__ Bl4 = (const float4 *) L.B.l4;
   const int2 *__restrict__ Bwq = (const int2 *) L.B.wq;
@@ -735,6 +791,7 @@ k_count32(const fcfcg_launch L) {
       for (int k = lane; k < m; k += 32) {
         S.a[k] = ((const float4 *) L.A.l4)[first + k];
         if (WT) S.aw[k] = ((const int2 *) L.A.wq)[first + k];
+        if (ADJ) S.wa[k] = L.A.w[first + k];
       }
     } else if (warp == 0) {
       /* neighbour cells of this chunk, laid end to end */
@@ -785,6 +842,7 @@ k_count32(const fcfcg_launch L) {
       const uint32_t p = base + (uint32_t) lane;
       float bx = 0.f, by = 0.f, bz = 0.f;
       int ilim = 0;
+      uint32_t bjl = 0;
       if (p < total) {
         /* neighbour cell of position p: last t with pre[t] <= p */
         int lo = 0, hi = L.nsten;
@@ -816,6 +874,8 @@ k_count32(const fcfcg_launch L) {
         if (L.isauto && t == L.tzero) ilim = min(m, (int) jc - aoff);
         S.b[lane] = make_float4(bx, by, bz, __uint_as_float(bj));
         S.bt[lane] = (uint16_t) t;
+        bjl = bj;
+        if (ADJ) S.wb[lane] = L.B.w[bj];
         if (WT) {
           const int2 wq = Bwq[bj];
           S.bw[lane] = make_float4(pb.w, __int_as_float(wq.x),
@@ -867,11 +927,30 @@ k_count32(const fcfcg_launch L) {
         for (uint32_t k = 0; k < np; k++) {
           const uint32_t e = (uint32_t) lane * np + k;
           if (e < nr)
-            bin_pair<GEOM, BIN, WT, BATCH>(L, &sh_mock, S, S.q[e], first, cx,
-                                           cy, cz, c2x, c2y, c2z, fs, fp,
-                                           fse, fpe, h, n_in, n_q, n_inline);
+            bin_pair<GEOM, BIN, WT, BATCH, ADJ>(L, &sh_mock, S, S.q[e], first,
+                                                cx, cy, cz, c2x, c2y, c2z, fs,
+                                                fp, fse, fpe, h, n_in, n_q,
+                                                n_inline);
         }
         __syncwarp();
+      }
+      if (ADJ) {
+        /* the block's neighbour points are done: their gradients out */
+        if (p < total) {
+          const double v = S.gb[lane];
+          if (v != 0.0) atomicAdd(L.dB + bjl, v);
+          S.gb[lane] = 0;
+        }
+        __syncwarp();
+      }
+    }
+    if (ADJ) {
+      /* the chunk is done: its points' gradients out */
+      __syncthreads();
+      for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        const double v = S.ga[k];
+        if (v != 0.0) atomicAdd(L.dA + first + k, v);
+        S.ga[k] = 0;
       }
     }
     n_in64 += n_in;
@@ -891,7 +970,7 @@ k_count32(const fcfcg_launch L) {
     atomicAdd(L.stats + 3, n_inline);
   }
   __syncthreads();
-  if (L.hist_smem && (!BATCH || cur >= 0))
+  if (!ADJ && L.hist_smem && (!BATCH || cur >= 0))
     hist_flush<WT>(L, h, BATCH ? sh_mock.g : (WT ? L.gwt : L.gcnt));
 }
 
@@ -900,13 +979,13 @@ k_count32(const fcfcg_launch L) {
  * reference's FP64 formula.  Weighted sums are FP64 products accumulated
  * in FP64.
  */
-template <int GEOM, int WT>
+template <int GEOM, int WT, int ADJ>
 __global__ void __launch_bounds__(CT_THREADS)
 k_count64(const fcfcg_launch L) {
   extern __shared__ __align__(16) unsigned char smem[];
   uint32_t *h32 = (uint32_t *) smem;
   double *hd = (double *) smem;
-  if (L.hist_smem) {
+  if (!ADJ && L.hist_smem) {
     if (WT)
       for (long i = threadIdx.x; i < L.ntot; i += blockDim.x) hd[i] = 0;
     else
@@ -916,6 +995,7 @@ k_count64(const fcfcg_launch L) {
   unsigned long long n_cand = 0, n_in = 0;
   WarpChunk w;
   while (next_chunk(L, w)) {
+    double ga = 0;      /* adjoint: this lane's share of dL/dw of its point */
     for (int t = 0; t < L.nsten; t++) {
       const int4 o = __ldg((const int4 *) L.sten + t);
       uint32_t cb, code;
@@ -931,7 +1011,11 @@ k_count64(const fcfcg_launch L) {
         int bin = ref_bin_pair(L, w.ai, bj, code, L.box);
         if (bin < 0) continue;
         n_in++;
-        if (WT) {
+        if (ADJ) {
+          const double g = __ldg(L.gadj + bin);
+          ga = __dadd_rn(ga, __dmul_rn(L.B.w[bj], g));
+          atomicAdd(L.dB + bj, __dmul_rn(L.A.w[w.ai], g));
+        } else if (WT) {
           double v = __dmul_rn(L.A.w[w.ai], L.B.w[bj]);
           if (L.hist_smem) atomicAdd(hd + bin, v);
           else atomicAdd(L.gwd + bin, v);
@@ -941,6 +1025,7 @@ k_count64(const fcfcg_launch L) {
         }
       }
     }
+    if (ADJ && ga != 0.0) atomicAdd(L.dA + w.ai, ga);
   }
   for (int o = 16; o > 0; o >>= 1) {
     n_cand += __shfl_xor_sync(FULLMASK, n_cand, o);
@@ -951,7 +1036,7 @@ k_count64(const fcfcg_launch L) {
     atomicAdd(L.stats + 1, n_in);
   }
   __syncthreads();
-  if (L.hist_smem) {
+  if (!ADJ && L.hist_smem) {
     for (long i = threadIdx.x; i < L.ntot; i += blockDim.x) {
       if (WT) {
         double v = hd[i];
@@ -962,6 +1047,22 @@ k_count64(const fcfcg_launch L) {
       }
     }
   }
+}
+
+/* Adjoint: FP64 recheck of queued pairs. */
+__global__ void k_recheck_adj(const fcfcg_launch L, uint32_t nq) {
+  unsigned long long n_in = 0;
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq;
+       q += gridDim.x * blockDim.x) {
+    const uint4 e = ((const uint4 *) L.queue)[q];
+    int bin = ref_bin_pair(L, e.x, e.y, e.z, L.box);
+    if (bin < 0) continue;
+    n_in++;
+    adj_pair(L, e.x, e.y, bin);
+  }
+  for (int o = 16; o > 0; o >>= 1)
+    n_in += __shfl_xor_sync(FULLMASK, n_in, o);
+  if ((threadIdx.x & 31) == 0 && n_in) atomicAdd(L.stats + 1, n_in);
 }
 
 /* FP64 recheck of queued pairs. */
@@ -987,13 +1088,25 @@ __global__ void k_recheck(const fcfcg_launch L, uint32_t nq) {
 
 typedef void (*kfun_t)(const fcfcg_launch);
 
-static kfun_t pick32(int geom, int bin, int wt, int batch) {
+static kfun_t pick32(int geom, int bin, int wt, int batch, int adj) {
+  if (adj) {
+#define K32A(G, B)                                                         \
+  if (geom == G && bin == B) return (kfun_t) k_count32<G, B, 1, 0, 1>;
+    K32A(FCFCG_GEOM_BOX, FCFCG_BIN_ISO)
+    K32A(FCFCG_GEOM_BOX, FCFCG_BIN_SMU)
+    K32A(FCFCG_GEOM_BOX, FCFCG_BIN_SPI)
+    K32A(FCFCG_GEOM_SURVEY, FCFCG_BIN_ISO)
+    K32A(FCFCG_GEOM_SURVEY, FCFCG_BIN_SMU)
+    K32A(FCFCG_GEOM_SURVEY, FCFCG_BIN_SPI)
+#undef K32A
+    return 0;
+  }
   if (batch) {
     if (geom != FCFCG_GEOM_BOX) return 0;
 #define K32B(B)                                                            \
   if (bin == B)                                                            \
-    return wt ? (kfun_t) k_count32<FCFCG_GEOM_BOX, B, 1, 1>                \
-              : (kfun_t) k_count32<FCFCG_GEOM_BOX, B, 0, 1>;
+    return wt ? (kfun_t) k_count32<FCFCG_GEOM_BOX, B, 1, 1, 0>             \
+              : (kfun_t) k_count32<FCFCG_GEOM_BOX, B, 0, 1, 0>;
     K32B(FCFCG_BIN_ISO)
     K32B(FCFCG_BIN_SMU)
     K32B(FCFCG_BIN_SPI)
@@ -1002,8 +1115,8 @@ static kfun_t pick32(int geom, int bin, int wt, int batch) {
   }
 #define K32(G, B)                                                          \
   if (geom == G && bin == B)                                               \
-    return wt ? (kfun_t) k_count32<G, B, 1, 0>                             \
-              : (kfun_t) k_count32<G, B, 0, 0>;
+    return wt ? (kfun_t) k_count32<G, B, 1, 0, 0>                          \
+              : (kfun_t) k_count32<G, B, 0, 0, 0>;
   K32(FCFCG_GEOM_BOX, FCFCG_BIN_ISO)
   K32(FCFCG_GEOM_BOX, FCFCG_BIN_SMU)
   K32(FCFCG_GEOM_BOX, FCFCG_BIN_SPI)
@@ -1014,12 +1127,15 @@ static kfun_t pick32(int geom, int bin, int wt, int batch) {
   return 0;
 }
 
-static kfun_t pick64(int geom, int wt) {
+static kfun_t pick64(int geom, int wt, int adj) {
+  if (adj)
+    return geom == FCFCG_GEOM_BOX ? (kfun_t) k_count64<FCFCG_GEOM_BOX, 1, 1>
+                                  : (kfun_t) k_count64<FCFCG_GEOM_SURVEY, 1, 1>;
   if (geom == FCFCG_GEOM_BOX)
-    return wt ? (kfun_t) k_count64<FCFCG_GEOM_BOX, 1>
-              : (kfun_t) k_count64<FCFCG_GEOM_BOX, 0>;
-  return wt ? (kfun_t) k_count64<FCFCG_GEOM_SURVEY, 1>
-            : (kfun_t) k_count64<FCFCG_GEOM_SURVEY, 0>;
+    return wt ? (kfun_t) k_count64<FCFCG_GEOM_BOX, 1, 0>
+              : (kfun_t) k_count64<FCFCG_GEOM_BOX, 0, 0>;
+  return wt ? (kfun_t) k_count64<FCFCG_GEOM_SURVEY, 1, 0>
+            : (kfun_t) k_count64<FCFCG_GEOM_SURVEY, 0, 0>;
 }
 
 extern "C" int fcfcg_k_count(void *stream, const fcfcg_launch *L,
@@ -1028,14 +1144,17 @@ extern "C" int fcfcg_k_count(void *stream, const fcfcg_launch *L,
   size_t smem;
   int threads;
   if (precision == FCFCG_PREC_FP64) {
-    f = pick64(L->geometry, L->withwt);
-    smem = L->hist_smem ? (size_t) L->ntot * (L->withwt ? 8 : 4) : 0;
+    f = pick64(L->geometry, L->withwt, L->adjoint);
+    smem = (L->hist_smem && !L->adjoint)
+               ? (size_t) L->ntot * (L->withwt ? 8 : 4) : 0;
     threads = CT_THREADS;
   } else {
-    f = pick32(L->geometry, L->bintype, L->withwt, L->mocks != NULL);
+    f = pick32(L->geometry, L->bintype, L->withwt, L->mocks != NULL,
+               L->adjoint);
     size_t tab = fcfcg_k_count32_tab_bytes(L->nfs, L->nfp, L->nsb, L->npb);
     smem = tab + (L->hist_smem ? (size_t) L->ntot * (L->withwt ? 8 : 4) : 0);
-    smem = ((smem + 15) & ~(size_t) 15) + stage_bytes(L->nsten, L->withwt);
+    smem = ((smem + 15) & ~(size_t) 15) +
+           stage_bytes(L->nsten, L->withwt + L->adjoint);
     threads = CT32_THREADS;
   }
   if (!f) return (int) cudaErrorInvalidValue;
@@ -1070,7 +1189,9 @@ extern "C" int fcfcg_k_recheck(void *stream, const fcfcg_launch *L,
   if (!nq) return 0;
   unsigned blocks = (nq + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
-  if (L->withwt)
+  if (L->adjoint)
+    k_recheck_adj<<<blocks, 256, 0, (cudaStream_t) stream>>>(*L, nq);
+  else if (L->withwt)
     k_recheck<1><<<blocks, 256, 0, (cudaStream_t) stream>>>(*L, nq);
   else
     k_recheck<0><<<blocks, 256, 0, (cudaStream_t) stream>>>(*L, nq);

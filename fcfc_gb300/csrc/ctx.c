@@ -77,6 +77,8 @@ struct fcfcg_ctx {
   size_t d_mock_cap;
   uint32_t *d_mbase;
   size_t d_mbase_cap;
+  double *d_grad;                /* adjoint: sorted and input-order gradients */
+  size_t d_grad_cap;
   unsigned long long *d_bout, *d_bstat;
   size_t d_bout_cap, d_bstat_cap;
 };
@@ -178,7 +180,7 @@ void fcfcg_destroy(fcfcg_ctx *c) {
                  c->d_fp, c->d_rs, c->d_rp, c->d_s2edge, c->d_pedge,
                  c->d_sten, c->d_stenD, c->d_cnt, c->d_wt, c->d_stats,
                  c->d_bbox, c->d_wd, c->d_head, c->d_queue, c->d_cnvt,
-                 c->d_mock, c->d_mbase, c->d_bout, c->d_bstat};
+                 c->d_mock, c->d_mbase, c->d_bout, c->d_bstat, c->d_grad};
     for (size_t i = 0; i < sizeof p / sizeof p[0]; i++)
       if (p[i]) cudaFree(p[i]);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
@@ -856,7 +858,7 @@ static void launch_bins(const fcfcg_ctx *c, fcfcg_launch *L) {
     L->pmax = b->p.vmax;
     L->pmin0 = b->p.min0;
   }
-  L->fixF = 42;
+  L->fixF = FCFCG_FIX_F;
   L->gcnt = c->d_cnt;
   L->gwt = c->d_wt;
   L->gwd = c->d_wd;
@@ -895,8 +897,30 @@ static int ensure_pinned(fcfcg_ctx *c, size_t bytes) {
   return FCFCG_OK;
 }
 
+/* Adjoint request of count_impl: cotangent in, gradients out (host). */
+typedef struct {
+  const double *g;
+  double *dwa, *dwb;
+} adj_req;
+
+static int count_impl(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
+    int precision, int64_t *icnt, double *wcnt, const adj_req *adj);
+
 int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
     int precision, int64_t *icnt, double *wcnt) {
+  return count_impl(c, sa, sb, isauto, withwt, precision, icnt, wcnt, NULL);
+}
+
+int fcfcg_adjoint(fcfcg_ctx *c, int sa, int sb, int isauto, const double *g,
+    double *dwa, double *dwb) {
+  if (!c || !g || !dwa) return FCFCG_ERR_ARG;
+  adj_req r = {g, dwa, isauto ? NULL : dwb};
+  return count_impl(c, sa, sb, isauto, 1, FCFCG_PREC_FP32_RECHECK, NULL,
+                    NULL, &r);
+}
+
+static int count_impl(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
+    int precision, int64_t *icnt, double *wcnt, const adj_req *adj) {
   if (!c || c->host_only) return FCFCG_ERR_ARG;
   const int nslot = FCFCG_MAX_SLOT + c->internal;
   if (sa < 0 || sa >= nslot || sb < 0 || sb >= nslot) {
@@ -909,7 +933,7 @@ int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
   }
   if (precision != FCFCG_PREC_FP32_RECHECK && precision != FCFCG_PREC_FP64)
     return FCFCG_ERR_ARG;
-  if ((withwt && !wcnt) || (!withwt && !icnt)) return FCFCG_ERR_ARG;
+  if (!adj && ((withwt && !wcnt) || (!withwt && !icnt))) return FCFCG_ERR_ARG;
   CK(cudaSetDevice(c->device));
   const fcfcg_bins *b = &c->bins;
   slot_t *A = c->slot + sa, *B = c->slot + sb;
@@ -921,6 +945,10 @@ int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
   if (A->n == 0 || B->n == 0) {
     if (icnt) memset(icnt, 0, sizeof(int64_t) * b->ntot);
     if (wcnt) memset(wcnt, 0, sizeof(double) * b->ntot);
+    if (adj) {
+      memset(adj->dwa, 0, sizeof(double) * A->n);
+      if (adj->dwb) memset(adj->dwb, 0, sizeof(double) * B->n);
+    }
     return FCFCG_OK;
   }
   CK(cudaEventRecord(c->ev[0], c->stream));
@@ -978,13 +1006,24 @@ int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
       ? fcfcg_k_count32_tab_bytes(L.nfs, L.nfp, L.nsb, L.npb) : 0;
   size_t hbytes = (size_t) b->ntot * (withwt ? 8 : 4);
   size_t stage = (prec == FCFCG_PREC_FP32_RECHECK)
-      ? fcfcg_k_count32_stage(nsten, withwt) : 0;
+      ? fcfcg_k_count32_stage(nsten, withwt + (adj ? 1 : 0)) : 0;
   if (tabbytes + stage > 200 * 1024) {
     prec = FCFCG_PREC_FP64;
     tabbytes = 0;
     stage = 0;
   }
   L.hist_smem = (tabbytes + stage + hbytes <= 200 * 1024);
+  if (adj) {
+    const size_t ng = A->n + (isauto ? 0 : B->n);
+    GROW(c->d_grad, c->d_grad_cap, sizeof(double) * 2 * ng);
+    L.adjoint = 1;
+    L.gadj = c->d_wd;
+    L.dA = c->d_grad;
+    L.dB = isauto ? c->d_grad : c->d_grad + A->n;
+    CK(cudaMemcpyAsync(c->d_wd, adj->g, sizeof(double) * b->ntot,
+                       cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(c->d_grad, 0, sizeof(double) * ng, c->stream));
+  }
 
   /* work chunks: 64 points per CTA in the FP32 kernel, 32 per warp in the
    * FP64 kernel */
@@ -1001,7 +1040,8 @@ int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
                      c->stream));
   CK(cudaMemsetAsync(c->d_wt, 0, sizeof(unsigned long long) * 2 * b->ntot,
                      c->stream));
-  CK(cudaMemsetAsync(c->d_wd, 0, sizeof(double) * b->ntot, c->stream));
+  if (!adj)
+    CK(cudaMemsetAsync(c->d_wd, 0, sizeof(double) * b->ntot, c->stream));
   CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * 4, c->stream));
   CK(cudaMemsetAsync(c->d_head, 0, sizeof(uint32_t) * 2, c->stream));
   CK(cudaEventRecord(c->ev[2], c->stream));
@@ -1019,6 +1059,38 @@ int fcfcg_count(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
     c->launches += nq ? 1 : 0;
   }
   CK(cudaEventRecord(c->ev[4], c->stream));
+  if (adj) {
+    /* sorted order back to input order, then to the host */
+    const size_t ng = A->n + (isauto ? 0 : B->n);
+    double *unsorted = c->d_grad + ng;
+    CKK(fcfcg_k_unsort(c->stream, A->n, A->sid, L.dA, unsorted));
+    if (!isauto)
+      CKK(fcfcg_k_unsort(c->stream, B->n, B->sid, L.dB, unsorted + A->n));
+    c->launches += isauto ? 1 : 2;
+    unsigned long long hst[4];
+    CK(cudaMemcpyAsync(adj->dwa, unsorted, sizeof(double) * A->n,
+                       cudaMemcpyDeviceToHost, c->stream));
+    if (!isauto && adj->dwb)
+      CK(cudaMemcpyAsync(adj->dwb, unsorted + A->n, sizeof(double) * B->n,
+                         cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(hst, c->d_stats, sizeof hst, cudaMemcpyDeviceToHost,
+                       c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    fcfcg_stats *o = &c->stats;
+    o->candidates = hst[0];
+    o->in_range = hst[1];
+    o->rechecked = hst[2];
+    o->recheck_inline = hst[3];
+    float ms = 0;
+    cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
+    o->ms_count = ms;
+    cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]);
+    o->ms_total = ms;
+    o->cells_per_smax = g.k;
+    o->precision_used = prec;
+    o->launches = c->launches;
+    return FCFCG_OK;
+  }
   /* results */
   size_t rbytes = sizeof(unsigned long long) * 2 * b->ntot + 64;
   if ((rc = ensure_pinned(c, rbytes))) return rc;

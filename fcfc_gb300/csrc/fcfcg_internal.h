@@ -18,6 +18,7 @@ extern "C" {
 #define FCFCG_CHUNK 32            /* chunk length of the FP64 kernel */
 #define FCFCG_CHUNK32 64          /* chunk length of the FP32 kernel */
 #define FCFCG_MAX_STENCIL 4096
+#define FCFCG_FIX_F 51            /* fractional bits of a weight product */
 /* FP32 edge-window tables: one uint16 per cell of width w = 2^-shift units
  * of the binned quantity; cell i covers [i w, (i + 1) w). */
 #define FCFCG_FTAB_BIN_MASK 0x0FFFu /* bin at the cell start, or "out" */
@@ -148,6 +149,11 @@ typedef struct {
    * catalogue, queue entries carry it too */
   const fcfcg_mock *mocks;
   int nmock;
+  /* adjoint of the weighted counts: gadj[ntot] in, FP64 gradients per
+   * sorted point out (dA, dB; the same array for auto counts) */
+  int adjoint;
+  const double *gadj;
+  double *dA, *dB;
 } fcfcg_launch;
 
 /* Launchers implemented in the .cu files; return 0 or a CUDA error code. */
@@ -177,8 +183,12 @@ int fcfcg_k_scatter_batch(void *stream, size_t n, const double *x,
     uint32_t id_base, const uint32_t *cell_of, const uint32_t *cstart,
     uint32_t *cfill, float *l4, int *wq, double *sx, double *sy, double *sz,
     double *sw, uint32_t *sid);
+/* out[sid[p]] = in[p] for p < n (sorted order back to input order). */
+int fcfcg_k_unsort(void *stream, size_t n, const uint32_t *sid,
+    const double *in, double *out);
 int fcfcg_scan(void *stream, const uint32_t *in, size_t n, uint32_t *out,
     uint32_t *tmp);
+/* withwt: 0 unweighted, 1 weighted, 2 adjoint */
 size_t fcfcg_k_count32_stage(int nsten, int withwt);
 size_t fcfcg_k_count32_tab_bytes(int nfs, int nfp, int nsb, int npb);
 int fcfcg_k_bbox(void *stream, size_t n, const double *x, const double *y,

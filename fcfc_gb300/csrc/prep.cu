@@ -405,6 +405,21 @@ extern "C" int fcfcg_k_chunks(void *stream, const uint32_t *cstart,
   return 0;
 }
 
+__global__ void k_unsort(size_t n, const uint32_t *__restrict__ sid,
+    const double *__restrict__ in, double *__restrict__ out) {
+  for (size_t p = blockIdx.x * (size_t) blockDim.x + threadIdx.x; p < n;
+       p += (size_t) gridDim.x * blockDim.x)
+    out[sid[p]] = in[p];
+}
+
+extern "C" int fcfcg_k_unsort(void *stream, size_t n, const uint32_t *sid,
+    const double *in, double *out) {
+  if (!n) return 0;
+  k_unsort<<<grid_for(n, PREP_THREADS), PREP_THREADS, 0,
+             (cudaStream_t) stream>>>(n, sid, in, out);
+  return (int) cudaGetLastError();
+}
+
 extern "C" const char *fcfcg_cuda_errstr(int code) {
   return cudaGetErrorString((cudaError_t) code);
 }

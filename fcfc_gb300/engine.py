@@ -253,6 +253,24 @@ class PairCounter:
         del keep, outs
         return k.value, ms.value
 
+    def adjoint(self, a: int, b: int | None, g):
+        """Gradient of sum_k g_k C_k (C: the weighted count of slots a, b as
+        count_pairs(weighted=True) returns it) with respect to the weights of
+        slot a (and of slot b for a cross count): (dw_a, dw_b or None)."""
+        isauto = b is None or b == a
+        g = np.ascontiguousarray(g, np.float64)
+        if g.shape != (self.ntot,):
+            raise ValueError("g needs %d entries" % self.ntot)
+        na = self._n.get(a, (0, False))[0]
+        dwa = np.zeros(na)
+        dwb = None
+        if not isauto:
+            dwb = np.zeros(self._n.get(b, (0, False))[0])
+        self._check(self.lib.fcfcg_adjoint(self.h, a, a if isauto else b,
+                                           int(isauto), capi.ptr(g),
+                                           capi.ptr(dwa), capi.ptr(dwb)))
+        return dwa, dwb
+
     def stats(self) -> dict:
         s = capi.Stats()
         self._check(self.lib.fcfcg_stats_get(self.h, C.byref(s)))

@@ -279,6 +279,22 @@ int fcfcg_catalog_info(const fcfcg_ctx *ctx, int slot, size_t *n,
 int fcfcg_count(fcfcg_ctx *ctx, int slot_a, int slot_b, int isauto,
     int withwt, int precision, int64_t *icnt, double *wcnt);
 
+/*
+ * Adjoint of the weighted count (no reference counterpart: FCFC has no
+ * derivatives).  With C_b = sum over counted pairs (i, j) in bin b of
+ * w_i w_j, as fcfcg_count(withwt = 1) returns it, and a cotangent g[ntot]
+ * (host), this writes the gradient of sum_b g_b C_b with respect to the
+ * weights: dw_a[i] = sum_j w_j g[bin(i, j)] over catalogue a (input order,
+ * n_a entries) and, for a cross count, dw_b likewise over catalogue b (may
+ * be NULL).  For auto counts every unordered pair feeds both of its points.
+ * The pair bins are recomputed, exactly as the count bins them (FP32 windows
+ * with the FP64 recheck); the gradients are FP64 sums.  Catalogues without
+ * weights count as unit weights.  Where the count falls back to the
+ * all-FP64 kernel (FP32 windows too wide), so does the adjoint.
+ */
+int fcfcg_adjoint(fcfcg_ctx *ctx, int slot_a, int slot_b, int isauto,
+    const double *g, double *dw_a, double *dw_b);
+
 int fcfcg_stats_get(const fcfcg_ctx *ctx, fcfcg_stats *out);
 
 /* Grid refinement: cells per maximum separation (0 = automatic). */

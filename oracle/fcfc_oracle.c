@@ -904,3 +904,37 @@ size_t fco_cnvt_spline(size_t m, const double *zs, const double *ds,
   free(cp);
   return bad;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Per-object gradient of sum_b g_b C_b, C_b the weighted count (the engine's */
+/* adjoint has no reference counterpart; this is its CPU reference).        */
+/* Brute force over pairs, FP64: dwa[i] = sum_j w_j g[bin(i, j)], dwb[j] =   */
+/* sum_i w_i g[bin(i, j)]; for auto counts every unordered pair feeds both   */
+/* points of dwa.  Returns 0, or -1 when out of memory.                      */
+int fco_adjoint(const fco_bins *b, size_t na, const double *ax,
+    const double *ay, const double *az, const double *aw, size_t nb,
+    const double *bx, const double *by, const double *bz, const double *bw,
+    int isauto, const double *g, double *dwa, double *dwb) {
+  fco_cat A, B;
+  if (fco_cat_make(&A, b, na, ax, ay, az, aw)) return -1;
+  if (isauto) B = A;
+  else if (fco_cat_make(&B, b, nb, bx, by, bz, bw)) { fco_cat_free(&A); return -1; }
+  for (size_t i = 0; i < A.n; i++) dwa[i] = 0;
+  if (!isauto && dwb)
+    for (size_t j = 0; j < B.n; j++) dwb[j] = 0;
+  for (size_t i = 0; i < A.n; i++) {
+    for (size_t j = isauto ? i + 1 : 0; j < B.n; j++) {
+      double sh[3] = {0, 0, 0};
+      if (!b->survey)
+        fco_min_image(b, A.x[i], A.y[i], A.z[i], B.x[j], B.y[j], B.z[j], sh);
+      long k = fco_pair(b, &A, i, &B, j, sh, isauto);
+      if (k < 0) continue;
+      dwa[i] += B.w[j] * g[k];
+      if (isauto) dwa[j] += A.w[i] * g[k];
+      else if (dwb) dwb[j] += A.w[i] * g[k];
+    }
+  }
+  fco_cat_free(&A);
+  if (!isauto) fco_cat_free(&B);
+  return 0;
+}

@@ -68,6 +68,9 @@ def lib():
         L.fco_count.restype = C.c_int
         L.fco_count.argtypes = [P, C.c_size_t, P, P, P, P, C.c_size_t, P, P, P, P,
                                 C.c_int, C.c_int, C.c_int, C.c_int, P, P]
+        L.fco_adjoint.restype = C.c_int
+        L.fco_adjoint.argtypes = [P, C.c_size_t, P, P, P, P, C.c_size_t, P, P,
+                                  P, P, C.c_int, P, P, P]
         L.fco_cnvt_order.restype = C.c_int
         L.fco_cnvt_order.argtypes = [D, D, D, D, D, C.c_size_t, P]
         L.fco_cnvt_integr.argtypes = [D, D, D, D, C.c_int, C.c_size_t, P, P, P,
@@ -175,6 +178,32 @@ class Bins:
         if rc:
             raise MemoryError("oracle count failed")
         return wcnt if weighted else icnt
+
+    def adjoint(self, a, g, b=None, wa=None, wb=None):
+        """Gradient of sum_b g_b C_b over the weights, C the weighted count
+        (brute force, FP64): (dwa, dwb); dwb is None for auto counts."""
+        isauto = b is None
+        a = np.ascontiguousarray(a, np.float64)
+        cols_a = [np.ascontiguousarray(a[:, k]) for k in range(3)]
+        wa_ = None if wa is None else np.ascontiguousarray(wa, np.float64)
+        g = np.ascontiguousarray(g, np.float64)
+        dwa = np.zeros(len(a))
+        dwb = None
+        if isauto:
+            cols_b, wb_, nb = [None] * 3, None, 0
+        else:
+            b = np.ascontiguousarray(b, np.float64)
+            cols_b = [np.ascontiguousarray(b[:, k]) for k in range(3)]
+            wb_ = None if wb is None else np.ascontiguousarray(wb, np.float64)
+            nb = len(b)
+            dwb = np.zeros(nb)
+        rc = lib().fco_adjoint(self.h, len(a), *[_ptr(c) for c in cols_a],
+                               _ptr(wa_), nb, *[_ptr(c) for c in cols_b],
+                               _ptr(wb_), int(isauto), _ptr(g), _ptr(dwa),
+                               _ptr(dwb))
+        if rc:
+            raise MemoryError("oracle adjoint failed")
+        return dwa, dwb
 
 
 def cosmo_params(omega_m, omega_l=None, dew=-1.0):
