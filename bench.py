@@ -349,6 +349,243 @@ def run_mocks(args, rank, world, local, dist):
     return 0
 
 
+def survey_workload(nd, nr, seed=11):
+    """RA uniform in [100, 260) deg, sin(Dec) uniform over [0, 60) deg,
+    z ~ N(0.55, 0.10) truncated to [0.4, 0.7]; FKP weights 1 / (1 + n(z) P0),
+    P0 = 1e4, n(z) from the data in dz = 0.01 shells (flat LCDM, Om = 0.31),
+    applied to data and randoms alike."""
+    from fcfc_gb300 import synth
+    d = synth.survey_radecz(nd, seed=seed)
+    r = synth.survey_radecz(nr, seed=seed + 1)
+    wd = synth.fkp_weights(d)
+    # the randoms carry the data's n(z) at their redshifts
+    z = d[:, 2]
+    edges = np.arange(z.min(), z.max() + 0.01, 0.01)
+    nz_w = synth.fkp_weights(d)
+    idx = np.clip(np.searchsorted(edges, r[:, 2], side="right") - 1, 0,
+                  len(edges) - 2)
+    per = np.zeros(len(edges) - 1)
+    cnt = np.zeros(len(edges) - 1)
+    di = np.clip(np.searchsorted(edges, z, side="right") - 1, 0, len(edges) - 2)
+    np.add.at(per, di, nz_w)
+    np.add.at(cnt, di, 1)
+    wr = (per / np.maximum(cnt, 1))[idx]
+    return d, r, wd, wr
+
+
+def _dev(a, dev):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def run_survey(args, rank, world, local, dist):
+    """Survey Landy-Szalay counts: DD, DR, RR weighted, in (s, mu) 40 x 100
+    and (s_perp, pi) 40 log x 40, RA/Dec/z converted on the device."""
+    import torch
+    import fcfc_gb300 as fg
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    nd, nr = (100000, 1000000) if args.small else (1000000, 10000000)
+    d, r, wd, wr = survey_workload(nd, nr, seed=11 + rank)
+    D = [_dev(d[:, k], dev) for k in range(3)] + [_dev(wd, dev)]
+    R = [_dev(r[:, k], dev) for k in range(3)] + [_dev(wr, dev)]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    p1 = fg.PairCounter("survey", fg.BIN_SMU, smin=0, smax=200, ds=5, nmu=100,
+                        device=local)
+    p2 = fg.PairCounter("survey", fg.BIN_SPI, sedges=LOGBINS, pmin=0, pmax=40,
+                        dpi=1, device=local)
+
+    def load(pc):
+        pc.load_radecz_device(0, D[0].data_ptr(), D[1].data_ptr(),
+                              D[2].data_ptr(), nd, D[3].data_ptr())
+        pc.load_radecz_device(1, R[0].data_ptr(), R[1].data_ptr(),
+                              R[2].data_ptr(), nr, R[3].data_ptr())
+
+    def step(weighted=True, prec=fg.PREC_FP32_RECHECK, pairs=("DD", "DR", "RR")):
+        res = {}
+        kms = {}
+        for name, pc in (("smu", p1), ("spi", p2)):
+            load(pc)
+            for pr in pairs:
+                a, b = (0, None) if pr == "DD" else ((0, 1) if pr == "DR" else (1, None))
+                res[(name, pr)] = pc.count_pairs(a, b, weighted=weighted,
+                                                 precision=prec)
+                kms[(name, pr)] = pc.stats()["ms_count"]
+        return res, kms
+
+    cnt, _ = step(weighted=False)
+    pairs = {k: int(v.sum()) for k, v in cnt.items()}
+    pairs_step = sum(pairs.values())
+    for _ in range(max(args.warmup, 0)):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = ClockSampler(local)
+    clk.start()
+    l0 = p1.stats()["launches"] + p2.stats()["launches"]
+    tt = 0.0
+    kt = {}
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, kms = step()
+        tt += time.perf_counter() - t0
+        for k, v in kms.items():
+            kt[k] = kt.get(k, 0.0) + v
+    clocks = clk.stop()
+    launches = p1.stats()["launches"] + p2.stats()["launches"] - l0
+    ms_step = max_over_ranks(tt / args.steps * 1e3, dist)
+    value = pairs_step * world / (ms_step * 1e-3)
+    # all-FP64 path on DD (both binnings), against FP32 + recheck
+    t0 = time.perf_counter()
+    c64, k64 = step(prec=fg.PREC_FP64, pairs=("DD",))
+    ms64 = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    c32, _ = step(pairs=("DD",))
+    ms32 = (time.perf_counter() - t0) * 1e3
+    rel = max(float(np.max(np.abs(c32[k] - c64[k]) /
+                           np.maximum(np.abs(c64[k]), 1e-300))) for k in c64)
+    dd_pairs = pairs[("smu", "DD")] + pairs[("spi", "DD")]
+    # end to end from host arrays (conversion included)
+    def e2e():
+        for pc in (p1, p2):
+            pc.load_radecz(0, d, wd)
+            pc.load_radecz(1, r, wr)
+            pc.count_pairs(0, weighted=True)
+            pc.count_pairs(0, 1, weighted=True)
+            pc.count_pairs(1, weighted=True)
+    e2e()
+    t0 = time.perf_counter()
+    e2e()
+    e2e_ms = (time.perf_counter() - t0) * 1e3
+    peak = fp32_peak_tflops(dev)
+    k_rr = kt[("smu", "RR")] / args.steps
+    achieved = pairs[("smu", "RR")] * FLOPS_PER_PAIR["smu"] / (k_rr * 1e-3) / 1e12
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64-recheck", "data": "synthetic",
+        "config": {"workload": "survey_ls_%dx%d" % (nd, nr), "n_data": nd,
+                   "n_random": nr, "weights": "FKP, P0 = 1e4",
+                   "coordinates": "RA/Dec/z converted on the device (Om = 0.31)",
+                   "bins": "(s,mu) 40x100 s<200 + (s_perp,pi) 40 log [0.1,100) x 40 lin [0,40)",
+                   "pairs": {"%s_%s" % k: v for k, v in pairs.items()},
+                   "pairs_per_step": pairs_step,
+                   "l2": "flushed between steps (256 MiB write)",
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "fp64": {"value": dd_pairs / (ms64 * 1e-3), "unit": UNIT,
+                 "counts": "DD (s,mu) + DD (s_perp,pi)", "ms": ms64,
+                 "fp32_recheck_ms_same_counts": ms32,
+                 "speedup_fp32_recheck_over_fp64": ms64 / ms32,
+                 "max_rel_diff_weighted": rel},
+        "e2e": {"value": pairs_step / (e2e_ms * 1e-3), "unit": UNIT,
+                "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": 2 * (nd + nr) * 32,
+                "d2h_bytes_per_step": 3 * (p1.ntot + p2.ntot) * 8},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,
+                     "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                     "kernel": "k_count32<survey,smu,weighted> (RR)",
+                     "kernel_ms": k_rr,
+                     "peak_source": "measured cuBLAS SGEMM (TF32 off) on this GPU",
+                     "flops_per_pair": FLOPS_PER_PAIR["smu"]},
+        "counters": {"kernel_ms_%s_%s" % k: v / args.steps for k, v in kt.items()},
+        "clocks": clocks,
+        "gpu_launches": int(launches),
+    }
+    if dist:
+        dist.barrier()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    return 0
+
+
+def run_adjoint(args, rank, world, local, dist):
+    """dL/dw for every data weight, L = sum_b g_b xi_LS(b) over (s, mu)
+    40 x 100, data 5e5 (lognormal weights) and randoms 5e6 of the survey
+    generator: forward DD, DR, RR and the adjoint of DD and DR."""
+    import torch
+    import fcfc_gb300 as fg
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from fcfc_gb300 import synth
+    nd, nr = (50000, 500000) if args.small else (500000, 5000000)
+    d = synth.radecz_to_xyz(synth.survey_radecz(nd, seed=31 + rank))
+    r = synth.radecz_to_xyz(synth.survey_radecz(nr, seed=32 + rank))
+    wd = synth.lognormal_weights(nd, 0.3, seed=33 + rank)
+    pc = fg.PairCounter("survey", fg.BIN_SMU, smin=0, smax=200, ds=5, nmu=100,
+                        device=local)
+    g = np.random.default_rng(34).normal(size=pc.ntot)
+    pc.load(0, d, wd)
+    pc.load(1, r)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def forward():
+        dd = pc.count_pairs(0, weighted=True)
+        dr = pc.count_pairs(0, 1, weighted=True)
+        rr = pc.count_pairs(1, weighted=True)
+        return dd, dr, rr
+
+    def backward(dd, dr, rr):
+        W, Wr = float(np.sum(wd)), float(nr)
+        nDD, nDR, nRR = W * (W - 1), W * Wr, Wr * (Wr - 1)
+        rrn = 2 * rr / nRR
+        ok = rrn > 0
+        gdd = np.where(ok, g * 2 / nDD / np.where(ok, rrn, 1), 0.0)
+        gdr = np.where(ok, -g * 2 / nDR / np.where(ok, rrn, 1), 0.0)
+        a1, _ = pc.adjoint(0, None, gdd)
+        ms1 = pc.stats()["ms_total"]
+        a2, _ = pc.adjoint(0, 1, gdr)
+        ms2 = pc.stats()["ms_total"]
+        return a1 + a2, ms1 + ms2
+
+    un = [int(pc.count_pairs(0).sum()), int(pc.count_pairs(0, 1).sum())]
+    pairs_grad = sum(un)
+    for _ in range(max(args.warmup, 0)):
+        backward(*forward())
+    torch.cuda.synchronize()
+    clk = ClockSampler(local)
+    clk.start()
+    tf = tb = 0.0
+    kb = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c = forward()
+        t1 = time.perf_counter()
+        grad, msb = backward(*c)
+        t2 = time.perf_counter()
+        tf += t1 - t0
+        tb += t2 - t1
+        kb += msb
+    clocks = clk.stop()
+    ms_b = max_over_ranks(tb / args.steps * 1e3, dist)
+    out = {
+        "metric": "adjoint: DD + DR pairs differentiated per second (dL/dw for "
+                  "all data weights)",
+        "value": pairs_grad * world / (ms_b * 1e-3), "unit": UNIT,
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_b, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64-recheck bins, f64 gradients",
+        "data": "synthetic",
+        "config": {"workload": "adjoint_ls_%dx%d" % (nd, nr), "n_data": nd,
+                   "n_random": nr, "bins": "(s,mu) 40x100 s<200",
+                   "loss": "sum_b g_b xi_LS(b), g ~ N(0,1)",
+                   "pairs_dd_dr": pairs_grad,
+                   "forward_ms_dd_dr_rr": tf / args.steps * 1e3,
+                   "backward_device_ms": kb / args.steps,
+                   "grad_norm": float(np.linalg.norm(grad)),
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    return 0
+
+
 def cpu_baseline_sample(x, w, box):
     """The CPU restatement of FCFC's counter (oracle/, OpenMP on every host
     core) on the whole workload, one weighted step: 10-30 s of CPU work."""
@@ -377,8 +614,10 @@ def main():
                     help="quarter-size box (for profiler captures)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="ns_box_2e6",
-                    choices=["ns_box_2e6", "mocks256"],
-                    help="mocks256: 256 mock boxes in one persistent launch")
+                    choices=["ns_box_2e6", "mocks256", "survey", "adjoint"],
+                    help="mocks256: 256 mock boxes in one persistent launch; "
+                         "survey: DD/DR/RR of 1e6 data and 1e7 randoms; "
+                         "adjoint: dL/dw of a Landy-Szalay loss")
     args = ap.parse_args()
     rank, world, local = env_rank()
     dist = None
@@ -393,6 +632,10 @@ def main():
 
     if args.workload == "mocks256":
         return run_mocks(args, rank, world, local, dist)
+    if args.workload == "survey":
+        return run_survey(args, rank, world, local, dist)
+    if args.workload == "adjoint":
+        return run_adjoint(args, rank, world, local, dist)
     import torch
     import fcfc_gb300 as fg
     torch.cuda.set_device(local)

@@ -808,14 +808,10 @@ static int fp32_bounds(const fcfcg_ctx *c, const grid_t *g, double dmax,
   if (!(Es < 0.45 * ldexp(1.0, b->s.fshift))) return -1;
   if (b->bintype == FCFCG_BIN_SPI && !(Ep < 0.45 * ldexp(1.0, b->p.fshift)))
     return -1;
-  /* the FP32 tables must cover every value below the limits */
-  if ((double) L->s_lim * ldexp(1.0, -b->s.fshift) >=
-      (double) (b->s.foff + b->s.nftab - 1))
-    return -1;
-  if (b->bintype == FCFCG_BIN_SPI && box &&
-      (double) L->p_lim * ldexp(1.0, -b->p.fshift) >=
-          (double) (b->p.foff + b->p.nftab - 1))
-    return -1;
+  /* Values beyond either end of an FP32 table need no check: a table runs
+   * from at least one cell below its lowest edge to at least one cell above
+   * its highest (fcfcg_axis_ftab), so an FP32 value outside it is more than
+   * a cell, hence more than its window, away from every edge. */
   return 0;
 }
 

@@ -137,6 +137,19 @@ class PairCounter:
         del keep
         self._n[slot] = (len(a), w is not None)
 
+    def load_radecz_device(self, slot: int, ra_ptr: int, dec_ptr: int,
+                           z_ptr: int, n: int, w_ptr: int | None = None,
+                           omega_m=0.31, omega_l=None, dew=-1.0,
+                           cmvdst_err=0.0, ztable=None):
+        """load_radecz from device FP64 arrays (the inputs are not changed)."""
+        cs, keep = capi.make_cosmo(omega_m, omega_l, dew, cmvdst_err, ztable)
+        vp = C.c_void_p
+        self._check(self.lib.fcfcg_load_catalog_radecz_device(
+            self.h, int(slot), int(n), vp(ra_ptr), vp(dec_ptr), vp(z_ptr),
+            vp(w_ptr) if w_ptr else None, C.byref(cs)))
+        del keep
+        self._n[slot] = (int(n), w_ptr is not None)
+
     def convert_device(self, n: int, ra_ptr: int, dec_ptr: int, z_ptr: int,
                        x_ptr: int, y_ptr: int, zc_ptr: int, omega_m=0.31,
                        omega_l=None, dew=-1.0, cmvdst_err=0.0, ztable=None):

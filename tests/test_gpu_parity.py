@@ -166,6 +166,8 @@ def test_survey_vs_oracle(cfg, weighted):
         _assert_counts(pc.count_pairs(0, weighted=weighted, precision=prec),
                        ob.count(d, wa=wd, weighted=weighted), weighted,
                        "%s DD prec %d" % (name, prec))
+        # these separations keep the FP32 windows narrow: no FP64 fallback
+        assert pc.stats()["precision_used"] == prec
         _assert_counts(pc.count_pairs(0, 1, weighted=weighted, precision=prec),
                        ob.count(d, r, wa=wd, weighted=weighted), weighted,
                        "%s DR prec %d" % (name, prec))
