@@ -31,7 +31,7 @@ class Binning(C.Structure):
                 ("box", C.c_double * 3), ("ns", C.c_int), ("smin", C.c_double),
                 ("ds", C.c_double), ("sedges", _dp), ("nmu", C.c_int),
                 ("np", C.c_int), ("pmin", C.c_double), ("dpi", C.c_double),
-                ("pedges", _dp)]
+                ("pedges", _dp), ("with_mu_one", C.c_int)]
 
 
 class BinsInfo(C.Structure):
@@ -184,7 +184,7 @@ def ptr(a):
 
 def make_binning(geometry, bintype, box=None, ns=None, smin=0.0, ds=1.0,
                  sedges=None, nmu=1, np_=0, pmin=0.0, dpi=1.0, pedges=None,
-                 smax=None, pmax=None):
+                 smax=None, pmax=None, with_mu_one=False):
     """Binning struct plus the arrays it points to (keep both alive)."""
     lib = load_library()
     keep = []
@@ -212,4 +212,5 @@ def make_binning(geometry, bintype, box=None, ns=None, smin=0.0, ds=1.0,
         if bintype == BIN_SPI and not np_:
             np_ = lib.fcfcg_linear_nbin(pmin, pmax, dpi)
         b.np, b.pmin, b.dpi = int(np_), float(pmin), float(dpi)
+    b.with_mu_one = int(bool(with_mu_one))
     return b, keep

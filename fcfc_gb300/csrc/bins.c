@@ -281,6 +281,7 @@ int fcfcg_bins_setup(const fcfcg_binning *cfg, fcfcg_bins *b, char *err,
   b->ns = ns;
   b->np = np;
   b->nmu = nmu;
+  b->mu_one = cfg->with_mu_one ? 1 : 0;
   b->ntot = (long) ns * (spi ? np : nmu);
 
   sb = malloc(sizeof(double) * (ns + 1));

@@ -163,7 +163,11 @@ __device__ int ref_bin_box(const fcfcg_launch &L, double dx, double dy,
     const int nmu2 = L.nmu * L.nmu;
     int p = (d < DBL_EPSILON) ? 0
             : __double2int_rz(__dmul_rn(__ddiv_rn(dz2, d), (double) nmu2));
-    if (p >= nmu2 || p < 0) return -1;
+    if (p < 0) return -1;
+    if (p >= nmu2) {
+      if (!L.mu_one) return -1;
+      p = nmu2 - 1;
+    }
     /* mutab[p] = floor(sqrt(p)) (setup_cf.c:513-531) */
     int k = (int) sqrt((double) p);
     while (k * k > p) k--;
@@ -200,7 +204,11 @@ __device__ int ref_bin_survey(const fcfcg_launch &L, double x1, double y1,
     const int nmu2 = L.nmu * L.nmu;
     int p = (d < DBL_EPSILON) ? 0
             : __double2int_rz(__dmul_rn(__ddiv_rn(pi2, d), (double) nmu2));
-    if (p >= nmu2 || p < 0) return -1;
+    if (p < 0) return -1;
+    if (p >= nmu2) {
+      if (!L.mu_one) return -1;
+      p = nmu2 - 1;
+    }
     int k = (int) sqrt((double) p);
     while (k * k > p) k--;
     while ((k + 1) * (k + 1) <= p) k++;
@@ -568,7 +576,11 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
         unsigned sb = ftab_bin<GEOM == FCFCG_GEOM_SURVEY>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb,
                                                             s2, E, amb);
         if (!amb) {
-          if (sb == FCFCG_FTAB_BIN_MASK || qi >= L.nmu) return;
+          if (qi >= L.nmu) {
+            if (!L.mu_one) return;
+            qi = L.nmu - 1;
+          }
+          if (sb == FCFCG_FTAB_BIN_MASK) return;
           bin = (int) sb + qi * L.ns;
         }
       } else {
@@ -1347,6 +1359,7 @@ extern "C" int fcfcg_count_noalloc(const fcfcg_ctx *bins_ctx, int isauto,
   for (int k = 0; k < 3; k++) L.box[k] = b->box[k];
   L.ns = b->ns;
   L.nmu = b->nmu;
+  L.mu_one = b->mu_one;
   L.np = b->np;
   L.ntot = b->ntot;
   L.rs = (const uint16_t *) (base + o_rs);

@@ -849,6 +849,7 @@ static void launch_bins(const fcfcg_ctx *c, fcfcg_launch *L) {
   L->s2min = b->s.vmin;
   L->s2max = b->s.vmax;
   L->smin0 = b->s.min0;
+  L->mu_one = b->mu_one;
   if (b->bintype == FCFCG_BIN_SPI) {
     L->pmin = b->p.vmin;
     L->pmax = b->p.vmax;

@@ -121,7 +121,7 @@ static int write_bin(const fcfcg_bins *b, FILE *fp, int isauto, int withwt,
     return -1;
   int32_t spec[8];
   spec[0] = 1;                                  /* double precision */
-  spec[1] = 0;                                  /* mu = 1 excluded */
+  spec[1] = b->mu_one;                          /* WITH_MU_ONE build */
   spec[2] = (b->geometry == FCFCG_GEOM_BOX);    /* periodic */
   spec[3] = isauto ? 0 : 1;
   spec[4] = withwt ? 1 : 0;
@@ -239,27 +239,39 @@ int fcfcg_read_paircount(const fcfcg_ctx *c, const char *fname, int *isauto,
   int32_t spec[8] = {0};
   uint64_t ssz = (b->bintype == FCFCG_BIN_ISO ? 7 : 8) * sizeof(int32_t);
   if (get_rec(fp, spec, ssz)) goto done;
-  if (spec[0] != 1 || spec[2] != (b->geometry == FCFCG_GEOM_BOX) ||
-      spec[5] != b->bintype || spec[6] != b->ns)
+  /* spec[0] = 0: a SINGLE_PREC build wrote the box and the edges as float;
+   * spec[1] (WITH_MU_ONE) only draws a warning from FCFC
+   * (src/fcfc/2pt_box/read_res.c:270-300) */
+  if ((spec[0] != 0 && spec[0] != 1) ||
+      spec[2] != (b->geometry == FCFCG_GEOM_BOX) || spec[5] != b->bintype ||
+      spec[6] != b->ns)
     goto done;
   if (b->bintype == FCFCG_BIN_SMU && spec[7] != b->nmu) goto done;
   if (b->bintype == FCFCG_BIN_SPI && spec[7] != b->np) goto done;
   const int au = (spec[3] == 0), wt = (spec[4] == 1);
+  const int sp = (spec[0] == 0);
+  const size_t rsz = sp ? sizeof(float) : sizeof(double);
+  const double tol = sp ? 1e-5 : 1e-10;          /* FLOAT_TOL, DOUBLE_TOL */
   tmp = malloc(sizeof(double) * (b->ntot > 16 ? b->ntot : 16) +
                sizeof(double) * (b->ns + b->np + 8));
   if (!tmp) {
     rc = FCFCG_ERR_MEMORY;
     goto done;
   }
-  if (b->geometry == FCFCG_GEOM_BOX && get_rec(fp, tmp, 3 * sizeof(double)))
-    goto done;
-  if (get_rec(fp, tmp, (b->ns + 1) * sizeof(double))) goto done;
+  float *tf = (float *) tmp;
+  if (b->geometry == FCFCG_GEOM_BOX) {
+    if (get_rec(fp, tmp, 3 * rsz)) goto done;
+    for (int k = 0; k < 3; k++)
+      if (fabs((sp ? (double) tf[k] : tmp[k]) - b->box[k]) > tol) goto done;
+  }
+  if (get_rec(fp, tmp, (b->ns + 1) * rsz)) goto done;
   for (int i = 0; i <= b->ns; i++)
-    if (fabs(tmp[i] - b->sbin_raw[i]) > 1e-10) goto done;
+    if (fabs((sp ? (double) tf[i] : tmp[i]) - b->sbin_raw[i]) > tol) goto done;
   if (b->bintype == FCFCG_BIN_SPI) {
-    if (get_rec(fp, tmp, (b->np + 1) * sizeof(double))) goto done;
+    if (get_rec(fp, tmp, (b->np + 1) * rsz)) goto done;
     for (int i = 0; i <= b->np; i++)
-      if (fabs(tmp[i] - b->pbin_raw[i]) > 1e-10) goto done;
+      if (fabs((sp ? (double) tf[i] : tmp[i]) - b->pbin_raw[i]) > tol)
+        goto done;
   }
   uint64_t t2[2] = {0, 0};
   double w2[2] = {0, 0};

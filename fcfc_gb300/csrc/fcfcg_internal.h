@@ -58,6 +58,7 @@ typedef struct {
   double *sbin_raw, *pbin_raw;
   fcfcg_axis s;          /* s^2 (or s_perp^2) */
   fcfcg_axis p;          /* pi (box) or pi^2 (survey) */
+  int mu_one;            /* mu = 1 in the last mu bin (WITH_MU_ONE) */
 } fcfcg_bins;
 
 int fcfcg_bins_setup(const fcfcg_binning *cfg, fcfcg_bins *b, char *err,
@@ -132,6 +133,7 @@ typedef struct {
   const double *s2edge, *pedge;
   double s2min, s2max, pmin, pmax;
   int smin0, pmin0;
+  int mu_one;                  /* WITH_MU_ONE: clamp the mu bin, not drop */
   /* weights: fixed point with F fractional bits */
   int fixF;
   /* outputs */

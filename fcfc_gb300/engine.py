@@ -33,7 +33,8 @@ class PairCounter:
 
     def __init__(self, geometry="box", bintype=BIN_SMU, box=None, smin=0.0,
                  smax=None, ds=None, sedges=None, nmu=1, pmin=0.0, pmax=None,
-                 dpi=None, pedges=None, device=-1, host_only=False):
+                 dpi=None, pedges=None, device=-1, host_only=False,
+                 with_mu_one=False):
         lib = capi.load_library()
         self.lib = lib
         geom = GEOM_BOX if geometry in ("box", GEOM_BOX) else GEOM_SURVEY
@@ -42,7 +43,8 @@ class PairCounter:
         self._b, self._keep = capi.make_binning(
             geom, bintype, box=box, smin=smin, ds=ds if ds is not None else 1.0,
             smax=smax, sedges=sedges, nmu=nmu, pmin=pmin, pmax=pmax,
-            dpi=dpi if dpi is not None else 1.0, pedges=pedges)
+            dpi=dpi if dpi is not None else 1.0, pedges=pedges,
+            with_mu_one=with_mu_one)
         h = C.c_void_p()
         if host_only:
             rc = lib.fcfcg_create_host(C.byref(self._b), C.byref(h))

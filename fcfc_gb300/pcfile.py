@@ -61,16 +61,18 @@ def read_binary(path: str) -> PairCountFile:
     recs = _records(data, nl)
     spec = np.frombuffer(recs[0], np.int32)
     bintype = int(spec[5])
+    # box sizes and bin edges are `real`: float in a SINGLE_PREC build
+    real = np.float32 if spec[0] == 0 else np.float64
     k = 1
     box = None
     if spec[2]:
-        box = np.frombuffer(recs[k], np.float64).copy()
+        box = np.frombuffer(recs[k], real).astype(np.float64)
         k += 1
-    sbin = np.frombuffer(recs[k], np.float64).copy()
+    sbin = np.frombuffer(recs[k], real).astype(np.float64)
     k += 1
     pbin = None
     if bintype == 2:
-        pbin = np.frombuffer(recs[k], np.float64).copy()
+        pbin = np.frombuffer(recs[k], real).astype(np.float64)
         k += 1
     weighted = bool(spec[4])
     tr = np.frombuffer(recs[k], np.float64 if weighted else np.uint64).copy()

@@ -173,8 +173,10 @@ def read_bins_file(path):
 # --------------------------------------------------------------------------
 
 def run(conf: dict, geometry: str = "box", device: int = -1,
-        precision: int = capi.PREC_FP32_RECHECK, verbose: bool = False):
-    """Run one FCFC job.  Returns a dict with counts, xi, multipoles, wp."""
+        precision: int = capi.PREC_FP32_RECHECK, verbose: bool = False,
+        with_mu_one: bool = False):
+    """Run one FCFC job.  Returns a dict with counts, xi, multipoles, wp.
+    with_mu_one: behave as FCFC built with -DWITH_MU_ONE."""
     box = geometry == "box"
     files = _arr(conf, "CATALOG")
     ncat = len(files)
@@ -226,7 +228,7 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
             kw.update(pmin=float(conf["PI_BIN_MIN"]), pmax=float(conf["PI_BIN_MAX"]),
                       dpi=float(conf["PI_BIN_SIZE"]))
 
-    pc = PairCounter(**kw)
+    pc = PairCounter(with_mu_one=with_mu_one, **kw)
     # catalogues, loaded on first use
     loaded = {}
 
@@ -317,12 +319,15 @@ def main(argv=None):
     g.add_argument("--survey", action="store_true", help="FCFC_2PT keys")
     ap.add_argument("-c", "--conf", required=True)
     ap.add_argument("--fp64", action="store_true", help="all-FP64 GPU path")
+    ap.add_argument("--with-mu-one", action="store_true",
+                    help="mu = 1 in the last mu bin, as FCFC built with "
+                         "-DWITH_MU_ONE")
     ap.add_argument("-v", "--verbose", action="store_true")
     a = ap.parse_args(argv)
     conf = parse_conf(open(a.conf).read())
     run(conf, "survey" if a.survey else "box",
         precision=capi.PREC_FP64 if a.fp64 else capi.PREC_FP32_RECHECK,
-        verbose=a.verbose)
+        verbose=a.verbose, with_mu_one=a.with_mu_one)
     return 0
 
 

@@ -89,6 +89,9 @@ typedef struct {
   int np;                /* number of pi bins ((s_perp,pi) only) */
   double pmin, dpi;      /* PI_BIN_MIN, PI_BIN_SIZE (linear bins) */
   const double *pedges;  /* np+1 edges, or NULL */
+  int with_mu_one;       /* FCFC built with -DWITH_MU_ONE: mu = 1 counted in
+                            the last mu bin, not dropped
+                            (src/fcfc/2pt_box/metric_common.c:185-189) */
 } fcfcg_binning;
 
 /* Summary of the bin set-up cf_setup would produce. */

@@ -83,6 +83,7 @@ typedef struct {
   uint8_t *mutab;
   double bsize[3];              /* rescaled box */
   long ntot;
+  int mu_one;                   /* -DWITH_MU_ONE build */
 } fco_bins;
 
 /* ------------------------------------------------------------------------ */
@@ -336,6 +337,7 @@ fail:
 
 /* Accessors for ctypes. */
 double fco_bins_rescale(const fco_bins *b) { return b->rescale; }
+void fco_bins_set_mu_one(fco_bins *b, int on) { b->mu_one = on ? 1 : 0; }
 int fco_bins_tabtype(const fco_bins *b) { return b->tabtype; }
 long fco_bins_ntot(const fco_bins *b) { return b->ntot; }
 long fco_bins_nstab(const fco_bins *b) { return b->nstab; }
@@ -391,7 +393,12 @@ static inline long fco_bin_box(const fco_bins *b, double dx, double dy,
   if (b->bintype == FCO_BIN_SMU) {
     const int nmu2 = b->nmu * b->nmu;
     int p = (d < DBL_EPSILON) ? 0 : (int) ((dz2 / d) * nmu2);
-    if (p >= nmu2) return -1;    /* mu = 1 excluded (no WITH_MU_ONE) */
+    /* mu = 1 excluded, or with WITH_MU_ONE put in the last bin
+     * (src/fcfc/2pt_box/metric_common.c:185-189) */
+    if (p >= nmu2) {
+      if (!b->mu_one) return -1;
+      p = nmu2 - 1;
+    }
     mi = b->mutab[p];
   }
   int si = fco_lookup(b->stab, b->smin_i, b->ns, b->s2bin, d);
@@ -420,7 +427,10 @@ static inline long fco_bin_survey(const fco_bins *b, double x1, double y1,
     double pi2 = dd * dd / (s + t);
     const int nmu2 = b->nmu * b->nmu;
     int p = (d < DBL_EPSILON) ? 0 : (int) ((pi2 / d) * nmu2);
-    if (p >= nmu2) return -1;
+    if (p >= nmu2) {           /* src/fcfc/2pt/metric_common.c:209-214 */
+      if (!b->mu_one) return -1;
+      p = nmu2 - 1;
+    }
     long mi = b->mutab[p];
     int si = fco_lookup(b->stab, b->smin_i, b->ns, b->s2bin, d);
     return si + mi * b->ns;

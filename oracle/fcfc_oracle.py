@@ -55,6 +55,7 @@ def lib():
         L.fco_bins_new.argtypes = [C.c_int, C.c_int, C.c_int, D, D, C.c_int, dp,
                                    C.c_int, C.c_int, D, D, C.c_int, dp, dp]
         L.fco_bins_free.argtypes = [P]
+        L.fco_bins_set_mu_one.argtypes = [P, C.c_int]
         L.fco_bins_rescale.restype = D
         L.fco_bins_rescale.argtypes = [P]
         for f in ("fco_bins_tabtype",):
@@ -98,7 +99,7 @@ class Bins:
 
     def __init__(self, survey: bool, bintype: int, ns: int, smin=0.0, ds=1.0,
                  sedges=None, nmu=1, np_=0, pmin=0.0, dpi=1.0, pedges=None,
-                 box=None):
+                 box=None, with_mu_one=False):
         L = lib()
         self._keep = []
         se = None if sedges is None else np.ascontiguousarray(sedges, np.float64)
@@ -115,6 +116,7 @@ class Bins:
         if not h:
             raise ValueError("oracle bin set-up failed")
         self.h = h
+        L.fco_bins_set_mu_one(h, int(bool(with_mu_one)))
 
     def __del__(self):
         h = getattr(self, "h", None)

@@ -141,6 +141,37 @@ def survey_cases():
     return c
 
 
+def variant_cases():
+    """Cases for the compile-time variants of FCFC: WITH_MU_ONE (mu = 1 in
+    the last mu bin) and SINGLE_PREC (float coordinates: its pair-count file
+    format)."""
+    from fcfc_gb300 import synth
+    c = {}
+    # a lattice: many pairs along z, i.e. mu = 1 exactly
+    g = np.arange(0.0, 200.0, 12.5)
+    lat = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    x = np.concatenate([lat, synth.uniform_box(2000, 200.0, seed=51)])
+    c["box_smu_muone"] = dict(
+        box=[200.0], bintype=1, cats={"D": x}, pairs=["DD"],
+        cf=["DD / @@ - 1"], poles=[0, 2], nmu=10,
+        sbin=dict(smin=0, smax=50, ds=5), exe="FCFC_2PT_BOX_muone")
+    # survey: objects on common lines of sight (same RA, Dec)
+    kw = dict(ra=(120.0, 125.0), dec=(5.0, 10.0), zmu=0.45, zsig=0.05,
+              zr=(0.4, 0.5))
+    rd = synth.survey_radecz(1200, seed=52, **kw)
+    rd[600:, :2] = rd[:600, :2]          # pairs along the line of sight
+    xs = synth.radecz_to_xyz(rd)
+    c["survey_smu_muone"] = dict(
+        bintype=1, cats={"D": xs}, pairs=["DD"], cf=["DD"], poles=[0],
+        nmu=10, sbin=dict(smin=0, smax=40, ds=4), exe="FCFC_2PT_muone")
+    c["box_smu_sp"] = dict(
+        box=[200.0], bintype=1, cats={"D": synth.uniform_box(1500, 200.0,
+                                                            seed=53)},
+        pairs=["DD"], cf=["DD / @@ - 1"], nmu=10,
+        sbin=dict(smin=0, smax=50, ds=5), exe="FCFC_2PT_BOX_sp", fmt="%f")
+    return c
+
+
 def write_conf(case, tmp, exe_box):
     labels = list(case["cats"].keys())
     lines = []
@@ -150,7 +181,8 @@ def write_conf(case, tmp, exe_box):
         fn = os.path.join(tmp, lab + ".txt")
         np.savetxt(fn, a, fmt="%.17g")
         cats.append(fn)
-    fmt = ", ".join('"%s"' % " ".join(["%lf"] * case["cats"][l].shape[1])
+    tok = case.get("fmt", "%lf")    # a SINGLE_PREC build reads floats
+    fmt = ", ".join('"%s"' % " ".join([tok] * case["cats"][l].shape[1])
                     for l in labels)
     lines.append("CATALOG = [%s]" % ", ".join(cats))
     lines.append("CATALOG_LABEL = [%s]" % ", ".join(labels))
@@ -250,7 +282,9 @@ def run_case(name, case, exe):
             shutil.copy(os.path.join(tmp, "zcmv.txt"), os.path.join(out, "zcmv.txt"))
     for lab, a in case["cats"].items():
         np.save(os.path.join(out, lab + ".npy"), np.ascontiguousarray(a))
-    meta = {k: v for k, v in case.items() if k not in ("cats", "sfile", "ztab")}
+    meta = {k: v for k, v in case.items()
+            if k not in ("cats", "sfile", "ztab", "exe")}
+    meta["build"] = case.get("exe", os.path.basename(exe))
     if "ztab" in case:
         meta["zfile"] = "zcmv.txt"
     if orders:
@@ -271,6 +305,8 @@ def main(argv):
         allc[name] = (c, os.path.join(REF, "FCFC_2PT_BOX"))
     for name, c in survey_cases().items():
         allc[name] = (c, os.path.join(REF, "FCFC_2PT"))
+    for name, c in variant_cases().items():
+        allc[name] = (c, os.path.join(REF, c["exe"]))
     names = argv or sorted(allc)
     for n in names:
         run_case(n, *allc[n])

@@ -11,18 +11,23 @@ from fcfc_gb300 import pcfile
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
-def case_names(convert=None):
+def case_names(convert=None, single_prec=False):
     """Golden case names; convert=True / False keeps only the cases whose
-    catalogues are RA/Dec/z (COORD_CONVERT) / Cartesian."""
+    catalogues are RA/Dec/z (COORD_CONVERT) / Cartesian.  Cases written by a
+    SINGLE_PREC build of FCFC (float arithmetic: other counts, another file
+    layout) come only with single_prec=True (only them) or None (all)."""
     out = []
     for d in sorted(os.listdir(GOLDEN)):
         fn = os.path.join(GOLDEN, d, "meta.json")
         if not os.path.isfile(fn):
             continue
-        if convert is not None:
-            with open(fn) as f:
-                if bool(json.load(f).get("convert")) != convert:
-                    continue
+        with open(fn) as f:
+            m = json.load(f)
+        if convert is not None and bool(m.get("convert")) != convert:
+            continue
+        sp = m.get("build", "").endswith("_sp")
+        if single_prec is not None and sp != single_prec:
+            continue
         out.append(d)
     return out
 
@@ -73,7 +78,14 @@ class Case:
             kw.update(np_=n, pmin=p["pmin"], dpi=p["dpi"])
         if self.box:
             kw["box"] = (m["box"] * 3)[:3] if len(m["box"]) == 1 else m["box"]
+        if self.mu_one:
+            kw["with_mu_one"] = True
         return kw
+
+    @property
+    def mu_one(self):
+        """Written by a WITH_MU_ONE build (mu = 1 in the last mu bin)."""
+        return self.meta.get("build", "").endswith("_muone")
 
     @property
     def convert(self):

@@ -31,6 +31,8 @@ def host_counter(case):
     if case.box:
         args["box"] = case.meta["box"] * 3 if len(case.meta["box"]) == 1 \
             else case.meta["box"]
+    if kw.get("with_mu_one"):
+        args["with_mu_one"] = True
     return fg.PairCounter(**args)
 
 
@@ -135,3 +137,20 @@ def test_estimator_syntax():
     assert ev("DD / @@")[0] != 0          # no analytic RR given
     assert ev("DX")[0] != 0               # unknown label
     assert ev("DD +")[0] != 0
+
+
+@pytest.mark.parametrize("name", case_names(single_prec=True))
+def test_reads_single_precision_files(name):
+    """A pair-count file written by a SINGLE_PREC build of FCFC (float box
+    and bin edges) reads back, as FCFC's double build reads it
+    (src/fcfc/2pt_box/read_res.c:256-420)."""
+    case = Case(name)
+    pc = host_counter(case)
+    for pair in case.meta["pairs"]:
+        fn = os.path.join(case.dir, pair + ".bin")
+        r = pc.read_paircount(fn)
+        ref = case.pcfile(pair)
+        assert r["auto"] == (pair[0] == pair[1])
+        np.testing.assert_array_equal(r["cnt"], ref.cnt)
+        np.testing.assert_array_equal(r["ncnt"], ref.ncnt)
+        assert r["norm"] == ref.norm

@@ -34,6 +34,8 @@ def engine_for(case):
                     pmax=kw["pmin"] + kw["dpi"] * kw["np_"])
     if case.box:
         args["box"] = kw["box"]
+    if kw.get("with_mu_one"):
+        args["with_mu_one"] = True
     return fg.PairCounter(**args)
 
 

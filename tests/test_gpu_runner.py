@@ -88,7 +88,7 @@ def test_run_matches_upstream_outputs(name, tmp_path):
     from fcfc_gb300 import runner
     case = Case(name)
     conf = runner.parse_conf(open(_write_conf(case, str(tmp_path))).read())
-    runner.run(conf, "box" if case.box else "survey")
+    runner.run(conf, "box" if case.box else "survey", with_mu_one=case.mu_one)
     any_wt = False
     for pair in case.meta["pairs"]:
         want = open(os.path.join(case.dir, pair + ".bin"), "rb").read()
