@@ -22,7 +22,7 @@ import sys
 
 import numpy as np
 
-from . import capi
+from . import ascii, capi
 from .capi import BIN_SMU, BIN_SPI, FCFCGError
 from .engine import PairCounter
 
@@ -96,30 +96,22 @@ def _bool(x):
 # catalogues
 
 def read_catalog(path, formatter=None, position=("$1", "$2", "$3"),
-                 weight=None, skip=0, comment=None):
-    """ASCII catalogue with column indicators $n (or ${n}); .npy arrays are
-    read directly (columns x y z [w])."""
+                 weight=None, skip=0, comment=None, selection=None):
+    """A catalogue as FCFC reads it: ASCII with ASCII_FORMATTER, POSITION /
+    WEIGHT column expressions and SELECTION (see ascii.py); .npy arrays
+    (columns x y z [w]) are read directly."""
     if path.endswith(".npy"):
         a = np.load(path)
         w = a[:, 3] if (weight is not None and a.shape[1] > 3) else None
         return a[:, :3].astype(np.float64), w
-    cols = []
-    for p in list(position) + ([weight] if weight else []):
-        m = re.fullmatch(r"\$\{?(\d+)\}?", str(p).strip())
-        if not m:
-            raise FCFCGError(capi.ERR_CFG, "only column indicators $n are "
-                             "supported in POSITION/WEIGHT: %r" % p)
-        cols.append(int(m.group(1)) - 1)
-    if formatter:
-        # skipped columns (%*...) do not count
-        fmts = formatter.split()
-        kept = [i for i, f in enumerate(fmts) if not f.startswith("%*")]
-        cols = [kept[c] for c in cols]
-    data = np.loadtxt(path, comments=comment or None, skiprows=int(skip or 0),
-                      usecols=cols, ndmin=2)
-    x = np.ascontiguousarray(data[:, :3], np.float64)
-    w = np.ascontiguousarray(data[:, 3], np.float64) if weight else None
-    return x, w
+    if not formatter:
+        ncol = max(int(c) for c in re.findall(r"\$\{?(\d+)",
+                                              " ".join(list(position) +
+                                                       [weight or "",
+                                                        selection or ""])))
+        formatter = " ".join(["%lf"] * ncol)
+    return ascii.read_ascii(path, formatter, list(position), weight, selection,
+                            int(skip or 0), comment if comment else None)
 
 
 def read_ztable(path):
@@ -186,6 +178,7 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
     wts = _arr(conf, "WEIGHT", ncat)
     skip = _arr(conf, "ASCII_SKIP", ncat, default=[0] * ncat)
     cmt = _arr(conf, "ASCII_COMMENT", ncat)
+    sel = _arr(conf, "SELECTION", ncat)
     bintype = int(conf.get("BINNING_SCHEME", 0))
     pairs = _arr(conf, "PAIR_COUNT")
     pcout = _arr(conf, "PAIR_COUNT_FILE")
@@ -238,7 +231,9 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
             p3 = pos[3 * i: 3 * i + 3]
             w = wts[i] if wts and wts[i] not in (None, "", "''", '""') else None
             x, ww = read_catalog(files[i], fmtr[i] if fmtr else None, p3, w,
-                                 skip[i], cmt[i] if cmt else None)
+                                 skip[i], cmt[i] if cmt else None,
+                                 sel[i] if sel and sel[i] not in ("", "''", '""')
+                                 else None)
             if cnvt[i]:
                 pc.load_radecz(i, x, ww, **cosmo)
             else:

@@ -172,6 +172,73 @@ def variant_cases():
     return c
 
 
+def expr_case():
+    """Catalogue columns combined by POSITION / WEIGHT expressions and
+    filtered by SELECTION (numbers, an integer flag, a string tag)."""
+    from fcfc_gb300 import synth
+    rng = np.random.default_rng(61)
+    x = synth.uniform_box(4000, 300.0, seed=62)
+    w = synth.lognormal_weights(len(x), 0.3, seed=63)
+    flag = rng.integers(0, 3, len(x))
+    tag = rng.choice(["A", "B"], len(x))
+    lines = ["# x/2 y-1.5 z w1 w2 flag tag"]
+    for i in range(len(x)):
+        lines.append("%.17g %.17g %.17g %.17g %.17g %d %s" % (
+            x[i, 0] / 2, x[i, 1] - 1.5, x[i, 2], w[i], 1.0 / (1 + i % 7),
+            flag[i], tag[i]))
+    return dict(
+        box=[300.0], bintype=1, pairs=["DD"], cf=["DD / @@ - 1"], poles=[0, 2],
+        nmu=10, sbin=dict(smin=0, smax=40, ds=4),
+        text={"D": "\n".join(lines) + "\n"},
+        keys={"ASCII_FORMATTER": '"%lf %lf %lf %lf %lf %d %s"',
+              "ASCII_COMMENT": "['#']", "ASCII_SKIP": "[0]",
+              "POSITION": "[$1*2, ${2} + 1.5, $3]",
+              "WEIGHT": "[$4 * $5]",
+              "SELECTION": """'$6 >= 1 && ($7 == "A" || $5 > 0.3)'"""})
+
+
+def run_expr_case(name, case, exe):
+    out = os.path.join(HERE, name)
+    if os.path.isdir(out):
+        shutil.rmtree(out)
+    os.makedirs(out)
+    with tempfile.TemporaryDirectory() as tmp:
+        fn = os.path.join(tmp, "D.txt")
+        open(fn, "w").write(case["text"]["D"])
+        lines = ["CATALOG = [%s]" % fn, "CATALOG_LABEL = [D]",
+                 "BOX_SIZE = [%r]" % case["box"][0],
+                 "BINNING_SCHEME = %d" % case["bintype"],
+                 "PAIR_COUNT = [DD]",
+                 "PAIR_COUNT_FILE = [%s]" % os.path.join(tmp, "DD.bin"),
+                 "CF_ESTIMATOR = [\"%s\"]" % case["cf"][0],
+                 "CF_OUTPUT_FILE = [%s]" % os.path.join(tmp, "xi.txt"),
+                 "MULTIPOLE = [0, 2]",
+                 "MULTIPOLE_FILE = [%s]" % os.path.join(tmp, "mp.txt"),
+                 "SEP_BIN_MIN = 0", "SEP_BIN_MAX = 40", "SEP_BIN_SIZE = 4",
+                 "MU_BIN_NUM = 10", "OUTPUT_FORMAT = 0", "OVERWRITE = 2",
+                 "VERBOSE = F"]
+        lines += ["%s = %s" % kv for kv in case["keys"].items()]
+        conf = os.path.join(tmp, "run.conf")
+        open(conf, "w").write("\n".join(lines) + "\n")
+        env = dict(os.environ, OMP_NUM_THREADS="4")
+        subprocess.run([exe, "-c", conf], check=True, env=env,
+                       stdout=subprocess.DEVNULL)
+        for fnm in ("DD.bin", "xi.txt", "mp.txt"):
+            shutil.copy(os.path.join(tmp, fnm), os.path.join(out, fnm))
+    open(os.path.join(out, "D.txt"), "w").write(case["text"]["D"])
+    meta = {k: v for k, v in case.items() if k != "text"}
+    meta.update(labels=["D"], geometry="box", build=os.path.basename(exe),
+                catalog_text={"D": "D.txt"}, weighted={"D": True},
+                reader={"formatter": "%lf %lf %lf %lf %lf %d %s",
+                        "position": ["$1*2", "${2} + 1.5", "$3"],
+                        "weight": "$4 * $5",
+                        "selection": '$6 >= 1 && ($7 == "A" || $5 > 0.3)',
+                        "comment": "#"})
+    with open(os.path.join(out, "meta.json"), "w") as f:
+        json.dump(meta, f, indent=1, sort_keys=True)
+    print("wrote", name)
+
+
 def write_conf(case, tmp, exe_box):
     labels = list(case["cats"].keys())
     lines = []
@@ -307,9 +374,14 @@ def main(argv):
         allc[name] = (c, os.path.join(REF, "FCFC_2PT"))
     for name, c in variant_cases().items():
         allc[name] = (c, os.path.join(REF, c["exe"]))
-    names = argv or sorted(allc)
+    special = {"box_smu_expr": (expr_case, "FCFC_2PT_BOX")}
+    names = argv or sorted(list(allc) + list(special))
     for n in names:
-        run_case(n, *allc[n])
+        if n in special:
+            mk, exe = special[n]
+            run_expr_case(n, mk(), os.path.join(REF, exe))
+        else:
+            run_case(n, *allc[n])
 
 
 if __name__ == "__main__":

@@ -38,8 +38,20 @@ class Case:
         self.dir = os.path.join(GOLDEN, name)
         with open(os.path.join(self.dir, "meta.json")) as f:
             self.meta = json.load(f)
-        self.cats = {l: np.load(os.path.join(self.dir, l + ".npy"))
-                     for l in self.meta["labels"]}
+        if self.meta.get("catalog_text"):
+            # an ASCII catalogue read through FCFC's column expressions
+            from fcfc_gb300 import ascii
+            r = self.meta["reader"]
+            self.cats = {}
+            for l, fn in self.meta["catalog_text"].items():
+                xyz, w = ascii.read_ascii(os.path.join(self.dir, fn),
+                                          r["formatter"], r["position"],
+                                          r.get("weight"), r.get("selection"),
+                                          0, r.get("comment"))
+                self.cats[l] = xyz if w is None else np.c_[xyz, w]
+        else:
+            self.cats = {l: np.load(os.path.join(self.dir, l + ".npy"))
+                         for l in self.meta["labels"]}
         self.box = self.meta.get("geometry") == "box"
         self.sedges = None
         if self.meta.get("sfile"):

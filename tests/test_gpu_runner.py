@@ -22,7 +22,13 @@ def _write_conf(case, tmp):
     fmts = []
     pos = []
     wts = []
-    for lab in m["labels"]:
+    if m.get("catalog_text"):
+        # the catalogue file and FCFC's own reader keys, verbatim
+        lines.append("CATALOG = [%s]" % ", ".join(
+            os.path.join(case.dir, m["catalog_text"][l]) for l in m["labels"]))
+        lines.append("CATALOG_LABEL = [%s]" % ", ".join(m["labels"]))
+        lines += ["%s = %s" % kv for kv in m["keys"].items()]
+    for lab in ([] if m.get("catalog_text") else m["labels"]):
         a = case.cats[lab]
         fn = os.path.join(tmp, lab + ".txt")
         np.savetxt(fn, a, fmt="%.17g")
@@ -30,12 +36,13 @@ def _write_conf(case, tmp):
         fmts.append('"%s"' % " ".join(["%lf"] * a.shape[1]))
         pos += ["$1", "$2", "$3"]
         wts.append("$4" if a.shape[1] > 3 else "''")
-    lines.append("CATALOG = [%s]" % ", ".join(files))
-    lines.append("CATALOG_LABEL = [%s]" % ", ".join(m["labels"]))
-    lines.append("ASCII_FORMATTER = [%s]" % ", ".join(fmts))
-    lines.append("POSITION = [%s]" % ", ".join(pos))
-    if any(case.cats[l].shape[1] > 3 for l in m["labels"]):
-        lines.append("WEIGHT = [%s]" % ", ".join(wts))
+    if not m.get("catalog_text"):
+        lines.append("CATALOG = [%s]" % ", ".join(files))
+        lines.append("CATALOG_LABEL = [%s]" % ", ".join(m["labels"]))
+        lines.append("ASCII_FORMATTER = [%s]" % ", ".join(fmts))
+        lines.append("POSITION = [%s]" % ", ".join(pos))
+        if any(case.cats[l].shape[1] > 3 for l in m["labels"]):
+            lines.append("WEIGHT = [%s]" % ", ".join(wts))
     if case.box:
         lines.append("BOX_SIZE = [%s]" % ", ".join(repr(v) for v in m["box"]))
     if case.convert:
