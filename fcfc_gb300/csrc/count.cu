@@ -679,8 +679,10 @@ __device__ __forceinline__ uint32_t scan_chunk(const fcfcg_launch &L,
  * in-range pairs are then compacted into the warp queue and binned 32 at a
  * time, every lane busy.
  */
+/* (s, mu) binning keeps more values live: 3 CTAs per SM (85 registers)
+ * measure faster there, 4 CTAs (64 registers) for the other binnings. */
 template <int GEOM, int BIN, int WT, int BATCH, int ADJ>
-__global__ void __launch_bounds__(CT32_THREADS, 4)
+__global__ void __launch_bounds__(CT32_THREADS, BIN == FCFCG_BIN_SMU ? 3 : 4)
 k_count32(const fcfcg_launch L) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t sh_chunk;
@@ -933,11 +935,10 @@ k_count32(const fcfcg_launch L) {
         }
         __syncwarp();
         const uint32_t nr = (tot - r0 < QCAP) ? tot - r0 : QCAP;
-        /* pass k: lane l takes entry l * np + k, so that the lanes of a
-         * pass hold pairs of different neighbour points (different bins) */
+        /* pass k: lane l takes entry 32 k + l */
         const uint32_t np = (nr + 31) >> 5;
         for (uint32_t k = 0; k < np; k++) {
-          const uint32_t e = (uint32_t) lane * np + k;
+          const uint32_t e = k * 32u + (uint32_t) lane;
           if (e < nr)
             bin_pair<GEOM, BIN, WT, BATCH, ADJ>(L, &sh_mock, S, S.q[e], first,
                                                 cx, cy, cz, c2x, c2y, c2z, fs,
