@@ -57,7 +57,11 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OBJDIR, exist_ok=True)
     hdrs = [os.path.join(CSRC, h) for h in HEADERS]
     srcs = [os.path.join(CSRC, s) for s in CU_SOURCES + C_SOURCES]
-    if not force and _newer(LIB, srcs + hdrs + [__file__]):
+    drv = [os.path.join(CSRC, "driver", s) for s in DRIVER_SOURCES] + \
+        [os.path.join(CSRC, "driver", h) for h in ("catalog.h", "expr.h")]
+    bins = [os.path.join(BINDIR, n) for n in DRIVERS]
+    if not force and _newer(LIB, srcs + hdrs + [__file__]) and \
+            all(_newer(b, drv + [LIB]) for b in bins):
         return LIB
     jobs = []
     for s in CU_SOURCES:
@@ -81,7 +85,28 @@ def build(force: bool = False, verbose: bool = False) -> str:
     tmp = LIB + ".tmp%d" % os.getpid()
     _run([nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lm"])
     os.replace(tmp, LIB)
+    build_drivers()
     return LIB
+
+
+DRIVER_SOURCES = ["main.c", "catalog.c", "expr.c"]
+DRIVERS = {"FCFC_2PT_BOX_GPU": [], "FCFC_2PT_GPU": ["-DFCFCG_SURVEY"]}
+BINDIR = os.path.join(HERE, "bin")
+
+
+def build_drivers():
+    """The command line drivers (C, linked against libfcfcg.so)."""
+    os.makedirs(BINDIR, exist_ok=True)
+    src = [os.path.join(CSRC, "driver", s) for s in DRIVER_SOURCES]
+    jobs = []
+    for name, defs in DRIVERS.items():
+        out = os.path.join(BINDIR, name)
+        jobs.append(["gcc", "-O2", "-std=c11", "-ffp-contract=off",
+                     "-fno-fast-math", "-Wall", *defs, "-o", out, *src,
+                     "-L", LIBDIR, "-lfcfcg", "-Wl,-rpath,$ORIGIN/../lib",
+                     "-lm"])
+    with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        list(ex.map(_run, jobs))
 
 
 if __name__ == "__main__":

@@ -1,0 +1,521 @@
+/*
+ * main.c -- FCFC_2PT_BOX_GPU / FCFC_2PT_GPU: FCFC's command line run flow
+ * over the engine's C ABI.
+ *
+ * The flow of FCFC's main (src/fcfc/2pt_box/fcfc.c:19-82, survey
+ * src/fcfc/2pt/fcfc.c): read the configuration (load_conf.c), set up the
+ * bins (cf_setup), and for every entry of PAIR_COUNT read the catalogues
+ * (tree_create: ASCII reading, RA/Dec/z conversion for FCFC_2PT, rescaling
+ * on the device), count the pairs (count_pairs -> fcfcg_count), normalise
+ * and save them (eval_pairs, save_res) or read an existing pair-count file
+ * back (OVERWRITE <= 1, check_output); then evaluate CF_ESTIMATOR and write
+ * the correlation function, its multipoles or w_p (eval_cf).
+ *
+ * Built twice by fcfc_gb300/build.py: as FCFC_2PT_BOX_GPU and, with
+ * -DFCFCG_SURVEY, as FCFC_2PT_GPU.
+ *
+ *   FCFC_2PT_BOX_GPU -c fcfc_2pt_box.conf [--fp64] [--with-mu-one] [-v]
+ */
+#define _POSIX_C_SOURCE 200809L
+#include <ctype.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <sys/stat.h>
+
+#include "../../../include/fcfcg.h"
+#include "catalog.h"
+
+#ifdef FCFCG_SURVEY
+#define PROG "FCFC_2PT_GPU"
+#define GEOM FCFCG_GEOM_SURVEY
+#else
+#define PROG "FCFC_2PT_BOX_GPU"
+#define GEOM FCFCG_GEOM_BOX
+#endif
+
+#define MAXCAT 26
+
+/* ------------------------------------------------------------------------ */
+/* Configuration: KEY = value | [v1, v2, ...]; '#' comments outside quotes;  */
+/* a trailing '\' joins lines; values may be quoted with ' or ".            */
+
+typedef struct {
+  char *key;
+  int n;          /* number of values (1 for a scalar) */
+  char **v;
+} entry_t;
+
+typedef struct {
+  entry_t *e;
+  int n, cap;
+} conf_t;
+
+static void die(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  fprintf(stderr, "Error: ");
+  vfprintf(stderr, fmt, ap);
+  fprintf(stderr, "\n");
+  va_end(ap);
+  exit(1);
+}
+
+static char *trim(char *s) {
+  while (isspace((unsigned char) *s)) s++;
+  char *e = s + strlen(s);
+  while (e > s && isspace((unsigned char) e[-1])) *--e = '\0';
+  return s;
+}
+
+static char *unquote(char *s) {
+  s = trim(s);
+  size_t l = strlen(s);
+  if (l >= 2 && (s[0] == '"' || s[0] == '\'') && s[l - 1] == s[0]) {
+    s[l - 1] = '\0';
+    s++;
+  }
+  return s;
+}
+
+static char *strip_comment(char *s) {
+  char q = 0;
+  for (char *p = s; *p; p++) {
+    if (q) {
+      if (*p == q) q = 0;
+    } else if (*p == '"' || *p == '\'') {
+      q = *p;
+    } else if (*p == '#') {
+      *p = '\0';
+      break;
+    }
+  }
+  return s;
+}
+
+static void conf_add(conf_t *C, const char *key, char *val) {
+  if (C->n == C->cap) {
+    C->cap = C->cap ? 2 * C->cap : 32;
+    C->e = realloc(C->e, sizeof *C->e * C->cap);
+    if (!C->e) die("out of memory");
+  }
+  entry_t *E = C->e + C->n++;
+  E->key = strdup(key);
+  E->n = 0;
+  E->v = NULL;
+  val = trim(val);
+  if (*val == '[') {
+    char *end = strrchr(val, ']');
+    if (end) *end = '\0';
+    char *p = val + 1;
+    for (;;) {
+      /* split at commas outside quotes */
+      char q = 0, *s = p;
+      while (*p && (q || *p != ',')) {
+        if (q && *p == q) q = 0;
+        else if (!q && (*p == '"' || *p == '\'')) q = *p;
+        p++;
+      }
+      int last = (*p == '\0');
+      *p = '\0';
+      E->v = realloc(E->v, sizeof(char *) * (E->n + 1));
+      E->v[E->n++] = strdup(unquote(s));
+      if (last) break;
+      p++;
+    }
+    if (E->n == 1 && !*E->v[0]) E->n = 0;
+  } else {
+    E->v = malloc(sizeof(char *));
+    E->v[0] = strdup(unquote(val));
+    E->n = 1;
+  }
+}
+
+static void conf_read(conf_t *C, const char *fname) {
+  FILE *fp = fopen(fname, "r");
+  if (!fp) die("cannot open the configuration file `%s'", fname);
+  char *line = NULL, *acc = NULL;
+  size_t cap = 0, alen = 0;
+  while (getline(&line, &cap, fp) >= 0) {
+    char *l = strip_comment(line);
+    size_t len = strlen(l);
+    while (len && isspace((unsigned char) l[len - 1])) l[--len] = '\0';
+    int cont = (len && l[len - 1] == '\\');
+    if (cont) l[--len] = ' ';
+    acc = realloc(acc, alen + len + 2);
+    memcpy(acc + alen, l, len);
+    alen += len;
+    acc[alen] = '\0';
+    if (cont) continue;
+    char *eq = strchr(acc, '=');
+    if (eq) {
+      *eq = '\0';
+      char *k = trim(acc);
+      if (*k) conf_add(C, k, eq + 1);
+    }
+    alen = 0;
+  }
+  free(line);
+  free(acc);
+  fclose(fp);
+}
+
+static const entry_t *conf_get(const conf_t *C, const char *key) {
+  for (int i = C->n - 1; i >= 0; i--)
+    if (!strcmp(C->e[i].key, key)) return C->e + i;
+  return NULL;
+}
+
+/* the i-th value, a single value broadcast, or NULL */
+static const char *conf_str(const conf_t *C, const char *key, int i) {
+  const entry_t *E = conf_get(C, key);
+  if (!E || E->n == 0) return NULL;
+  if (E->n == 1) return E->v[0];
+  return (i < E->n) ? E->v[i] : NULL;
+}
+
+static int conf_len(const conf_t *C, const char *key) {
+  const entry_t *E = conf_get(C, key);
+  return E ? E->n : 0;
+}
+
+static double conf_dbl(const conf_t *C, const char *key, double def) {
+  const char *s = conf_str(C, key, 0);
+  if (!s || !*s) return def;
+  char *end;
+  double v = strtod(s, &end);
+  if (*trim(end)) die("invalid value of %s: `%s'", key, s);
+  return v;
+}
+
+static long conf_long(const conf_t *C, const char *key, int i, long def) {
+  const char *s = conf_str(C, key, i);
+  if (!s || !*s) return def;
+  return strtol(s, NULL, 10);
+}
+
+static int is_true(const char *s) {
+  return s && (s[0] == 'T' || s[0] == 't' || s[0] == '1' || s[0] == 'Y' ||
+               s[0] == 'y');
+}
+
+static int file_exists(const char *f) {
+  struct stat st;
+  return stat(f, &st) == 0;
+}
+
+/* ------------------------------------------------------------------------ */
+
+static void check(fcfcg_ctx *ctx, int rc, const char *what) {
+  if (rc)
+    die("%s: %s (%s)", what, fcfcg_strerror(rc),
+        ctx ? fcfcg_last_error(ctx) : "");
+}
+
+/* SEP_BIN_FILE / PI_BIN_FILE: (lower, upper) rows -> ns + 1 edges, a
+ * discontinuity of more than 1e-10 rejected (setup_cf.c:74-119) */
+static double *read_bins(const char *fname, int *nbin) {
+  double *lo, *hi;
+  size_t n;
+  char err[256];
+  if (cat_read_table(fname, &lo, &hi, &n, err, sizeof err) || n < 1)
+    die("cannot read the bin file `%s'", fname);
+  double *e = malloc(sizeof(double) * (n + 1));
+  e[0] = lo[0];
+  for (size_t i = 1; i < n; i++) {
+    if (fabs(lo[i] - hi[i - 1]) > 1e-10) die("discontinuous bins in `%s'", fname);
+    e[i] = (lo[i] == hi[i - 1]) ? lo[i] : 0.5 * (lo[i] + hi[i - 1]);
+  }
+  e[n] = hi[n - 1];
+  free(lo);
+  free(hi);
+  *nbin = (int) n;
+  return e;
+}
+
+int main(int argc, char **argv) {
+  const char *cfile = NULL;
+  int prec = FCFCG_PREC_FP32_RECHECK, mu_one = 0, verbose = 0;
+  for (int i = 1; i < argc; i++) {
+    if ((!strcmp(argv[i], "-c") || !strcmp(argv[i], "--conf")) && i + 1 < argc)
+      cfile = argv[++i];
+    else if (!strncmp(argv[i], "--conf=", 7))
+      cfile = argv[i] + 7;
+    else if (!strcmp(argv[i], "--fp64"))
+      prec = FCFCG_PREC_FP64;
+    else if (!strcmp(argv[i], "--with-mu-one"))
+      mu_one = 1;
+    else if (!strcmp(argv[i], "-v"))
+      verbose = 1;
+    else {
+      printf("Usage: %s -c CONFIG [--fp64] [--with-mu-one] [-v]\n"
+             "FCFC's configuration keys; the pairs are counted on the GPU.\n",
+             PROG);
+      return strcmp(argv[i], "-h") && strcmp(argv[i], "--help") ? 1 : 0;
+    }
+  }
+  if (!cfile) cfile = "fcfc.conf";
+  conf_t C = {0};
+  conf_read(&C, cfile);
+
+  /* catalogues */
+  const int ncat = conf_len(&C, "CATALOG");
+  if (ncat < 1 || ncat > MAXCAT) die("CATALOG must list 1 to 26 catalogues");
+  char label[MAXCAT];
+  for (int i = 0; i < ncat; i++) {
+    const char *l = conf_str(&C, "CATALOG_LABEL", i);
+    label[i] = (conf_len(&C, "CATALOG_LABEL") && l) ? l[0] : (char) ('A' + i);
+  }
+  for (int i = 0; i < ncat; i++) {
+    const char *t = conf_str(&C, "CATALOG_TYPE", i);
+    if (t && strtol(t, NULL, 10) != 0)
+      die("only ASCII catalogues (CATALOG_TYPE = 0) are supported");
+  }
+  if (conf_len(&C, "POSITION") != 3 * ncat)
+    die("POSITION needs 3 entries per catalogue");
+
+  /* bins */
+  fcfcg_binning b;
+  memset(&b, 0, sizeof b);
+  b.geometry = GEOM;
+  b.bintype = (int) conf_long(&C, "BINNING_SCHEME", 0, 0);
+  b.with_mu_one = mu_one;
+  double *sedges = NULL, *pedges = NULL;
+#ifndef FCFCG_SURVEY
+  {
+    int nb = conf_len(&C, "BOX_SIZE");
+    if (nb != 1 && nb != 3) die("BOX_SIZE needs 1 or 3 numbers");
+    for (int k = 0; k < 3; k++)
+      b.box[k] = strtod(conf_str(&C, "BOX_SIZE", nb == 1 ? 0 : k), NULL);
+  }
+#endif
+  if (conf_str(&C, "SEP_BIN_FILE", 0)) {
+    sedges = read_bins(conf_str(&C, "SEP_BIN_FILE", 0), &b.ns);
+    b.sedges = sedges;
+  } else {
+    b.smin = conf_dbl(&C, "SEP_BIN_MIN", 0);
+    b.ds = conf_dbl(&C, "SEP_BIN_SIZE", 0);
+    b.ns = fcfcg_linear_nbin(b.smin, conf_dbl(&C, "SEP_BIN_MAX", 0), b.ds);
+    if (b.ns < 1) die("invalid SEP_BIN_MIN / SEP_BIN_MAX / SEP_BIN_SIZE");
+  }
+  if (b.bintype == FCFCG_BIN_SMU) b.nmu = (int) conf_long(&C, "MU_BIN_NUM", 0, 0);
+  if (b.bintype == FCFCG_BIN_SPI) {
+    if (conf_str(&C, "PI_BIN_FILE", 0)) {
+      pedges = read_bins(conf_str(&C, "PI_BIN_FILE", 0), &b.np);
+      b.pedges = pedges;
+    } else {
+      b.pmin = conf_dbl(&C, "PI_BIN_MIN", 0);
+      b.dpi = conf_dbl(&C, "PI_BIN_SIZE", 0);
+      b.np = fcfcg_linear_nbin(b.pmin, conf_dbl(&C, "PI_BIN_MAX", 0), b.dpi);
+      if (b.np < 1) die("invalid PI_BIN_MIN / PI_BIN_MAX / PI_BIN_SIZE");
+    }
+  }
+  fcfcg_ctx *ctx = NULL;
+  int rc = fcfcg_create(&b, -1, &ctx);
+  check(ctx, rc, "bin set-up");
+  fcfcg_bins_info info;
+  check(ctx, fcfcg_bins_info_get(ctx, &info), "bin set-up");
+  const long ntot = (long) info.ntot;
+
+#ifdef FCFCG_SURVEY
+  /* coordinate conversion */
+  int cnvt[MAXCAT] = {0};
+  fcfcg_cosmo cosmo;
+  memset(&cosmo, 0, sizeof cosmo);
+  double *zs = NULL, *zd = NULL;
+  {
+    int nc = conf_len(&C, "COORD_CONVERT"), any = 0;
+    if (nc > 1 && nc < ncat) die("too few elements of COORD_CONVERT");
+    for (int i = 0; i < ncat && nc; i++)
+      any |= (cnvt[i] = is_true(conf_str(&C, "COORD_CONVERT", nc == 1 ? 0 : i)));
+    if (any) {
+      const char *zf = conf_str(&C, "Z_CMVDST_FILE", 0);
+      if (zf && *zf) {
+        char err[256];
+        size_t ns;
+        if (cat_read_table(zf, &zs, &zd, &ns, err, sizeof err)) die("%s", err);
+        cosmo.nsample = ns;
+        cosmo.z_sample = zs;
+        cosmo.d_sample = zd;
+      } else {
+        if (!conf_str(&C, "OMEGA_M", 0)) die("OMEGA_M is not set");
+        cosmo.omega_m = conf_dbl(&C, "OMEGA_M", 0);
+        if (conf_str(&C, "OMEGA_LAMBDA", 0)) {
+          cosmo.has_omega_l = 1;
+          cosmo.omega_l = conf_dbl(&C, "OMEGA_LAMBDA", 0);
+        }
+        cosmo.dew = conf_dbl(&C, "DE_EOS_W", 0);
+        cosmo.cmvdst_err = conf_dbl(&C, "CMVDST_ERR", 0);
+      }
+    }
+  }
+#endif
+
+  /* pairs and outputs */
+  const int npair = conf_len(&C, "PAIR_COUNT");
+  if (npair < 1) die("PAIR_COUNT is not set");
+  if (conf_len(&C, "PAIR_COUNT_FILE") < npair)
+    die("PAIR_COUNT_FILE needs one file per pair");
+  const int ofmt = (int) conf_long(&C, "OUTPUT_FORMAT", 0, 0);
+  const int ovw = (int) conf_long(&C, "OVERWRITE", 0, 0);
+  double *ncnt_all = calloc((size_t) npair * ntot, sizeof(double));
+  int64_t *icnt = malloc(sizeof(int64_t) * ntot);
+  double *wcnt = malloc(sizeof(double) * ntot);
+  double *tmp = malloc(sizeof(double) * ntot);
+  char labels[2 * 64 + 1];
+  int loaded[MAXCAT] = {0};
+  int weighted[MAXCAT];
+  for (int i = 0; i < ncat; i++) {
+    const char *w = conf_str(&C, "WEIGHT", i);
+    weighted[i] = (conf_len(&C, "WEIGHT") && w && *w);
+  }
+  if (npair > 64) die("too many pairs");
+  for (int k = 0; k < npair; k++) {
+    const char *pr = conf_str(&C, "PAIR_COUNT", k);
+    const char *fn = conf_str(&C, "PAIR_COUNT_FILE", k);
+    if (!pr || strlen(pr) != 2) die("invalid PAIR_COUNT entry `%s'", pr ? pr : "");
+    labels[2 * k] = pr[0];
+    labels[2 * k + 1] = pr[1];
+    int ia = -1, ib = -1;
+    for (int i = 0; i < ncat; i++) {
+      if (label[i] == pr[0]) ia = i;
+      if (label[i] == pr[1]) ib = i;
+    }
+    if (ia < 0 || ib < 0) die("unknown catalogue label in PAIR_COUNT `%s'", pr);
+    const int isauto = (ia == ib);
+    const int wt = weighted[ia] || weighted[ib];
+    if (file_exists(fn) && ovw <= 1) {
+      int au, ww;
+      uint64_t nt[2];
+      double wtr[2], norm;
+      check(ctx, fcfcg_read_paircount(ctx, fn, &au, &ww, nt, wtr, &norm,
+                                      ncnt_all + (size_t) k * ntot, icnt, wcnt),
+            "reading an existing pair-count file");
+      if (verbose) printf("read %s from `%s'\n", pr, fn);
+      continue;
+    }
+    const int need[2] = {ia, ib};
+    for (int q = 0; q < 2; q++) {
+      const int i = need[q];
+      if (loaded[i]) continue;
+      const char *pos[3] = {conf_str(&C, "POSITION", 3 * i),
+                            conf_str(&C, "POSITION", 3 * i + 1),
+                            conf_str(&C, "POSITION", 3 * i + 2)};
+      const char *fmtr = conf_str(&C, "ASCII_FORMATTER", i);
+      if (!fmtr || !*fmtr) die("ASCII_FORMATTER is not set for catalogue %c",
+                               label[i]);
+      const char *cm = conf_str(&C, "ASCII_COMMENT", i);
+      const char *sel = conf_str(&C, "SELECTION", i);
+      double *xyz[3], *w = NULL;
+      size_t n;
+      char err[512];
+      if (cat_read_ascii(conf_str(&C, "CATALOG", i), fmtr, pos,
+                         weighted[i] ? conf_str(&C, "WEIGHT", i) : NULL,
+                         (sel && *sel) ? sel : NULL,
+                         conf_long(&C, "ASCII_SKIP", i, 0),
+                         (cm && *cm) ? cm[0] : 0, xyz, &w, &n, err,
+                         sizeof err))
+        die("%s", err);
+#ifdef FCFCG_SURVEY
+      if (cnvt[i])
+        rc = fcfcg_load_catalog_radecz(ctx, i % 8, n, xyz[0], xyz[1], xyz[2],
+                                       w, &cosmo);
+      else
+#endif
+        rc = fcfcg_load_catalog(ctx, i % 8, n, xyz[0], xyz[1], xyz[2], w);
+      check(ctx, rc, "loading a catalogue");
+      free(xyz[0]);
+      free(xyz[1]);
+      free(xyz[2]);
+      free(w);
+      /* slots are per catalogue index modulo 8: drop what this evicts */
+      for (int j = 0; j < ncat; j++)
+        if (j != i && j % 8 == i % 8) loaded[j] = 0;
+      loaded[i] = 1;
+      if (verbose) printf("catalogue %c: %zu objects\n", label[i], n);
+    }
+    if (!loaded[ia] || !loaded[ib])
+      die("catalogues %c and %c share a slot: at most 8 catalogues per pair "
+          "set", label[ia], label[ib]);
+    const int sa = ia % 8, sb = ib % 8;
+    rc = fcfcg_count(ctx, sa, sb, isauto, wt, prec, icnt, wcnt);
+    check(ctx, rc, "counting pairs");
+    size_t na, nb;
+    double wa, wbs;
+    fcfcg_catalog_info(ctx, sa, &na, &wa);
+    fcfcg_catalog_info(ctx, sb, &nb, &wbs);
+    const double norm = wt ? fcfcg_norm(isauto, 1, wa, wbs)
+                           : fcfcg_norm(isauto, 0, (double) na, (double) nb);
+    double *nc = ncnt_all + (size_t) k * ntot;
+    for (long j = 0; j < ntot; j++) {
+      if (wt) {
+        if (isauto) wcnt[j] *= 2;
+        nc[j] = wcnt[j] / norm;
+      } else {
+        if (isauto) icnt[j] *= 2;
+        nc[j] = (double) icnt[j] / norm;
+      }
+    }
+    uint64_t ntr[2] = {na, nb};
+    double wtr[2] = {wa, wbs};
+    check(ctx, fcfcg_write_paircount(ctx, fn, ofmt, isauto, wt, ntr, wtr, norm,
+                                     nc, wt ? NULL : icnt, wt ? wcnt : NULL),
+          "writing a pair-count file");
+    if (verbose) {
+      fcfcg_stats st;
+      fcfcg_stats_get(ctx, &st);
+      printf("%s: %llu pairs in range, %.3f ms on the device\n", pr,
+             (unsigned long long) st.in_range, st.ms_total);
+    }
+  }
+
+  /* correlation functions */
+  const int nest = conf_len(&C, "CF_ESTIMATOR");
+  double *rr = NULL;
+#ifndef FCFCG_SURVEY
+  rr = malloc(sizeof(double) * ntot);
+  check(ctx, fcfcg_analytic_rr(ctx, rr), "analytic RR");
+#endif
+  const int npole = conf_len(&C, "MULTIPOLE");
+  int poles[16];
+  for (int j = 0; j < npole && j < 16; j++)
+    poles[j] = (int) strtol(conf_str(&C, "MULTIPOLE", j), NULL, 10);
+  const int dowp = is_true(conf_str(&C, "PROJECTED_CF", 0));
+  for (int e = 0; e < nest; e++) {
+    const char *ex = conf_str(&C, "CF_ESTIMATOR", e);
+    check(ctx, fcfcg_cf_eval(ex, npair, labels, ncnt_all, rr, ntot, tmp),
+          "CF_ESTIMATOR");
+    const char *cf = conf_str(&C, "CF_OUTPUT_FILE", e);
+    if (cf) check(ctx, fcfcg_write_cf(ctx, cf, tmp), "writing CF_OUTPUT_FILE");
+    if (npole > 0 && b.bintype == FCFCG_BIN_SMU) {
+      double *mp = malloc(sizeof(double) * npole * b.ns);
+      check(ctx, fcfcg_multipoles(ctx, tmp, npole, poles, mp), "multipoles");
+      const char *mf = conf_str(&C, "MULTIPOLE_FILE", e);
+      if (mf) check(ctx, fcfcg_write_multipoles(ctx, mf, npole, poles, mp),
+                    "writing MULTIPOLE_FILE");
+      free(mp);
+    } else if (dowp && b.bintype == FCFCG_BIN_SPI) {
+      double *wp = malloc(sizeof(double) * b.ns);
+      check(ctx, fcfcg_wp(ctx, tmp, wp), "w_p");
+      const char *wf = conf_str(&C, "PROJECTED_FILE", e);
+      if (wf) check(ctx, fcfcg_write_wp(ctx, wf, wp), "writing PROJECTED_FILE");
+      free(wp);
+    }
+  }
+  fcfcg_destroy(ctx);
+  free(rr);
+  free(ncnt_all);
+  free(icnt);
+  free(wcnt);
+  free(tmp);
+  free(sedges);
+  free(pedges);
+#ifdef FCFCG_SURVEY
+  free(zs);
+  free(zd);
+#endif
+  return 0;
+}
