@@ -525,7 +525,7 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
     int cy, int cz,
     float c2x, float c2y, float c2z, const uint16_t *fs, const uint16_t *fp,
     const float *fse, const float *fpe, uint32_t *h, uint32_t &n_in,
-    uint32_t &n_q, unsigned long long &n_inline) {
+    uint32_t &n_q, unsigned long long &n_inline, double &gbv) {
   const int i = (int) (ent & 63u), src = (int) (ent >> 6);
   const float4 pa = S.a[i];
   const float4 pb = S.b[src];
@@ -614,10 +614,11 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
   }
   n_in++;
   if (ADJ) {
-    /* d/dw_a of w_a w_b g[bin] is w_b g[bin], and the other way round */
+    /* d/dw_a of w_a w_b g[bin] is w_b g[bin], and the other way round; the
+     * neighbour side is summed across the warp by the caller */
     const double g = L.hist_smem ? ((const double *) h)[bin] : __ldg(L.gadj + bin);
     atomicAdd(S.ga + i, __dmul_rn(S.wb[src], g));
-    atomicAdd(S.gb + src, __dmul_rn(S.wa[i], g));
+    gbv = __dmul_rn(S.wa[i], g);
     return;
   }
   long long w = 0;
@@ -939,11 +940,30 @@ k_count32(const fcfcg_launch L) {
         const uint32_t np = (nr + 31) >> 5;
         for (uint32_t k = 0; k < np; k++) {
           const uint32_t e = k * 32u + (uint32_t) lane;
-          if (e < nr)
-            bin_pair<GEOM, BIN, WT, BATCH, ADJ>(L, &sh_mock, S, S.q[e], first,
+          double gbv = 0;
+          int key = -1;
+          if (e < nr) {
+            const uint32_t ent = S.q[e];
+            key = (int) (ent >> 6);
+            bin_pair<GEOM, BIN, WT, BATCH, ADJ>(L, &sh_mock, S, ent, first,
                                                 cx, cy, cz, c2x, c2y, c2z, fs,
                                                 fp, fse, fpe, h, n_in, n_q,
-                                                n_inline);
+                                                n_inline, gbv);
+          }
+          if (ADJ) {
+            /* the pass's entries run in neighbour order: sum each run of
+             * equal neighbours across the lanes (suffix sums within a run)
+             * and let the run's first lane add it -- the neighbour block is
+             * this warp's own, so no atomic is needed */
+            for (int o = 1; o < 32; o <<= 1) {
+              const double t = __shfl_down_sync(FULLMASK, gbv, o);
+              const int k2 = __shfl_down_sync(FULLMASK, key, o);
+              if (lane + o < 32 && k2 == key) gbv += t;
+            }
+            const int kp = __shfl_up_sync(FULLMASK, key, 1);
+            if (key >= 0 && (lane == 0 || kp != key)) S.gb[key] += gbv;
+            __syncwarp();
+          }
         }
         __syncwarp();
       }
