@@ -135,17 +135,38 @@ def fp32_peak_tflops(dev):
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
-def profile_traffic():
-    """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary, if there is one."""
+def profile_value(key):
+    """A figure of the committed ncu summary of the dominant kernel (DRAM
+    bytes per launch, warp instructions per in-range pair), if present."""
     p = os.path.join(ROOT, "profiles", "k_count32_box_smu_wt_ns_box.txt")
     try:
         for line in open(p):
-            if line.startswith("traffic_bytes_per_launch_full_workload:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":")[1])
     except OSError:
         pass
     return None
+
+
+def profile_traffic():
+    return profile_value("traffic_bytes_per_launch_full_workload")
+
+
+def issue_bound(pairs_per_s, clocks):
+    """The bound the count kernel actually meets: instruction issue.  Warp
+    instructions per in-range pair (ncu, committed summary) x pairs/s over
+    the issue rate of the GPU (SMs x 4 schedulers x the SM clock sampled
+    during the run)."""
+    ipp = profile_value("warp_instructions_per_in_range_pair")
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    if ipp is None:
+        return None
+    peak = 152 * 4 * mhz * 1e6
+    ach = pairs_per_s * ipp
+    return {"achieved": ach, "peak": peak, "unit": "warp instructions/s",
+            "frac": ach / peak, "warp_instructions_per_pair": ipp,
+            "source": "ncu instruction count of the small case x measured "
+                      "pairs/s; peak = 152 SMs x 4 issue slots x SM clock"}
 
 
 def max_over_ranks(value, dist):
@@ -769,7 +790,8 @@ def main():
                      "kernel": "k_count32<box,smu,weighted>",
                      "kernel_ms": k1_ms,
                      "peak_source": "measured cuBLAS SGEMM (TF32 off) on this GPU",
-                     "flops_per_pair": FLOPS_PER_PAIR["smu"]},
+                     "flops_per_pair": FLOPS_PER_PAIR["smu"],
+                     "issue": issue_bound(n_in[0] / (k1_ms * 1e-3), clocks)},
         "counters": {"candidates_smu": st1["candidates"],
                      "rechecked_smu": st1["rechecked"],
                      "candidates_spi": st2["candidates"],
