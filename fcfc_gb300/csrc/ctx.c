@@ -77,6 +77,7 @@ struct fcfcg_ctx {
   size_t d_mock_cap;
   uint32_t *d_mbase;
   size_t d_mbase_cap;
+  double *d_wpart;               /* weight-sum partials; [0] the sum */
   double *d_grad;                /* adjoint: sorted and input-order gradients */
   size_t d_grad_cap;
   unsigned long long *d_bout, *d_bstat;
@@ -180,7 +181,8 @@ void fcfcg_destroy(fcfcg_ctx *c) {
                  c->d_fp, c->d_rs, c->d_rp, c->d_s2edge, c->d_pedge,
                  c->d_sten, c->d_stenD, c->d_cnt, c->d_wt, c->d_stats,
                  c->d_bbox, c->d_wd, c->d_head, c->d_queue, c->d_cnvt,
-                 c->d_mock, c->d_mbase, c->d_bout, c->d_bstat, c->d_grad};
+                 c->d_mock, c->d_mbase, c->d_bout, c->d_bstat, c->d_grad,
+                 c->d_wpart};
     for (size_t i = 0; i < sizeof p / sizeof p[0]; i++)
       if (p[i]) cudaFree(p[i]);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
@@ -260,6 +262,8 @@ int fcfcg_create(const fcfcg_binning *cfg, int device, fcfcg_ctx **out) {
   CK(cudaMalloc((void **) &c->d_wt, sizeof(unsigned long long) * 2 * b->ntot));
   CK(cudaMalloc((void **) &c->d_wd, sizeof(double) * b->ntot));
   CK(cudaMalloc((void **) &c->d_stats, sizeof(unsigned long long) * 8));
+  CK(cudaMalloc((void **) &c->d_wpart,
+                sizeof(double) * (fcfcg_prep_partials() + 1)));
   CK(cudaMalloc((void **) &c->d_bbox, sizeof(unsigned long long) * 6));
   CK(cudaMalloc((void **) &c->d_head, sizeof(uint32_t) * 4));
   c->d_qcount = c->d_head + 1;
@@ -383,8 +387,9 @@ static int load_common(fcfcg_ctx *c, int slot, size_t n, const double *x,
   unsigned long long *wbits = c->d_stats + 7;
   CK(cudaMemsetAsync(wbits, 0, sizeof(unsigned long long), c->stream));
   CKK(fcfcg_k_prep(c->stream, n, ix, iy, iz, iw, c->bins.rescale, survey,
-                   s->x, s->y, s->z, s->s, s->w, wbits));
-  c->launches += n ? 2 : 0;
+                   s->x, s->y, s->z, s->s, s->w, wbits, c->d_wpart + 1,
+                   c->d_wpart));
+  c->launches += n ? (w ? 3 : 2) : 0;
   /* bounding box of the rescaled catalogue and max |w| */
   unsigned long long init[6] = {~0ull, ~0ull, ~0ull, 0, 0, 0};
   CK(cudaMemcpyAsync(c->d_bbox, init, sizeof init, cudaMemcpyHostToDevice,
@@ -395,6 +400,10 @@ static int load_common(fcfcg_ctx *c, int slot, size_t n, const double *x,
                      cudaMemcpyDeviceToHost, c->stream));
   CK(cudaMemcpyAsync(hb + 6, wbits, sizeof(unsigned long long),
                      cudaMemcpyDeviceToHost, c->stream));
+  double wsum = 0;
+  if (w && n)
+    CK(cudaMemcpyAsync(&wsum, c->d_wpart, sizeof(double),
+                       cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
   double mn[3], mx[3];
   for (int k = 0; k < 3; k++) {
@@ -437,28 +446,9 @@ static int load_common(fcfcg_ctx *c, int slot, size_t n, const double *x,
   }
   s->wexp = (s->wmax > 0) ? (int) ceil(log2(s->wmax)) : 0;
   if (ldexp(1.0, s->wexp) < s->wmax) s->wexp++;
-  /* sum of weights on the host, in input order (the reference sums with an
-   * OpenMP reduction whose order varies) */
-  if (w) {
-    double sum = 0;
-    if (on_device) {
-      double *hw = malloc(sizeof(double) * (n ? n : 1));
-      if (!hw) return FCFCG_ERR_MEMORY;
-      cudaError_t e = cudaMemcpy(hw, s->w, sizeof(double) * n,
-                                 cudaMemcpyDeviceToHost);
-      if (e) {
-        free(hw);
-        CK(e);
-      }
-      for (size_t i = 0; i < n; i++) sum += hw[i];
-      free(hw);
-    } else {
-      for (size_t i = 0; i < n; i++) sum += w[i];
-    }
-    s->sumw = sum;
-  } else {
-    s->sumw = (double) n;
-  }
+  /* the sum of the weights, summed on the device in a fixed order (FCFC
+   * sums with an OpenMP reduction, whose order varies with the threads) */
+  s->sumw = w ? wsum : (double) n;
   return FCFCG_OK;
 }
 
@@ -1364,19 +1354,21 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
   }
   S->n = N;
   S->has_w = withwt;
-  BGROW(c->d_bstat, c->d_bstat_cap, sizeof(unsigned long long) * 7 * na);
+  /* per catalogue: bounding box (6), max |w| bits, weight sum (double) */
+  BGROW(c->d_bstat, c->d_bstat_cap, sizeof(unsigned long long) * 8 * na);
   {
-    unsigned long long *init = malloc(sizeof(unsigned long long) * 7 * na);
+    unsigned long long *init = malloc(sizeof(unsigned long long) * 8 * na);
     if (!init) BFAIL(FCFCG_ERR_MEMORY);
     for (int a = 0; a < na; a++) {
       for (int k = 0; k < 3; k++) {
-        init[7 * a + k] = ~0ull;
-        init[7 * a + 3 + k] = 0;
+        init[8 * a + k] = ~0ull;
+        init[8 * a + 3 + k] = 0;
       }
-      init[7 * a + 6] = 0;
+      init[8 * a + 6] = 0;
+      init[8 * a + 7] = 0;
     }
     cudaError_t e = cudaMemcpy(c->d_bstat, init,
-                               sizeof(unsigned long long) * 7 * na,
+                               sizeof(unsigned long long) * 8 * na,
                                cudaMemcpyHostToDevice);
     free(init);
     BCK(e);
@@ -1403,17 +1395,18 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
     }
     BCKK(fcfcg_k_prep(c->stream, n, ix, iy, iz, iw, b->rescale, 0, S->x + o,
                       S->y + o, S->z + o, NULL, S->w + o,
-                      c->d_bstat + 7 * a + 6));
+                      c->d_bstat + 8 * a + 6, c->d_wpart,
+                      (double *) (c->d_bstat + 8 * a + 7)));
     BCKK(fcfcg_k_bbox(c->stream, n, S->x + o, S->y + o, S->z + o,
-                      c->d_bstat + 7 * a));
-    c->launches += 2;
+                      c->d_bstat + 8 * a));
+    c->launches += iw ? 3 : 2;
   }
   /* 2. per-catalogue range checks, weight scales and sums */
-  unsigned long long *hb = malloc(sizeof(unsigned long long) * 7 * na);
+  unsigned long long *hb = malloc(sizeof(unsigned long long) * 8 * na);
   if (!hb) BFAIL(FCFCG_ERR_MEMORY);
   {
     cudaError_t e = cudaMemcpyAsync(hb, c->d_bstat,
-                                    sizeof(unsigned long long) * 7 * na,
+                                    sizeof(unsigned long long) * 8 * na,
                                     cudaMemcpyDeviceToHost, c->stream);
     if (!e) e = cudaStreamSynchronize(c->stream);
     if (e) {
@@ -1422,8 +1415,6 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
     }
   }
   int *wexp = malloc(sizeof(int) * na);
-  double *hw = NULL;
-  size_t hwcap = 0;
   if (!wexp) {
     free(hb);
     BFAIL(FCFCG_ERR_MEMORY);
@@ -1431,7 +1422,7 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
   for (int a = 0; a < na; a++) {
     fcfcg_job *J = jobs + acc[a];
     for (int k = 0; k < 3; k++) {
-      unsigned long long lo = hb[7 * a + k], hi = hb[7 * a + 3 + k];
+      unsigned long long lo = hb[8 * a + k], hi = hb[8 * a + 3 + k];
       lo = (lo >> 63) ? (lo & 0x7FFFFFFFFFFFFFFFull) : ~lo;
       hi = (hi >> 63) ? (hi & 0x7FFFFFFFFFFFFFFFull) : ~hi;
       double mn, mx;
@@ -1442,44 +1433,16 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
         J->status = FCFCG_ERR_DATA;
     }
     double wmax = 1;
-    if (withwt) memcpy(&wmax, hb + 7 * a + 6, 8);
+    if (withwt) memcpy(&wmax, hb + 8 * a + 6, 8);
     if (!isfinite(wmax)) J->status = FCFCG_ERR_DATA;
     int we = (wmax > 0) ? (int) ceil(log2(wmax)) : 0;
     if (ldexp(1.0, we) < wmax) we++;
     wexp[a] = we;
     if (J->status) continue;
-    if (withwt) {
-      const double *wv = J->w;
-      if (on_device) {
-        if (hwcap < J->n) {
-          free(hw);
-          hw = malloc(sizeof(double) * J->n);
-          hwcap = hw ? J->n : 0;
-        }
-        if (!hw) {
-          free(hb);
-          free(wexp);
-          BFAIL(FCFCG_ERR_MEMORY);
-        }
-        cudaError_t e = cudaMemcpy(hw, J->w, sizeof(double) * J->n,
-                                   cudaMemcpyDeviceToHost);
-        if (e) {
-          free(hb);
-          free(wexp);
-          free(hw);
-          BCK(e);
-        }
-        wv = hw;
-      }
-      double sum = 0;
-      for (size_t i = 0; i < J->n; i++) sum += wv[i];
-      J->sumw = sum;
-    } else {
-      J->sumw = (double) J->n;
-    }
+    if (withwt) memcpy(&J->sumw, hb + 8 * a + 7, 8);
+    else J->sumw = (double) J->n;
   }
   free(hb);
-  free(hw);
   /* 3. grids: one refinement k for the batch, each catalogue's cells tile
    * its own box */
   grid_t gr;

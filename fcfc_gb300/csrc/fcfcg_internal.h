@@ -159,10 +159,13 @@ typedef struct {
 } fcfcg_launch;
 
 /* Launchers implemented in the .cu files; return 0 or a CUDA error code. */
+/* Rescale, |x|^2, max |w|; with w and wsum, also the sum of the weights in
+ * a fixed order (partial: fcfcg_prep_partials() doubles of scratch). */
 int fcfcg_k_prep(void *stream, size_t n, const double *x, const double *y,
     const double *z, const double *w, double rescale, int survey,
     double *ox, double *oy, double *oz, double *os, double *ow,
-    unsigned long long *wmax_bits);
+    unsigned long long *wmax_bits, double *partial, double *wsum);
+size_t fcfcg_prep_partials(void);
 int fcfcg_k_grid(void *stream, size_t n, const double *x, const double *y,
     const double *z, const double *s, const double *w, int has_w, int wexp,
     const int ncell[3], const double cw[3], const double lo[3],

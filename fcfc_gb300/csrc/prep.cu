@@ -34,8 +34,10 @@ __global__ void k_prep(size_t n, const double *__restrict__ x,
     const double *__restrict__ w, double rescale, int survey,
     double *__restrict__ ox, double *__restrict__ oy, double *__restrict__ oz,
     double *__restrict__ os, double *__restrict__ ow,
-    unsigned long long *wmax_bits) {
+    unsigned long long *wmax_bits, double *__restrict__ partial) {
+  __shared__ double sh_sum[PREP_THREADS];
   unsigned long long wm = 0;
+  double ws = 0;
   for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n;
        i += (size_t) gridDim.x * blockDim.x) {
     double a = x[i], b = y[i], c = z[i];
@@ -53,10 +55,23 @@ __global__ void k_prep(size_t n, const double *__restrict__ x,
     if (w) {
       double v = w[i];
       ow[i] = v;
+      ws = __dadd_rn(ws, v);
       unsigned long long bits =
           (unsigned long long) __double_as_longlong(fabs(v));
       wm = bits > wm ? bits : wm;
     }
+  }
+  if (w && partial) {
+    /* this block's weight sum, in a fixed order (deterministic) */
+    sh_sum[threadIdx.x] = ws;
+    __syncthreads();
+    for (int o = PREP_THREADS / 2; o > 0; o >>= 1) {
+      if ((int) threadIdx.x < o)
+        sh_sum[threadIdx.x] = __dadd_rn(sh_sum[threadIdx.x],
+                                        sh_sum[threadIdx.x + o]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sh_sum[0];
   }
   if (w) {
     for (int o = 16; o > 0; o >>= 1) {
@@ -67,14 +82,38 @@ __global__ void k_prep(size_t n, const double *__restrict__ x,
   }
 }
 
+/* Sum of the per-block partial sums, in a fixed order. */
+__global__ void k_sum_partials(int nb, const double *__restrict__ partial,
+    double *out) {
+  __shared__ double sh[PREP_THREADS];
+  double v = 0;
+  for (int i = threadIdx.x; i < nb; i += PREP_THREADS)
+    v = __dadd_rn(v, partial[i]);
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int o = PREP_THREADS / 2; o > 0; o >>= 1) {
+    if ((int) threadIdx.x < o)
+      sh[threadIdx.x] = __dadd_rn(sh[threadIdx.x], sh[threadIdx.x + o]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+extern "C" size_t fcfcg_prep_partials(void) { return 152 * 32; }
+
 extern "C" int fcfcg_k_prep(void *stream, size_t n, const double *x,
     const double *y, const double *z, const double *w, double rescale,
     int survey, double *ox, double *oy, double *oz, double *os, double *ow,
-    unsigned long long *wmax_bits) {
+    unsigned long long *wmax_bits, double *partial, double *wsum) {
   if (!n) return 0;
-  k_prep<<<grid_for(n, PREP_THREADS), PREP_THREADS, 0,
-           (cudaStream_t) stream>>>(n, x, y, z, w, rescale, survey, ox, oy,
-                                    oz, os, ow, wmax_bits);
+  const int nb = grid_for(n, PREP_THREADS);
+  k_prep<<<nb, PREP_THREADS, 0, (cudaStream_t) stream>>>(
+      n, x, y, z, w, rescale, survey, ox, oy, oz, os, ow, wmax_bits,
+      (w && wsum) ? partial : NULL);
+  cudaError_t e = cudaGetLastError();
+  if (e || !w || !wsum) return (int) e;
+  k_sum_partials<<<1, PREP_THREADS, 0, (cudaStream_t) stream>>>(nb, partial,
+                                                                 wsum);
   return (int) cudaGetLastError();
 }
 
