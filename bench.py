@@ -15,8 +15,8 @@ i < j), summed over both counts.
 
   value   -- FP32 + FP64-recheck path, catalogue already in HBM; a step is
              catalogue preparation (rescale, cell sort) plus both counts,
-             timed with CUDA events on the engine's stream; L2 is flushed
-             between steps.
+             timed whole with CUDA events (the device idle on both sides,
+             host round trips included); L2 is flushed between steps.
   e2e     -- the same step through the C ABI from pinned host buffers: the
              host-to-device copy of the catalogue and the read-back of the
              counts are inside the timed region.
@@ -703,15 +703,25 @@ def main():
         dist.barrier()
     clk = ClockSampler(local)
     clk.start()
-    ms_tot, ms_k1, ms_k2 = 0.0, 0.0, 0.0
+    # A step is timed whole: CUDA events on the current stream around it,
+    # with the device idle on both sides.  The engine works on its own
+    # streams and returns only when its work is done, so the interval holds
+    # the preparation, both counts and every host round trip between them.
+    ms_tot, ms_dev, ms_k1, ms_k2 = 0.0, 0.0, 0.0, 0.0
     launches0 = p1.stats()["launches"] + p2.stats()["launches"]
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     t_wall0 = time.perf_counter()
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
+        e0.record()
         ms, res = step()
-        ms_tot += ms
+        e1.record()
+        torch.cuda.synchronize()
+        ms_tot += e0.elapsed_time(e1)
+        ms_dev += ms
         ms_k1 += res[0][1]["ms_count"]
         ms_k2 += res[1][1]["ms_count"]
     torch.cuda.synchronize()
@@ -724,8 +734,13 @@ def main():
     ms_step = max_over_ranks(ms_tot / args.steps, dist)
     value = pairs_per_step * world / (ms_step * 1e-3)
 
-    # all-FP64 GPU path, one step
-    ms64, _ = step(prec=fg.PREC_FP64)
+    # all-FP64 GPU path, one step, timed the same way
+    torch.cuda.synchronize()
+    e0.record()
+    step(prec=fg.PREC_FP64)
+    e1.record()
+    torch.cuda.synchronize()
+    ms64 = e0.elapsed_time(e1)
     fp64_value = pairs_per_step / (ms64 * 1e-3)
 
     # end to end through the C ABI from pinned host memory
@@ -797,6 +812,7 @@ def main():
                      "candidates_spi": st2["candidates"],
                      "rechecked_spi": st2["rechecked"],
                      "wall_ms_per_step": wall / args.steps * 1e3,
+                     "engine_device_ms_per_step": ms_dev / args.steps,
                      "kernel_ms_smu": ms_k1 / args.steps,
                      "kernel_ms_spi": ms_k2 / args.steps},
         "clocks": clocks,
