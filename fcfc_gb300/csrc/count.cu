@@ -380,7 +380,7 @@ __device__ __forceinline__ int first_j(const WarpChunk &w, bool self,
 struct MockSh {
   int nc[3];
   uint32_t base;
-  double cw[3];
+  float cwf[3], cwl[3];  /* cell widths: float + float residual */
   double box[3];
   unsigned long long *g;     /* gcnt, or gwt when weighted */
   uint32_t id;
@@ -774,7 +774,9 @@ k_count32(const fcfcg_launch L) {
           const fcfcg_mock *M = L.mocks + mk;
           for (int k = 0; k < 3; k++) {
             sh_mock.nc[k] = M->ncell[k];
-            sh_mock.cw[k] = M->cw[k];
+            const float f = (float) M->cw[k];
+            sh_mock.cwf[k] = f;
+            sh_mock.cwl[k] = (float) (M->cw[k] - (double) f);
             sh_mock.box[k] = M->box[k];
           }
           sh_mock.base = M->cell_base;
@@ -872,13 +874,18 @@ k_count32(const fcfcg_launch L) {
         const float4 pb = Bl4[bj];
         float4 D;
         if (BATCH) {
-          /* -offset * cell width of this catalogue, rounded as the stencil
-           * table of a single catalogue is */
+          /* -offset * cell width of this catalogue, rounded once: the width
+           * is held as a float plus its float residual, and the fused
+           * multiply-add rounds (-o) (cwf + cwl) a single time, as the
+           * single-catalogue stencil table is rounded (no FP64 needed) */
           const int4 o = __ldg(sten + t);
-          D = make_float4(__double2float_rn((double) (-o.x) * sh_mock.cw[0]),
-                          __double2float_rn((double) (-o.y) * sh_mock.cw[1]),
-                          __double2float_rn((double) (-o.z) * sh_mock.cw[2]),
-                          0.f);
+          const float ox = (float) (-o.x), oy = (float) (-o.y),
+                      oz = (float) (-o.z);
+          D = make_float4(
+              __fmaf_rn(ox, sh_mock.cwf[0], __fmul_rn(ox, sh_mock.cwl[0])),
+              __fmaf_rn(oy, sh_mock.cwf[1], __fmul_rn(oy, sh_mock.cwl[1])),
+              __fmaf_rn(oz, sh_mock.cwf[2], __fmul_rn(oz, sh_mock.cwl[2])),
+              0.f);
         } else {
           D = __ldg(stD + t);
         }
