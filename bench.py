@@ -590,7 +590,7 @@ def run_adjoint(args, rank, world, local, dist):
         "value": pairs_grad * world / (ms_b * 1e-3), "unit": UNIT,
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_b, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32+f64-recheck bins, f64 gradients",
+        "vs_baseline": None, "dtype": "f32+f64-recheck bins, f64-rounded products summed as int64",
         "data": "synthetic",
         "config": {"workload": "adjoint_ls_%dx%d" % (nd, nr), "n_data": nd,
                    "n_random": nr, "bins": "(s,mu) 40x100 s<200",

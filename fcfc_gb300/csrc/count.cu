@@ -418,6 +418,37 @@ __device__ __forceinline__ void enqueue(const fcfcg_launch &L,
   hist_add<WT, BATCH>(L, ms, h, bin, WT ? fix_prod_pair(L, a, b) : 0);
 }
 
+/*
+ * Adjoint terms of the FP32 kernel as integers.  With g' = g 2^S the scaled
+ * cotangent (|w g'| <= 2^50 for every weight), one fused multiply-add onto
+ * 1.5 2^52 rounds the exact product w g' to the nearest integer, which is
+ * then the low bits of the result (the classic magic-number conversion).
+ * Sums of these integers are exact; they convert back with 2^-S.
+ */
+#define ADJ_MAGIC 6755399441055744.0         /* 1.5 * 2^52 */
+#define ADJ_MAGIC_BITS 0x4338000000000000ll
+#define ADJ_SPILL (1ll << 61)
+
+__device__ __forceinline__ long long adj_term(double w, double g) {
+  return __double_as_longlong(__fma_rn(w, g, ADJ_MAGIC)) - ADJ_MAGIC_BITS;
+}
+
+/* Add a term to a chunk point's 64-bit accumulator.  The thread whose add
+ * carries it across +-2^61 moves 2^61 to the point's FP64 gradient (an
+ * exact transfer), so with terms below 2^51 the accumulator cannot wrap. */
+__device__ __forceinline__ void adj_acc(unsigned long long *acc, long long v,
+    double *dst, double unit) {
+  const long long old = (long long) atomicAdd(acc, (unsigned long long) v);
+  const long long nw = old + v;
+  if (nw >= ADJ_SPILL && old < ADJ_SPILL) {
+    atomicAdd(acc, (unsigned long long) (-ADJ_SPILL));
+    atomicAdd(dst, (double) ADJ_SPILL * unit);
+  } else if (nw <= -ADJ_SPILL && old > -ADJ_SPILL) {
+    atomicAdd(acc, (unsigned long long) ADJ_SPILL);
+    atomicAdd(dst, -(double) ADJ_SPILL * unit);
+  }
+}
+
 /* Adjoint: FP64 gradient contributions of one pair with a known bin. */
 __device__ __forceinline__ void adj_pair(const fcfcg_launch &L, uint32_t a,
     uint32_t b, int bin) {
@@ -476,9 +507,11 @@ struct Stage {
   float4 *bw;       /* per warp, 32: weight, integer weight, remainder */
   uint16_t *bt;     /* per warp, 32: stencil entry */
   uint16_t *q;      /* per warp, QCAP: queued pairs */
-  /* adjoint only */
-  double *ga, *wa;  /* FCHUNK: gradient accumulators, FP64 weights */
-  double *gb, *wb;  /* per warp, 32: the same for the neighbour points */
+  /* adjoint only: gradient sums in units of 2^-S, FP64 weights */
+  unsigned long long *ga;   /* FCHUNK */
+  double *wa;               /* FCHUNK */
+  long long *gb;            /* per warp, 32: the neighbour points */
+  double *wb;               /* per warp, 32 */
 };
 
 /* wt: 0 unweighted, 1 weighted, 2 adjoint (weighted + FP64 gradients) */
@@ -525,7 +558,7 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
     int cy, int cz,
     float c2x, float c2y, float c2z, const uint16_t *fs, const uint16_t *fp,
     const float *fse, const float *fpe, uint32_t *h, uint32_t &n_in,
-    uint32_t &n_q, unsigned long long &n_inline, double &gbv) {
+    uint32_t &n_q, unsigned long long &n_inline, long long &gbv) {
   const int i = (int) (ent & 63u), src = (int) (ent >> 6);
   const float4 pa = S.a[i];
   const float4 pb = S.b[src];
@@ -616,9 +649,9 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
   if (ADJ) {
     /* d/dw_a of w_a w_b g[bin] is w_b g[bin], and the other way round; the
      * neighbour side is summed across the warp by the caller */
-    const double g = L.hist_smem ? ((const double *) h)[bin] : __ldg(L.gadj + bin);
-    atomicAdd(S.ga + i, __dmul_rn(S.wb[src], g));
-    gbv = __dmul_rn(S.wa[i], g);
+    const double g = L.hist_smem ? ((const double *) h)[bin] : __ldg(L.gfix + bin);
+    adj_acc(S.ga + i, adj_term(S.wb[src], g), L.dA + ai, L.gunit);
+    gbv = adj_term(S.wa[i], g);
     return;
   }
   long long w = 0;
@@ -711,7 +744,7 @@ k_count32(const fcfcg_launch L) {
     S.bst = (uint32_t *) b;
     b += (((size_t) L.nsten) * 4 + 15) & ~(size_t) 15;
     if (ADJ) {
-      S.ga = (double *) b;
+      S.ga = (unsigned long long *) b;
       b += (size_t) FCHUNK * 8;
       S.wa = (double *) b;
       b += (size_t) FCHUNK * 8;
@@ -726,7 +759,7 @@ k_count32(const fcfcg_launch L) {
     S.q = (uint16_t *) b;
     if (ADJ) {
       b += QCAP * 2;
-      S.gb = (double *) b;
+      S.gb = (long long *) b;
       b += 32 * 8;
       S.wb = (double *) b;
     }
@@ -740,7 +773,7 @@ k_count32(const fcfcg_launch L) {
     /* the cotangent of the counts takes the histogram's place */
     if (L.hist_smem)
       for (long i = threadIdx.x; i < L.ntot; i += blockDim.x)
-        ((double *) h)[i] = L.gadj[i];
+        ((double *) h)[i] = L.gfix[i];
     for (int i = threadIdx.x; i < FCHUNK; i += blockDim.x) S.ga[i] = 0;
     if (lane < 32) S.gb[lane] = 0;
   } else if (L.hist_smem) {
@@ -947,7 +980,7 @@ k_count32(const fcfcg_launch L) {
         const uint32_t np = (nr + 31) >> 5;
         for (uint32_t k = 0; k < np; k++) {
           const uint32_t e = k * 32u + (uint32_t) lane;
-          double gbv = 0;
+          long long gbv = 0;
           int key = -1;
           if (e < nr) {
             const uint32_t ent = S.q[e];
@@ -963,7 +996,7 @@ k_count32(const fcfcg_launch L) {
              * and let the run's first lane add it -- the neighbour block is
              * this warp's own, so no atomic is needed */
             for (int o = 1; o < 32; o <<= 1) {
-              const double t = __shfl_down_sync(FULLMASK, gbv, o);
+              const long long t = __shfl_down_sync(FULLMASK, gbv, o);
               const int k2 = __shfl_down_sync(FULLMASK, key, o);
               if (lane + o < 32 && k2 == key) gbv += t;
             }
@@ -977,8 +1010,8 @@ k_count32(const fcfcg_launch L) {
       if (ADJ) {
         /* the block's neighbour points are done: their gradients out */
         if (p < total) {
-          const double v = S.gb[lane];
-          if (v != 0.0) atomicAdd(L.dB + bjl, v);
+          const long long v = S.gb[lane];
+          if (v != 0) atomicAdd(L.dB + bjl, (double) v * L.gunit);
           S.gb[lane] = 0;
         }
         __syncwarp();
@@ -988,8 +1021,8 @@ k_count32(const fcfcg_launch L) {
       /* the chunk is done: its points' gradients out */
       __syncthreads();
       for (int k = threadIdx.x; k < m; k += blockDim.x) {
-        const double v = S.ga[k];
-        if (v != 0.0) atomicAdd(L.dA + first + k, v);
+        const long long v = (long long) S.ga[k];
+        if (v != 0) atomicAdd(L.dA + first + k, (double) v * L.gunit);
         S.ga[k] = 0;
       }
     }

@@ -53,6 +53,7 @@ struct fcfcg_ctx {
   float *d_stenD;
   unsigned long long *d_cnt, *d_wt, *d_stats, *d_bbox;
   double *d_wd;
+  double *d_gfix;                /* adjoint: the scaled cotangent */
   uint32_t *d_head, *d_qcount, *d_queue;
   size_t qcap;
   void *h_pinned;
@@ -180,7 +181,7 @@ void fcfcg_destroy(fcfcg_ctx *c) {
                  c->d_fpe, c->d_fs,
                  c->d_fp, c->d_rs, c->d_rp, c->d_s2edge, c->d_pedge,
                  c->d_sten, c->d_stenD, c->d_cnt, c->d_wt, c->d_stats,
-                 c->d_bbox, c->d_wd, c->d_head, c->d_queue, c->d_cnvt,
+                 c->d_bbox, c->d_wd, c->d_gfix, c->d_head, c->d_queue, c->d_cnvt,
                  c->d_mock, c->d_mbase, c->d_bout, c->d_bstat, c->d_grad,
                  c->d_wpart};
     for (size_t i = 0; i < sizeof p / sizeof p[0]; i++)
@@ -261,6 +262,7 @@ int fcfcg_create(const fcfcg_binning *cfg, int device, fcfcg_ctx **out) {
   CK(cudaMalloc((void **) &c->d_cnt, sizeof(unsigned long long) * b->ntot));
   CK(cudaMalloc((void **) &c->d_wt, sizeof(unsigned long long) * 2 * b->ntot));
   CK(cudaMalloc((void **) &c->d_wd, sizeof(double) * b->ntot));
+  CK(cudaMalloc((void **) &c->d_gfix, sizeof(double) * b->ntot));
   CK(cudaMalloc((void **) &c->d_stats, sizeof(unsigned long long) * 8));
   CK(cudaMalloc((void **) &c->d_wpart,
                 sizeof(double) * (fcfcg_prep_partials() + 1)));
@@ -1010,6 +1012,41 @@ static int count_impl(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
     CK(cudaMemcpyAsync(c->d_wd, adj->g, sizeof(double) * b->ntot,
                        cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemsetAsync(c->d_grad, 0, sizeof(double) * ng, c->stream));
+    double gmax = 0;
+    for (size_t k = 0; k < (size_t) b->ntot; k++) {
+      if (!isfinite(adj->g[k])) {
+        set_err(c, "non-finite cotangent");
+        return FCFCG_ERR_ARG;
+      }
+      if (fabs(adj->g[k]) > gmax) gmax = fabs(adj->g[k]);
+    }
+    if (prec == FCFCG_PREC_FP32_RECHECK) {
+      /* unit of the integer gradient sums: 2^-S with |w| |g| 2^S <= 2^50
+       * for every weight and cotangent entry */
+      int gexp = 0;
+      if (gmax > 0) {
+        gexp = (int) ceil(log2(gmax));
+        if (ldexp(1.0, gexp) < gmax) gexp++;
+      }
+      const int wexp = A->wexp > B->wexp ? A->wexp : B->wexp;
+      int S = 50 - wexp - gexp;
+      if (S < -1000) {
+        set_err(c, "weights times cotangent out of range");
+        return FCFCG_ERR_ARG;
+      }
+      if (S > 1000) S = 1000;   /* products stay below 2^50 */
+      double *gf = malloc(sizeof(double) * b->ntot);
+      if (!gf) return FCFCG_ERR_MEMORY;
+      for (size_t k = 0; k < (size_t) b->ntot; k++)
+        gf[k] = ldexp(adj->g[k], S);
+      cudaError_t ce = cudaMemcpyAsync(c->d_gfix, gf,
+          sizeof(double) * b->ntot, cudaMemcpyHostToDevice, c->stream);
+      if (ce == cudaSuccess) ce = cudaStreamSynchronize(c->stream);
+      free(gf);
+      CK(ce);
+      L.gfix = c->d_gfix;
+      L.gunit = ldexp(1.0, -S);
+    }
   }
 
   /* work chunks: 64 points per CTA in the FP32 kernel, 32 per warp in the

@@ -156,6 +156,11 @@ typedef struct {
   int adjoint;
   const double *gadj;
   double *dA, *dB;
+  /* the FP32 kernel's integer accumulation: gfix[k] = gadj[k] 2^S with S
+   * chosen so that every |w g 2^S| <= 2^50; a product w gfix rounds to an
+   * int64 and integer sums convert back with gunit = 2^-S */
+  const double *gfix;
+  double gunit;
 } fcfcg_launch;
 
 /* Launchers implemented in the .cu files; return 0 or a CUDA error code. */

@@ -291,9 +291,15 @@ int fcfcg_count(fcfcg_ctx *ctx, int slot_a, int slot_b, int isauto,
  * n_a entries) and, for a cross count, dw_b likewise over catalogue b (may
  * be NULL).  For auto counts every unordered pair feeds both of its points.
  * The pair bins are recomputed, exactly as the count bins them (FP32 windows
- * with the FP64 recheck); the gradients are FP64 sums.  Catalogues without
- * weights count as unit weights.  Where the count falls back to the
- * all-FP64 kernel (FP32 windows too wide), so does the adjoint.
+ * with the FP64 recheck).  Each product w_j g[b] is rounded once (one
+ * FP64 fused multiply-add) to an integer multiple of 2^-S, where S makes
+ * max|w| max|g| 2^S <= 2^50; those integers are summed exactly (64-bit,
+ * with exact spills to FP64), so every gradient is within
+ * n 2^-49 max|w| max|g| (plus the rounding of the final FP64 additions) of
+ * the exact sum of its n products.  Catalogues
+ * without weights count as unit weights.  Where the count falls back to the
+ * all-FP64 kernel (FP32 windows too wide), so does the adjoint, which then
+ * sums in FP64.  A non-finite g entry fails with FCFCG_ERR_ARG.
  */
 int fcfcg_adjoint(fcfcg_ctx *ctx, int slot_a, int slot_b, int isauto,
     const double *g, double *dw_a, double *dw_b);
