@@ -80,6 +80,13 @@ class Job(C.Structure):
                 ("sumw", C.c_double), ("status", C.c_int)]
 
 
+class CountItem(C.Structure):
+    """fcfcg_count_item: one count of a count graph."""
+    _fields_ = [("slot_a", C.c_int), ("slot_b", C.c_int),
+                ("isauto", C.c_int), ("withwt", C.c_int),
+                ("icnt", C.POINTER(C.c_int64)), ("wcnt", _dp)]
+
+
 class Stats(C.Structure):
     _fields_ = [("candidates", C.c_uint64), ("in_range", C.c_uint64),
                 ("rechecked", C.c_uint64), ("recheck_inline", C.c_uint64),
@@ -133,6 +140,10 @@ PROTOTYPES = {
     "fcfcg_count": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                               P, P]),
     "fcfcg_stats_get": (C.c_int, [P, C.POINTER(Stats)]),
+    "fcfcg_graph_create": (C.c_int, [P, C.POINTER(CountItem), C.c_int,
+                                     C.c_int, C.POINTER(P)]),
+    "fcfcg_graph_run": (C.c_int, [P]),
+    "fcfcg_graph_destroy": (None, [P]),
     "fcfcg_set_cells_per_smax": (C.c_int, [P, C.c_int]),
     "fcfcg_autotune": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int,
                                  C.POINTER(C.c_int), C.POINTER(C.c_double)]),

@@ -51,14 +51,17 @@ __device__ __forceinline__ void add128(unsigned long long *lohi, long long v) {
  *   w_a w_b 2^51 = wi_a wi_b 2^-9 + (w_a wr_b + wr_a w_b) 2^51 (+ wr wr).
  * The first term is an exact 64-bit product rounded by a shift; the cross
  * term (|.| <= 2^21) is rounded with the 1.5 * 2^23 float trick; wr wr
- * (<= 2^-11 of a unit) is dropped.  No 64-bit float conversions.  Every
- * path uses this function, so a pair always adds the same integer.
+ * (<= 2^-11 of a unit) is dropped.  No 64-bit float conversions.  The
+ * function is symmetric in a and b (two rounded products and a commutative
+ * sum, no fused multiply-add), and every path uses it, so a pair adds the
+ * same integer whichever point is the chunk's: weighted sums do not depend
+ * on the order of the points within a cell.
  */
 __device__ __forceinline__ long long fix_prod(int ia, float ra, float fa,
     int ib, float rb, float fb) {
   const long long p = (long long) ia * (long long) ib;
   const long long main = (p + (1ll << 8)) >> 9;
-  const float c = __fmaf_rn(fa, rb, __fmul_rn(ra, fb));
+  const float c = __fadd_rn(__fmul_rn(fa, rb), __fmul_rn(ra, fb));
   const float t = __fmaf_rn(c, 2251799813685248.0f /* 2^51 */, 12582912.0f);
   return main + (long long) (__float_as_int(t) - 0x4B400000);
 }
@@ -318,7 +321,7 @@ __device__ __forceinline__ bool next_chunk(const fcfcg_launch &L,
   uint32_t c = 0;
   if (lane == 0) c = atomicAdd(L.chunk_head, 1u);
   c = __shfl_sync(FULLMASK, c, 0);
-  if (c >= L.nchunk) return false;
+  if (c >= (L.nchunk_dev ? __ldg(L.nchunk_dev) : L.nchunk)) return false;
   const uint4 ch = __ldg(((const uint4 *) L.chunks) + c);
   w.cell = ch.x;
   w.first = ch.y;
@@ -786,13 +789,14 @@ k_count32(const fcfcg_launch L) {
   const float4 *__restrict__ stD = (const float4 *) L.stenD;
   const int nwarp = CT32_THREADS / 32;
   unsigned long long n_cand = 0, n_in64 = 0, n_q64 = 0, n_inline = 0;
+  const uint32_t nchunk = L.nchunk_dev ? __ldg(L.nchunk_dev) : L.nchunk;
 
   for (;;) {
     __syncthreads();    /* the previous chunk is done with a / pre / bst */
     if (threadIdx.x == 0) sh_chunk = atomicAdd(L.chunk_head, 1u);
     __syncthreads();
     const uint32_t c = sh_chunk;
-    if (c >= L.nchunk) break;
+    if (c >= nchunk) break;
     const uint4 ch = __ldg(((const uint4 *) L.chunks) + c);
     int ncl[3] = {L.ncell[0], L.ncell[1], L.ncell[2]};
     uint32_t cbase = 0;
@@ -1122,8 +1126,15 @@ k_count64(const fcfcg_launch L) {
   }
 }
 
+/* Queued pairs to recheck: the queue's fill, at most its capacity. */
+__device__ __forceinline__ uint32_t queue_len(const fcfcg_launch &L) {
+  const uint32_t n = *(volatile const uint32_t *) L.qcount;
+  return n < L.qcap ? n : L.qcap;
+}
+
 /* Adjoint: FP64 recheck of queued pairs. */
-__global__ void k_recheck_adj(const fcfcg_launch L, uint32_t nq) {
+__global__ void k_recheck_adj(const fcfcg_launch L) {
+  const uint32_t nq = queue_len(L);
   unsigned long long n_in = 0;
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq;
        q += gridDim.x * blockDim.x) {
@@ -1140,7 +1151,8 @@ __global__ void k_recheck_adj(const fcfcg_launch L, uint32_t nq) {
 
 /* FP64 recheck of queued pairs. */
 template <int WT>
-__global__ void k_recheck(const fcfcg_launch L, uint32_t nq) {
+__global__ void k_recheck(const fcfcg_launch L) {
+  const uint32_t nq = queue_len(L);
   unsigned long long n_in = 0;
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < nq;
        q += gridDim.x * blockDim.x) {
@@ -1258,16 +1270,16 @@ extern "C" size_t fcfcg_k_count32_stage(int nsten, int withwt) {
 }
 
 extern "C" int fcfcg_k_recheck(void *stream, const fcfcg_launch *L,
-    uint32_t nq) {
-  if (!nq) return 0;
-  unsigned blocks = (nq + 255) / 256;
+    uint32_t nq_bound) {
+  if (!nq_bound) return 0;
+  unsigned blocks = (nq_bound + 255) / 256;
   if (blocks > 152 * 16) blocks = 152 * 16;
   if (L->adjoint)
-    k_recheck_adj<<<blocks, 256, 0, (cudaStream_t) stream>>>(*L, nq);
+    k_recheck_adj<<<blocks, 256, 0, (cudaStream_t) stream>>>(*L);
   else if (L->withwt)
-    k_recheck<1><<<blocks, 256, 0, (cudaStream_t) stream>>>(*L, nq);
+    k_recheck<1><<<blocks, 256, 0, (cudaStream_t) stream>>>(*L);
   else
-    k_recheck<0><<<blocks, 256, 0, (cudaStream_t) stream>>>(*L, nq);
+    k_recheck<0><<<blocks, 256, 0, (cudaStream_t) stream>>>(*L);
   return (int) cudaGetLastError();
 }
 

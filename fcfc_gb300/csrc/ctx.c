@@ -83,6 +83,9 @@ struct fcfcg_ctx {
   size_t d_grad_cap;
   unsigned long long *d_bout, *d_bstat;
   size_t d_bout_cap, d_bstat_cap;
+  /* bumped whenever a catalogue is loaded or a device buffer is
+   * reallocated: count graphs captured before are stale */
+  unsigned long bufgen;
 };
 
 static void set_err(fcfcg_ctx *c, const char *fmt, ...) {
@@ -137,6 +140,7 @@ const char *fcfcg_last_error(const fcfcg_ctx *ctx) {
 /* Grow a device buffer to at least `need` bytes. */
 static int grow(fcfcg_ctx *c, void **p, size_t *cap, size_t need) {
   if (*cap >= need && *p) return FCFCG_OK;
+  c->bufgen++;
   if (*p) cudaFree(*p);
   *p = NULL;
   *cap = 0;
@@ -338,6 +342,7 @@ static int load_common(fcfcg_ctx *c, int slot, size_t n, const double *x,
   CK(cudaSetDevice(c->device));
   slot_t *s = c->slot + slot;
   const int survey = (c->bins.geometry == FCFCG_GEOM_SURVEY);
+  c->bufgen++;
   if (s->cap < n || !s->x) {
     slot_free(s);
     size_t m = n ? n : 1;
@@ -682,15 +687,29 @@ static int stencil_build(fcfcg_ctx *c, const grid_t *g, int isauto, int *sten,
 }
 
 /* Sort a slot into the grid (skipped when already sorted for it). */
-static int slot_grid(fcfcg_ctx *c, slot_t *s, const grid_t *g) {
+/* Is slot s sorted into grid g? */
+static int slot_in_grid(const slot_t *s, const grid_t *g) {
   const size_t nc = (size_t) g->n[0] * g->n[1] * g->n[2];
-  if (s->grid_valid && s->ccap >= nc + 1 &&
-      !memcmp(s->gsig_n, g->n, sizeof g->n) &&
-      !memcmp(s->gsig_cw, g->cw, sizeof g->cw) &&
-      !memcmp(s->gsig_lo, g->lo, sizeof g->lo))
-    return FCFCG_OK;
+  return s->grid_valid && s->ccap >= nc + 1 &&
+         !memcmp(s->gsig_n, g->n, sizeof g->n) &&
+         !memcmp(s->gsig_cw, g->cw, sizeof g->cw) &&
+         !memcmp(s->gsig_lo, g->lo, sizeof g->lo);
+}
+
+/* Record that slot s is (or, once queued work ran, will be) in grid g. */
+static void slot_mark(slot_t *s, const grid_t *g) {
+  memcpy(s->gsig_n, g->n, sizeof g->n);
+  memcpy(s->gsig_cw, g->cw, sizeof g->cw);
+  memcpy(s->gsig_lo, g->lo, sizeof g->lo);
+  s->grid_valid = 1;
+}
+
+/* Buffers for sorting slot s into grid g (host side; may allocate). */
+static int slot_reserve(fcfcg_ctx *c, slot_t *s, const grid_t *g) {
+  const size_t nc = (size_t) g->n[0] * g->n[1] * g->n[2];
   const size_t n = s->n, m = n ? n : 1;
   if (s->scap < m) {
+    c->bufgen++;
     void *p[] = {s->l4, s->wq, s->sx, s->sy, s->sz, s->ss, s->sw, s->sid,
                  s->cell_of};
     for (size_t i = 0; i < sizeof p / sizeof p[0]; i++)
@@ -707,6 +726,7 @@ static int slot_grid(fcfcg_ctx *c, slot_t *s, const grid_t *g) {
     s->scap = m;
   }
   if (s->ccap < nc + 1) {
+    c->bufgen++;
     if (s->cstart) cudaFree(s->cstart);
     s->cstart = NULL;
     CK(cudaMalloc((void **) &s->cstart, sizeof(uint32_t) * (nc + 1)));
@@ -715,6 +735,14 @@ static int slot_grid(fcfcg_ctx *c, slot_t *s, const grid_t *g) {
   GROW(c->cfill, c->cfill_cap, sizeof(uint32_t) * (nc + 1));
   size_t st = fcfcg_scan_tmp_len(nc + 1) + 16;
   GROW(c->scan_tmp, c->scan_cap, sizeof(uint32_t) * st);
+  return FCFCG_OK;
+}
+
+/* Queue the sort of slot s into grid g (stream work only). */
+static int slot_sort(fcfcg_ctx *c, slot_t *s, const grid_t *g) {
+  const size_t nc = (size_t) g->n[0] * g->n[1] * g->n[2];
+  const size_t n = s->n;
+  size_t st = fcfcg_scan_tmp_len(nc + 1) + 16;
   const int survey = (c->bins.geometry == FCFCG_GEOM_SURVEY);
   CKK(fcfcg_k_grid(c->stream, n, s->x, s->y, s->z, survey ? s->s : NULL,
                    s->w, s->has_w, s->wexp, g->n, g->cw, g->lo, s->cell_of,
@@ -722,10 +750,6 @@ static int slot_grid(fcfcg_ctx *c, slot_t *s, const grid_t *g) {
                    s->sx, s->sy, s->sz, survey ? s->ss : NULL, s->sw,
                    s->sid));
   c->launches += n ? 5 : 3;
-  memcpy(s->gsig_n, g->n, sizeof g->n);
-  memcpy(s->gsig_cw, g->cw, sizeof g->cw);
-  memcpy(s->gsig_lo, g->lo, sizeof g->lo);
-  s->grid_valid = 1;
   return FCFCG_OK;
 }
 
@@ -908,10 +932,193 @@ int fcfcg_adjoint(fcfcg_ctx *c, int sa, int sb, int isauto, const double *g,
                     NULL, &r);
 }
 
-static int count_impl(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
-    int precision, int64_t *icnt, double *wcnt, const adj_req *adj) {
-  if (!c || c->host_only) return FCFCG_ERR_ARG;
-  const int nslot = FCFCG_MAX_SLOT + c->internal;
+/*
+ * A count in three parts.  count_plan_make (host side; may allocate): the
+ * grid, the stencil, the precision and the launch parameters, with every
+ * buffer the launches touch grown to size.  count_launch (stream work only:
+ * no allocation and no host synchronisation, so that it can be captured in
+ * a CUDA graph): sort the catalogues into the grid, cut its cells into
+ * chunks, count, recheck, and copy the histogram and the statistics to
+ * pinned host memory.  count_finish (once the stream has finished): the
+ * caller's histogram and the statistics.
+ */
+typedef struct {
+  slot_t *A, *B;
+  int isauto, withwt, prec;
+  grid_t g;
+  int nsten;
+  uint32_t ncell;
+  size_t st;                     /* scan scratch length of the chunk list */
+  fcfcg_launch L;                /* stencil pointers: set by the caller */
+} count_plan;
+
+#define STAT_WORDS 5   /* candidates, in range, rechecked, inline, chunks */
+
+static int count_plan_make(fcfcg_ctx *c, slot_t *A, slot_t *B, int isauto,
+    int withwt, int precision, int adj, int *sten, float *stD,
+    count_plan *P) {
+  const fcfcg_bins *b = &c->bins;
+  int rc;
+  memset(P, 0, sizeof *P);
+  P->A = A;
+  P->B = B;
+  P->isauto = isauto;
+  P->withwt = withwt;
+  grid_t *g = &P->g;
+  if ((rc = grid_setup(c, g, A, B))) return rc;
+  double dmax = 0;
+  if ((rc = stencil_build(c, g, isauto, sten, stD, &P->nsten, &dmax)))
+    return rc;
+  if ((rc = slot_reserve(c, A, g))) return rc;
+  if (B != A && (rc = slot_reserve(c, B, g))) return rc;
+  P->ncell = (uint32_t) ((size_t) g->n[0] * g->n[1] * g->n[2]);
+  GROW(c->cchunk, c->cchunk_cap,
+       sizeof(uint32_t) * 2 * ((size_t) P->ncell + 1));
+  P->st = fcfcg_scan_tmp_len(P->ncell + 1) + 16;
+  GROW(c->scan_tmp, c->scan_cap, sizeof(uint32_t) * P->st);
+  size_t maxchunk = A->n / FCFCG_CHUNK + P->ncell + 1;
+  GROW(c->chunks, c->chunk_cap, sizeof(uint32_t) * 4 * maxchunk);
+  fcfcg_launch *L = &P->L;
+  L->geometry = b->geometry;
+  L->bintype = b->bintype;
+  L->isauto = isauto;
+  L->withwt = withwt;
+  for (int d = 0; d < 3; d++) {
+    L->ncell[d] = g->n[d];
+    L->cw[d] = g->cw[d];
+    L->lo[d] = g->lo[d];
+    L->box[d] = b->box[d];
+    L->cwf[d] = (float) g->cw[d];
+    L->lof[d] = (float) g->lo[d];
+  }
+  L->nsten = P->nsten;
+  L->tzero = -1;
+  for (int t = 0; t < P->nsten; t++)
+    if (!sten[4 * t] && !sten[4 * t + 1] && !sten[4 * t + 2]) L->tzero = t;
+  L->chunks = c->chunks;
+  L->chunk_head = c->d_head;
+  /* k_chunks leaves the number of chunks after the ncell + 1 counts and
+   * ncell offsets in cchunk */
+  L->nchunk_dev = c->cchunk + ((size_t) P->ncell + 1) + P->ncell;
+  launch_cat(&L->A, A);
+  launch_cat(&L->B, B);
+  launch_bins(c, L);
+  int prec = precision;
+  if (prec == FCFCG_PREC_FP32_RECHECK && fp32_bounds(c, g, dmax, A, B, L))
+    prec = FCFCG_PREC_FP64;
+  if (prec == FCFCG_PREC_FP32_RECHECK) launch_fp32_tables(c, L);
+  size_t tabbytes = (prec == FCFCG_PREC_FP32_RECHECK)
+      ? fcfcg_k_count32_tab_bytes(L->nfs, L->nfp, L->nsb, L->npb) : 0;
+  size_t hbytes = (size_t) b->ntot * (withwt ? 8 : 4);
+  size_t stage = (prec == FCFCG_PREC_FP32_RECHECK)
+      ? fcfcg_k_count32_stage(P->nsten, withwt + (adj ? 1 : 0)) : 0;
+  if (tabbytes + stage > 200 * 1024) {
+    prec = FCFCG_PREC_FP64;
+    tabbytes = 0;
+    stage = 0;
+  }
+  L->hist_smem = (tabbytes + stage + hbytes <= 200 * 1024);
+  P->prec = prec;
+  return FCFCG_OK;
+}
+
+/* Stream side of a count.  sort_a / sort_b: sort that catalogue into the
+ * plan's grid first.  timed: record the context's events (not while
+ * capturing).  res (pinned, 2 ntot words) and stats (pinned, STAT_WORDS
+ * words): where the histogram and the statistics go; NULL for none. */
+static int count_launch(fcfcg_ctx *c, const count_plan *P, int sort_a,
+    int sort_b, int timed, void *res, unsigned long long *stats) {
+  const fcfcg_bins *b = &c->bins;
+  const fcfcg_launch *L = &P->L;
+  int rc;
+  if (timed) CK(cudaEventRecord(c->ev[0], c->stream));
+  if (sort_a && (rc = slot_sort(c, P->A, &P->g))) return rc;
+  if (sort_b && P->B != P->A && (rc = slot_sort(c, P->B, &P->g))) return rc;
+  /* work chunks: 64 points per CTA in the FP32 kernel, 32 per warp in the
+   * FP64 kernel */
+  const uint32_t clen = (P->prec == FCFCG_PREC_FP32_RECHECK) ? FCFCG_CHUNK32
+                                                             : FCFCG_CHUNK;
+  CKK(fcfcg_k_chunks(c->stream, P->A->cstart, P->ncell, clen, c->cchunk,
+                     c->scan_tmp, P->st, c->chunks, NULL, NULL, 0));
+  c->launches += 5;
+  if (timed) CK(cudaEventRecord(c->ev[1], c->stream));
+  CK(cudaMemsetAsync(c->d_cnt, 0, sizeof(unsigned long long) * b->ntot,
+                     c->stream));
+  CK(cudaMemsetAsync(c->d_wt, 0, sizeof(unsigned long long) * 2 * b->ntot,
+                     c->stream));
+  if (!L->adjoint)
+    CK(cudaMemsetAsync(c->d_wd, 0, sizeof(double) * b->ntot, c->stream));
+  CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * 4,
+                     c->stream));
+  CK(cudaMemsetAsync(c->d_head, 0, sizeof(uint32_t) * 2, c->stream));
+  if (timed) CK(cudaEventRecord(c->ev[2], c->stream));
+  size_t smem = 0;
+  CKK(fcfcg_k_count(c->stream, L, P->prec, c->nsm, &smem));
+  c->launches += 1;
+  if (timed) CK(cudaEventRecord(c->ev[3], c->stream));
+  if (P->prec == FCFCG_PREC_FP32_RECHECK) {
+    /* sized for a full queue; the kernel reads the fill on the device */
+    CKK(fcfcg_k_recheck(c->stream, L, (uint32_t) c->qcap));
+    c->launches += 1;
+  }
+  if (timed) CK(cudaEventRecord(c->ev[4], c->stream));
+  if (res) {
+    if (P->withwt && P->prec == FCFCG_PREC_FP64)
+      CK(cudaMemcpyAsync(res, c->d_wd, sizeof(double) * b->ntot,
+                         cudaMemcpyDeviceToHost, c->stream));
+    else if (P->withwt)
+      CK(cudaMemcpyAsync(res, c->d_wt,
+                         sizeof(unsigned long long) * 2 * b->ntot,
+                         cudaMemcpyDeviceToHost, c->stream));
+    else
+      CK(cudaMemcpyAsync(res, c->d_cnt, sizeof(unsigned long long) * b->ntot,
+                         cudaMemcpyDeviceToHost, c->stream));
+  }
+  if (stats) {
+    CK(cudaMemcpyAsync(stats, c->d_stats, sizeof(unsigned long long) * 4,
+                       cudaMemcpyDeviceToHost, c->stream));
+    /* the chunk count (32 bits) into the low half of the last word */
+    stats[4] = 0;
+    CK(cudaMemcpyAsync(stats + 4, L->nchunk_dev, sizeof(uint32_t),
+                       cudaMemcpyDeviceToHost, c->stream));
+  }
+  return FCFCG_OK;
+}
+
+/* Host side after the stream finished: the caller's histogram and the
+ * statistics (timings are the caller's). */
+static void count_finish(fcfcg_ctx *c, const count_plan *P, const void *res,
+    const unsigned long long *stats, int64_t *icnt, double *wcnt) {
+  const fcfcg_bins *b = &c->bins;
+  const unsigned long long *hres = (const unsigned long long *) res;
+  if (P->withwt && P->prec == FCFCG_PREC_FP64) {
+    memcpy(wcnt, res, sizeof(double) * b->ntot);
+  } else if (P->withwt) {
+    const int ex = P->A->wexp + P->B->wexp - P->L.fixF;
+    for (long i = 0; i < b->ntot; i++) {
+      __int128 v = (__int128) (((unsigned __int128) hres[2 * i + 1] << 64) |
+                               (unsigned __int128) hres[2 * i]);
+      wcnt[i] = ldexp((double) v, ex);
+    }
+  } else {
+    for (long i = 0; i < b->ntot; i++) icnt[i] = (int64_t) hres[i];
+  }
+  fcfcg_stats *o = &c->stats;
+  o->candidates = stats[0];
+  o->in_range = stats[1];
+  o->rechecked = stats[2];
+  o->recheck_inline = stats[3];
+  o->cells_per_smax = P->g.k;
+  for (int d = 0; d < 3; d++) o->ncell[d] = P->g.n[d];
+  o->nstencil = P->nsten;
+  o->nchunks = (uint32_t) stats[4];
+  o->precision_used = P->prec;
+  o->launches = c->launches;
+}
+
+/* Check the slots of a count: 0 or an error code. */
+static int count_args(fcfcg_ctx *c, int sa, int sb, int isauto,
+    int precision, int nslot) {
   if (sa < 0 || sa >= nslot || sb < 0 || sb >= nslot) {
     set_err(c, "slot out of range");
     return FCFCG_ERR_ARG;
@@ -922,14 +1129,23 @@ static int count_impl(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
   }
   if (precision != FCFCG_PREC_FP32_RECHECK && precision != FCFCG_PREC_FP64)
     return FCFCG_ERR_ARG;
+  if (!c->slot[sa].x || !c->slot[sb].x) {
+    set_err(c, "catalogue slot not loaded");
+    return FCFCG_ERR_ARG;
+  }
+  return FCFCG_OK;
+}
+
+static int count_impl(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
+    int precision, int64_t *icnt, double *wcnt, const adj_req *adj) {
+  if (!c || c->host_only) return FCFCG_ERR_ARG;
+  int rc = count_args(c, sa, sb, isauto, precision,
+                      FCFCG_MAX_SLOT + c->internal);
+  if (rc) return rc;
   if (!adj && ((withwt && !wcnt) || (!withwt && !icnt))) return FCFCG_ERR_ARG;
   CK(cudaSetDevice(c->device));
   const fcfcg_bins *b = &c->bins;
   slot_t *A = c->slot + sa, *B = c->slot + sb;
-  if (!A->x || !B->x) {
-    set_err(c, "catalogue slot not loaded");
-    return FCFCG_ERR_ARG;
-  }
   memset(&c->stats, 0, sizeof c->stats);
   if (A->n == 0 || B->n == 0) {
     if (icnt) memset(icnt, 0, sizeof(int64_t) * b->ntot);
@@ -940,75 +1156,26 @@ static int count_impl(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
     }
     return FCFCG_OK;
   }
-  CK(cudaEventRecord(c->ev[0], c->stream));
-  grid_t g;
-  memset(&g, 0, sizeof g);
-  int rc = grid_setup(c, &g, A, B);
+  count_plan P;
+  rc = count_plan_make(c, A, B, isauto, withwt, precision, adj != NULL,
+                       c->sten, c->stD, &P);
   if (rc) return rc;
-  int *sten = c->sten;
-  float *stD = c->stD;
-  int nsten = 0;
-  double dmax = 0;
-  if ((rc = stencil_build(c, &g, isauto, sten, stD, &nsten, &dmax))) return rc;
-  if ((rc = slot_grid(c, A, &g))) return rc;
-  if (B != A && (rc = slot_grid(c, B, &g))) return rc;
-  const uint32_t ncell = (uint32_t) ((size_t) g.n[0] * g.n[1] * g.n[2]);
-  GROW(c->cchunk, c->cchunk_cap, sizeof(uint32_t) * 2 * ((size_t) ncell + 1));
-  size_t st = fcfcg_scan_tmp_len(ncell + 1) + 16;
-  GROW(c->scan_tmp, c->scan_cap, sizeof(uint32_t) * st);
-  size_t maxchunk = A->n / FCFCG_CHUNK + ncell + 1;
-  GROW(c->chunks, c->chunk_cap, sizeof(uint32_t) * 4 * maxchunk);
-  rc = upload(c, (void **) &c->d_sten, sten, sizeof(int) * 4 * nsten);
+  rc = upload(c, (void **) &c->d_sten, c->sten, sizeof(int) * 4 * P.nsten);
   if (rc) return rc;
-  rc = upload(c, (void **) &c->d_stenD, stD, sizeof(float) * 4 * nsten);
+  rc = upload(c, (void **) &c->d_stenD, c->stD, sizeof(float) * 4 * P.nsten);
   if (rc) return rc;
-  fcfcg_launch L;
-  memset(&L, 0, sizeof L);
-  L.geometry = b->geometry;
-  L.bintype = b->bintype;
-  L.isauto = isauto;
-  L.withwt = withwt;
-  for (int d = 0; d < 3; d++) {
-    L.ncell[d] = g.n[d];
-    L.cw[d] = g.cw[d];
-    L.lo[d] = g.lo[d];
-    L.box[d] = b->box[d];
-    L.cwf[d] = (float) g.cw[d];
-    L.lof[d] = (float) g.lo[d];
-  }
-  L.nsten = nsten;
-  L.tzero = -1;
-  for (int t = 0; t < nsten; t++)
-    if (!sten[4 * t] && !sten[4 * t + 1] && !sten[4 * t + 2]) L.tzero = t;
-  L.sten = c->d_sten;
-  L.stenD = c->d_stenD;
-  L.chunks = c->chunks;
-  L.chunk_head = c->d_head;
-  launch_cat(&L.A, A);
-  launch_cat(&L.B, B);
-  launch_bins(c, &L);
-  int prec = precision;
-  if (prec == FCFCG_PREC_FP32_RECHECK && fp32_bounds(c, &g, dmax, A, B, &L))
-    prec = FCFCG_PREC_FP64;
-  if (prec == FCFCG_PREC_FP32_RECHECK) launch_fp32_tables(c, &L);
-  size_t tabbytes = (prec == FCFCG_PREC_FP32_RECHECK)
-      ? fcfcg_k_count32_tab_bytes(L.nfs, L.nfp, L.nsb, L.npb) : 0;
-  size_t hbytes = (size_t) b->ntot * (withwt ? 8 : 4);
-  size_t stage = (prec == FCFCG_PREC_FP32_RECHECK)
-      ? fcfcg_k_count32_stage(nsten, withwt + (adj ? 1 : 0)) : 0;
-  if (tabbytes + stage > 200 * 1024) {
-    prec = FCFCG_PREC_FP64;
-    tabbytes = 0;
-    stage = 0;
-  }
-  L.hist_smem = (tabbytes + stage + hbytes <= 200 * 1024);
+  P.L.sten = c->d_sten;
+  P.L.stenD = c->d_stenD;
+  const int sort_a = !slot_in_grid(A, &P.g);
+  const int sort_b = (B != A) && !slot_in_grid(B, &P.g);
+  fcfcg_launch *L = &P.L;
   if (adj) {
     const size_t ng = A->n + (isauto ? 0 : B->n);
     GROW(c->d_grad, c->d_grad_cap, sizeof(double) * 2 * ng);
-    L.adjoint = 1;
-    L.gadj = c->d_wd;
-    L.dA = c->d_grad;
-    L.dB = isauto ? c->d_grad : c->d_grad + A->n;
+    L->adjoint = 1;
+    L->gadj = c->d_wd;
+    L->dA = c->d_grad;
+    L->dB = isauto ? c->d_grad : c->d_grad + A->n;
     CK(cudaMemcpyAsync(c->d_wd, adj->g, sizeof(double) * b->ntot,
                        cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemsetAsync(c->d_grad, 0, sizeof(double) * ng, c->stream));
@@ -1020,7 +1187,7 @@ static int count_impl(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
       }
       if (fabs(adj->g[k]) > gmax) gmax = fabs(adj->g[k]);
     }
-    if (prec == FCFCG_PREC_FP32_RECHECK) {
+    if (P.prec == FCFCG_PREC_FP32_RECHECK) {
       /* unit of the integer gradient sums: 2^-S with |w| |g| 2^S <= 2^50
        * for every weight and cotangent entry */
       int gexp = 0;
@@ -1044,111 +1211,47 @@ static int count_impl(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
       if (ce == cudaSuccess) ce = cudaStreamSynchronize(c->stream);
       free(gf);
       CK(ce);
-      L.gfix = c->d_gfix;
-      L.gunit = ldexp(1.0, -S);
+      L->gfix = c->d_gfix;
+      L->gunit = ldexp(1.0, -S);
     }
   }
-
-  /* work chunks: 64 points per CTA in the FP32 kernel, 32 per warp in the
-   * FP64 kernel */
-  uint32_t nchunk = 0;
-  const uint32_t clen = (prec == FCFCG_PREC_FP32_RECHECK) ? FCFCG_CHUNK32
-                                                          : FCFCG_CHUNK;
-  CKK(fcfcg_k_chunks(c->stream, A->cstart, ncell, clen, c->cchunk,
-                     c->scan_tmp, st, c->chunks, &nchunk, NULL, 0));
-  c->launches += 5;
-  CK(cudaEventRecord(c->ev[1], c->stream));
-  CK(cudaStreamSynchronize(c->stream));
-  L.nchunk = nchunk;
-  CK(cudaMemsetAsync(c->d_cnt, 0, sizeof(unsigned long long) * b->ntot,
-                     c->stream));
-  CK(cudaMemsetAsync(c->d_wt, 0, sizeof(unsigned long long) * 2 * b->ntot,
-                     c->stream));
-  if (!adj)
-    CK(cudaMemsetAsync(c->d_wd, 0, sizeof(double) * b->ntot, c->stream));
-  CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * 4, c->stream));
-  CK(cudaMemsetAsync(c->d_head, 0, sizeof(uint32_t) * 2, c->stream));
-  CK(cudaEventRecord(c->ev[2], c->stream));
-  size_t smem = 0;
-  CKK(fcfcg_k_count(c->stream, &L, prec, c->nsm, &smem));
-  c->launches += 1;
-  CK(cudaEventRecord(c->ev[3], c->stream));
-  uint32_t nq = 0;
-  if (prec == FCFCG_PREC_FP32_RECHECK) {
-    CK(cudaMemcpyAsync(&nq, c->d_qcount, sizeof nq, cudaMemcpyDeviceToHost,
-                       c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    if (nq > c->qcap) nq = (uint32_t) c->qcap;
-    CKK(fcfcg_k_recheck(c->stream, &L, nq));
-    c->launches += nq ? 1 : 0;
-  }
-  CK(cudaEventRecord(c->ev[4], c->stream));
+  size_t rbytes = sizeof(unsigned long long) * (2 * b->ntot + STAT_WORDS);
+  if ((rc = ensure_pinned(c, rbytes))) return rc;
+  unsigned long long *hres = (unsigned long long *) c->h_pinned;
+  unsigned long long *hstats = hres + 2 * b->ntot;
+  rc = count_launch(c, &P, sort_a, sort_b, 1, adj ? NULL : hres, hstats);
+  if (rc) return rc;
+  slot_mark(A, &P.g);
+  if (B != A) slot_mark(B, &P.g);
   if (adj) {
     /* sorted order back to input order, then to the host */
     const size_t ng = A->n + (isauto ? 0 : B->n);
     double *unsorted = c->d_grad + ng;
-    CKK(fcfcg_k_unsort(c->stream, A->n, A->sid, L.dA, unsorted));
+    CKK(fcfcg_k_unsort(c->stream, A->n, A->sid, L->dA, unsorted));
     if (!isauto)
-      CKK(fcfcg_k_unsort(c->stream, B->n, B->sid, L.dB, unsorted + A->n));
+      CKK(fcfcg_k_unsort(c->stream, B->n, B->sid, L->dB, unsorted + A->n));
     c->launches += isauto ? 1 : 2;
-    unsigned long long hst[4];
     CK(cudaMemcpyAsync(adj->dwa, unsorted, sizeof(double) * A->n,
                        cudaMemcpyDeviceToHost, c->stream));
     if (!isauto && adj->dwb)
       CK(cudaMemcpyAsync(adj->dwb, unsorted + A->n, sizeof(double) * B->n,
                          cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(hst, c->d_stats, sizeof hst, cudaMemcpyDeviceToHost,
-                       c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    fcfcg_stats *o = &c->stats;
-    o->candidates = hst[0];
-    o->in_range = hst[1];
-    o->rechecked = hst[2];
-    o->recheck_inline = hst[3];
-    float ms = 0;
-    cudaEventElapsedTime(&ms, c->ev[2], c->ev[3]);
-    o->ms_count = ms;
-    cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]);
-    o->ms_total = ms;
-    o->cells_per_smax = g.k;
-    o->precision_used = prec;
-    o->launches = c->launches;
-    return FCFCG_OK;
   }
-  /* results */
-  size_t rbytes = sizeof(unsigned long long) * 2 * b->ntot + 64;
-  if ((rc = ensure_pinned(c, rbytes))) return rc;
-  unsigned long long *hres = (unsigned long long *) c->h_pinned;
-  unsigned long long hstats[4];
-  if (withwt && prec == FCFCG_PREC_FP64)
-    CK(cudaMemcpyAsync(hres, c->d_wd, sizeof(double) * b->ntot,
-                       cudaMemcpyDeviceToHost, c->stream));
-  else if (withwt)
-    CK(cudaMemcpyAsync(hres, c->d_wt, sizeof(unsigned long long) * 2 * b->ntot,
-                       cudaMemcpyDeviceToHost, c->stream));
-  else
-    CK(cudaMemcpyAsync(hres, c->d_cnt, sizeof(unsigned long long) * b->ntot,
-                       cudaMemcpyDeviceToHost, c->stream));
-  CK(cudaMemcpyAsync(hstats, c->d_stats, sizeof hstats, cudaMemcpyDeviceToHost,
-                     c->stream));
   CK(cudaStreamSynchronize(c->stream));
-  if (withwt && prec == FCFCG_PREC_FP64) {
-    memcpy(wcnt, hres, sizeof(double) * b->ntot);
-  } else if (withwt) {
-    const int ex = A->wexp + B->wexp - L.fixF;
-    for (long i = 0; i < b->ntot; i++) {
-      __int128 v = (__int128) (((unsigned __int128) hres[2 * i + 1] << 64) |
-                               (unsigned __int128) hres[2 * i]);
-      wcnt[i] = ldexp((double) v, ex);
-    }
+  if (adj) {
+    fcfcg_stats *o = &c->stats;
+    o->candidates = hstats[0];
+    o->in_range = hstats[1];
+    o->rechecked = hstats[2];
+    o->recheck_inline = hstats[3];
+    o->cells_per_smax = P.g.k;
+    o->nchunks = (uint32_t) hstats[4];
+    o->precision_used = P.prec;
+    o->launches = c->launches;
   } else {
-    for (long i = 0; i < b->ntot; i++) icnt[i] = (int64_t) hres[i];
+    count_finish(c, &P, hres, hstats, icnt, wcnt);
   }
   fcfcg_stats *o = &c->stats;
-  o->candidates = hstats[0];
-  o->in_range = hstats[1];
-  o->rechecked = hstats[2];
-  o->recheck_inline = hstats[3];
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
   o->ms_grid = ms;
@@ -1158,14 +1261,210 @@ static int count_impl(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
   o->ms_recheck = ms;
   cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]);
   o->ms_total = ms;
-  o->cells_per_smax = g.k;
-  for (int d = 0; d < 3; d++) o->ncell[d] = g.n[d];
-  o->nstencil = nsten;
-  o->nchunks = nchunk;
-  o->precision_used = prec;
-  o->launches = c->launches;
-  (void) smem;
   return FCFCG_OK;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Count graphs.                                                             */
+
+struct fcfcg_graph {
+  fcfcg_ctx *c;
+  int n, precision;
+  fcfcg_count_item item[FCFCG_MAX_GRAPH_ITEMS];
+  count_plan plan[FCFCG_MAX_GRAPH_ITEMS];
+  int empty[FCFCG_MAX_GRAPH_ITEMS];
+  int *d_sten[FCFCG_MAX_GRAPH_ITEMS];
+  float *d_stenD[FCFCG_MAX_GRAPH_ITEMS];
+  unsigned long long *h_stage;   /* pinned: per item 2 ntot + STAT_WORDS */
+  cudaGraph_t graph;
+  cudaGraphExec_t exec;
+  unsigned long bufgen;          /* the context's, when captured */
+  uint64_t launches;             /* kernel launches per run */
+  /* the grid each slot is left sorted into by a run */
+  grid_t last[FCFCG_MAX_SLOT];
+  int has_last[FCFCG_MAX_SLOT];
+};
+
+static void graph_release(fcfcg_graph *G) {
+  if (G->exec) cudaGraphExecDestroy(G->exec);
+  if (G->graph) cudaGraphDestroy(G->graph);
+  G->exec = NULL;
+  G->graph = NULL;
+  for (int i = 0; i < G->n; i++) {
+    if (G->d_sten[i]) cudaFree(G->d_sten[i]);
+    if (G->d_stenD[i]) cudaFree(G->d_stenD[i]);
+    G->d_sten[i] = NULL;
+    G->d_stenD[i] = NULL;
+  }
+}
+
+static unsigned long long *stage_of(const fcfcg_graph *G, int i) {
+  return G->h_stage + (size_t) i * (2 * (size_t) G->c->bins.ntot + STAT_WORDS);
+}
+
+/* Plan every item and capture their launches as one graph. */
+static int graph_build(fcfcg_graph *G) {
+  fcfcg_ctx *c = G->c;
+  graph_release(G);
+  CK(cudaSetDevice(c->device));
+  /* the first pass grows the context's buffers, the second takes their
+   * final addresses */
+  for (int pass = 0; pass < 2; pass++) {
+    const unsigned long gen0 = c->bufgen;
+    for (int i = 0; i < G->n; i++) {
+      const fcfcg_count_item *it = G->item + i;
+      slot_t *A = c->slot + it->slot_a, *B = c->slot + it->slot_b;
+      G->empty[i] = (A->n == 0 || B->n == 0);
+      if (G->empty[i]) continue;
+      int rc = count_plan_make(c, A, B, it->isauto, it->withwt,
+                               G->precision, 0, c->sten, c->stD,
+                               G->plan + i);
+      if (rc) return rc;
+      if (pass == 1) {
+        const size_t ns = (size_t) G->plan[i].nsten;
+        CK(cudaMalloc((void **) &G->d_sten[i], sizeof(int) * 4 * (ns ? ns : 1)));
+        CK(cudaMalloc((void **) &G->d_stenD[i],
+                      sizeof(float) * 4 * (ns ? ns : 1)));
+        CK(cudaMemcpy(G->d_sten[i], c->sten, sizeof(int) * 4 * ns,
+                      cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(G->d_stenD[i], c->stD, sizeof(float) * 4 * ns,
+                      cudaMemcpyHostToDevice));
+        G->plan[i].L.sten = G->d_sten[i];
+        G->plan[i].L.stenD = G->d_stenD[i];
+      }
+    }
+    if (pass == 1 && c->bufgen != gen0) {
+      set_err(c, "count graph: buffers moved while planning");
+      return FCFCG_ERR_CUDA;
+    }
+  }
+  G->bufgen = c->bufgen;
+  CK(cudaStreamSynchronize(c->stream));
+  const uint64_t l0 = c->launches;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed));
+  int rc = FCFCG_OK;
+  for (int i = 0; i < G->n && !rc; i++) {
+    if (G->empty[i]) continue;
+    unsigned long long *st = stage_of(G, i);
+    rc = count_launch(c, G->plan + i, 1, 1, 0, st,
+                      st + 2 * (size_t) c->bins.ntot);
+  }
+  cudaGraph_t gr = NULL;
+  cudaError_t e = cudaStreamEndCapture(c->stream, &gr);
+  if (rc || e != cudaSuccess) {
+    if (gr) cudaGraphDestroy(gr);
+    if (!rc) {
+      set_err(c, "CUDA: %s", cudaGetErrorString(e));
+      rc = FCFCG_ERR_CUDA;
+    }
+    return rc;
+  }
+  G->graph = gr;
+  CK(cudaGraphInstantiate(&G->exec, gr, 0));
+  G->launches = c->launches - l0;
+  c->launches = l0;
+  /* a run leaves each slot sorted into the grid of its last count; until
+   * then their order is unknown to plain counts */
+  memset(G->has_last, 0, sizeof G->has_last);
+  for (int i = 0; i < G->n; i++) {
+    if (G->empty[i]) continue;
+    const int s2[2] = {G->item[i].slot_a, G->item[i].slot_b};
+    for (int k = 0; k < 2; k++) {
+      G->last[s2[k]] = G->plan[i].g;
+      G->has_last[s2[k]] = 1;
+      c->slot[s2[k]].grid_valid = 0;
+    }
+  }
+  return FCFCG_OK;
+}
+
+int fcfcg_graph_create(fcfcg_ctx *c, const fcfcg_count_item *items,
+    int nitem, int precision, fcfcg_graph **out) {
+  if (!c || c->host_only || !items || !out || nitem < 1 ||
+      nitem > FCFCG_MAX_GRAPH_ITEMS)
+    return FCFCG_ERR_ARG;
+  *out = NULL;
+  for (int i = 0; i < nitem; i++) {
+    const fcfcg_count_item *it = items + i;
+    int rc = count_args(c, it->slot_a, it->slot_b, it->isauto, precision,
+                        FCFCG_MAX_SLOT);
+    if (rc) return rc;
+    if ((it->withwt && !it->wcnt) || (!it->withwt && !it->icnt))
+      return FCFCG_ERR_ARG;
+  }
+  CK(cudaSetDevice(c->device));
+  fcfcg_graph *G = calloc(1, sizeof *G);
+  if (!G) return FCFCG_ERR_MEMORY;
+  G->c = c;
+  G->n = nitem;
+  G->precision = precision;
+  memcpy(G->item, items, sizeof *items * nitem);
+  const size_t words = (size_t) nitem * (2 * (size_t) c->bins.ntot + STAT_WORDS);
+  cudaError_t e = cudaMallocHost((void **) &G->h_stage,
+                                 sizeof(unsigned long long) * words);
+  if (e != cudaSuccess) {
+    free(G);
+    set_err(c, "CUDA: %s", cudaGetErrorString(e));
+    return FCFCG_ERR_CUDA;
+  }
+  memset(G->h_stage, 0, sizeof(unsigned long long) * words);
+  int rc = graph_build(G);
+  if (rc) {
+    fcfcg_graph_destroy(G);
+    return rc;
+  }
+  *out = G;
+  return FCFCG_OK;
+}
+
+int fcfcg_graph_run(fcfcg_graph *G) {
+  if (!G) return FCFCG_ERR_ARG;
+  fcfcg_ctx *c = G->c;
+  CK(cudaSetDevice(c->device));
+  for (int i = 0; i < G->n; i++) {
+    /* a slot emptied or unloaded since the capture */
+    const fcfcg_count_item *it = G->item + i;
+    if (!c->slot[it->slot_a].x || !c->slot[it->slot_b].x) {
+      set_err(c, "catalogue slot not loaded");
+      return FCFCG_ERR_ARG;
+    }
+  }
+  if (!G->exec || c->bufgen != G->bufgen) {
+    int rc = graph_build(G);
+    if (rc) return rc;
+  }
+  CK(cudaEventRecord(c->ev[0], c->stream));
+  CK(cudaGraphLaunch(G->exec, c->stream));
+  CK(cudaEventRecord(c->ev[4], c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->launches += G->launches;
+  memset(&c->stats, 0, sizeof c->stats);
+  for (int i = 0; i < G->n; i++) {
+    const fcfcg_count_item *it = G->item + i;
+    const long ntot = c->bins.ntot;
+    if (G->empty[i]) {
+      if (it->icnt) memset(it->icnt, 0, sizeof(int64_t) * ntot);
+      if (it->wcnt) memset(it->wcnt, 0, sizeof(double) * ntot);
+      continue;
+    }
+    const unsigned long long *st = stage_of(G, i);
+    count_finish(c, G->plan + i, st, st + 2 * (size_t) ntot,
+                 it->withwt ? NULL : it->icnt, it->withwt ? it->wcnt : NULL);
+  }
+  for (int s = 0; s < FCFCG_MAX_SLOT; s++)
+    if (G->has_last[s]) slot_mark(c->slot + s, G->last + s);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]);
+  c->stats.ms_total = ms;
+  return FCFCG_OK;
+}
+
+void fcfcg_graph_destroy(fcfcg_graph *G) {
+  if (!G) return;
+  cudaSetDevice(G->c->device);
+  graph_release(G);
+  if (G->h_stage) cudaFreeHost(G->h_stage);
+  free(G);
 }
 
 const fcfcg_bins *fcfcg_ctx_bins(const fcfcg_ctx *c) {

@@ -104,8 +104,10 @@ typedef struct {
   int nsten;
   const int *sten;
   const float *stenD;
-  /* chunks: uint4 (cell, first sorted index, count, 0) */
+  /* chunks: uint4 (cell, first sorted index, count, 0); their number is
+   * nchunk, or *nchunk_dev when set (written by an earlier launch) */
   uint32_t nchunk;
+  const uint32_t *nchunk_dev;
   const uint32_t *chunks;
   uint32_t *chunk_head;
   fcfcg_dcat A, B;
@@ -205,7 +207,9 @@ int fcfcg_k_bbox(void *stream, size_t n, const double *x, const double *y,
     const double *z, unsigned long long *bits6);
 int fcfcg_k_count(void *stream, const fcfcg_launch *L, int precision,
     int nsm, size_t *smem_used);
-int fcfcg_k_recheck(void *stream, const fcfcg_launch *L, uint32_t nq);
+/* FP64 recheck of the queued pairs; the kernels read the queue length on
+ * the device, nq_bound (>= it) only sizes the grid. */
+int fcfcg_k_recheck(void *stream, const fcfcg_launch *L, uint32_t nq_bound);
 int fcfcg_k_flush_count(void *stream, const fcfcg_launch *L);
 size_t fcfcg_scan_tmp_len(size_t n);
 const char *fcfcg_cuda_errstr(int code);

@@ -14,6 +14,7 @@ missing GPU or library raises FCFCGError.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -68,6 +69,7 @@ class PairCounter:
         self._check(lib.fcfcg_bins_edges(self.h, capi.ptr(self.sbin),
                                          capi.ptr(self.pbin)))
         self._n = {}
+        self._graphs = weakref.WeakValueDictionary()
 
     # -- plumbing -----------------------------------------------------------
     def _check(self, rc):
@@ -76,6 +78,9 @@ class PairCounter:
             raise FCFCGError(rc, msg)
 
     def close(self):
+        # count graphs refer to the context: they go first
+        for g in list(getattr(self, "_graphs", {}).values()):
+            g.close()
         if getattr(self, "h", None):
             self.lib.fcfcg_destroy(self.h)
             self.h = None
@@ -204,6 +209,13 @@ class PairCounter:
                                              int(precision), capi.ptr(res),
                                              None))
         return res
+
+    def count_graph(self, pairs, precision=PREC_FP32_RECHECK):
+        """Capture counts as one CUDA graph (fcfcg_graph_create).  pairs:
+        (a, b, weighted) per count, b None or == a for an auto count; e.g.
+        DD, DR, RR of a survey.  Returns a CountGraph whose run() replays
+        them and returns the histograms, the same as count_pairs."""
+        return CountGraph(self, pairs, precision)
 
     # -- batches of periodic boxes -----------------------------------------
     def _jobs(self, cats, boxes, weights, weighted, on_device):
@@ -365,3 +377,50 @@ class PairCounter:
     def write_wp(self, fname, wp):
         wp = np.ascontiguousarray(wp, np.float64)
         self._check(self.lib.fcfcg_write_wp(self.h, fname.encode(), capi.ptr(wp)))
+
+
+class CountGraph:
+    """Counts of one PairCounter captured as a CUDA graph; run() replays it
+    (the catalogues are read when it runs) and returns one histogram per
+    count: int64 counts, or FP64 weighted sums."""
+
+    def __init__(self, pc: PairCounter, pairs, precision=PREC_FP32_RECHECK):
+        self.pc = pc
+        n = len(pairs)
+        items = (capi.CountItem * n)()
+        self.out = []
+        for i, (a, b, weighted) in enumerate(pairs):
+            isauto = b is None or b == a
+            b = a if b is None else b
+            it = items[i]
+            it.slot_a, it.slot_b = int(a), int(b)
+            it.isauto, it.withwt = int(isauto), int(bool(weighted))
+            if weighted:
+                res = np.zeros(pc.ntot, np.float64)
+                it.wcnt = res.ctypes.data_as(C.POINTER(C.c_double))
+            else:
+                res = np.zeros(pc.ntot, np.int64)
+                it.icnt = res.ctypes.data_as(C.POINTER(C.c_int64))
+            self.out.append(res)
+        self._items = items
+        self.h = None
+        h = C.c_void_p()
+        pc._check(pc.lib.fcfcg_graph_create(pc.h, items, n, int(precision),
+                                            C.byref(h)))
+        self.h = h
+        pc._graphs[id(self)] = self
+
+    def run(self):
+        self.pc._check(self.pc.lib.fcfcg_graph_run(self.h))
+        return [r.copy() for r in self.out]
+
+    def close(self):
+        if self.h and self.pc.h:
+            self.pc.lib.fcfcg_graph_destroy(self.h)
+        self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -283,6 +283,36 @@ int fcfcg_count(fcfcg_ctx *ctx, int slot_a, int slot_b, int isauto,
     int withwt, int precision, int64_t *icnt, double *wcnt);
 
 /*
+ * Count graphs (no reference counterpart): a fixed sequence of counts --
+ * typically DD, DR and RR of one survey, the eval_pairs loop of
+ * src/fcfc/2pt/eval_cf.c -- captured once as a CUDA graph and replayed.
+ * A replay queues, for every item, the sort of its catalogues into the
+ * item's cell grid, the chunk list, the count and the FP64 recheck kernels
+ * and the copy of the histogram to pinned host memory, with no host
+ * synchronisation in between; fcfcg_graph_run then writes each item's
+ * icnt or wcnt exactly as fcfcg_count would.  The graph reads the context's
+ * catalogue slots when it runs: reloading a slot (or a count that makes
+ * the context reallocate a buffer) makes the next run capture the graph
+ * again, transparently.  Items use user slots (0 .. FCFCG_MAX_SLOT - 1).
+ * Destroy a graph before its context.  fcfcg_stats after a run describes
+ * the last item, with ms_total the whole replay.
+ */
+#define FCFCG_MAX_GRAPH_ITEMS 16
+
+typedef struct {
+  int slot_a, slot_b, isauto, withwt;
+  int64_t *icnt;      /* ntot: unweighted counts (withwt = 0) */
+  double *wcnt;       /* ntot: weighted sums (withwt = 1) */
+} fcfcg_count_item;
+
+typedef struct fcfcg_graph fcfcg_graph;
+
+int fcfcg_graph_create(fcfcg_ctx *ctx, const fcfcg_count_item *items,
+    int nitem, int precision, fcfcg_graph **graph);
+int fcfcg_graph_run(fcfcg_graph *graph);
+void fcfcg_graph_destroy(fcfcg_graph *graph);
+
+/*
  * Adjoint of the weighted count (no reference counterpart: FCFC has no
  * derivatives).  With C_b = sum over counted pairs (i, j) in bin b of
  * w_i w_j, as fcfcg_count(withwt = 1) returns it, and a cotangent g[ntot]
