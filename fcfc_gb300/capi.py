@@ -143,6 +143,8 @@ PROTOTYPES = {
     "fcfcg_graph_create": (C.c_int, [P, C.POINTER(CountItem), C.c_int,
                                      C.c_int, C.POINTER(P)]),
     "fcfcg_graph_run": (C.c_int, [P]),
+    "fcfcg_graph_info": (C.c_int, [P, C.POINTER(C.c_int),
+                                   C.POINTER(C.c_uint64)]),
     "fcfcg_graph_destroy": (None, [P]),
     "fcfcg_set_cells_per_smax": (C.c_int, [P, C.c_int]),
     "fcfcg_autotune": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int,

@@ -342,8 +342,8 @@ static int load_common(fcfcg_ctx *c, int slot, size_t n, const double *x,
   CK(cudaSetDevice(c->device));
   slot_t *s = c->slot + slot;
   const int survey = (c->bins.geometry == FCFCG_GEOM_SURVEY);
-  c->bufgen++;
   if (s->cap < n || !s->x) {
+    c->bufgen++;
     slot_free(s);
     size_t m = n ? n : 1;
     CK(cudaMalloc((void **) &s->x, sizeof(double) * m));
@@ -944,6 +944,8 @@ int fcfcg_adjoint(fcfcg_ctx *c, int sa, int sb, int isauto, const double *g,
  */
 typedef struct {
   slot_t *A, *B;
+  size_t na, nb;                 /* catalogue sizes and weights planned for */
+  int hwa, hwb;
   int isauto, withwt, prec;
   grid_t g;
   int nsten;
@@ -962,6 +964,10 @@ static int count_plan_make(fcfcg_ctx *c, slot_t *A, slot_t *B, int isauto,
   memset(P, 0, sizeof *P);
   P->A = A;
   P->B = B;
+  P->na = A->n;
+  P->nb = B->n;
+  P->hwa = A->has_w;
+  P->hwb = B->has_w;
   P->isauto = isauto;
   P->withwt = withwt;
   grid_t *g = &P->g;
@@ -1280,6 +1286,7 @@ struct fcfcg_graph {
   cudaGraphExec_t exec;
   unsigned long bufgen;          /* the context's, when captured */
   uint64_t launches;             /* kernel launches per run */
+  int captures;
   /* the grid each slot is left sorted into by a run */
   grid_t last[FCFCG_MAX_SLOT];
   int has_last[FCFCG_MAX_SLOT];
@@ -1361,6 +1368,7 @@ static int graph_build(fcfcg_graph *G) {
   }
   G->graph = gr;
   CK(cudaGraphInstantiate(&G->exec, gr, 0));
+  G->captures++;
   G->launches = c->launches - l0;
   c->launches = l0;
   /* a run leaves each slot sorted into the grid of its last count; until
@@ -1429,7 +1437,25 @@ int fcfcg_graph_run(fcfcg_graph *G) {
       return FCFCG_ERR_ARG;
     }
   }
-  if (!G->exec || c->bufgen != G->bufgen) {
+  /* capture again when a buffer moved or the plan of an item changed (new
+   * catalogue sizes, bounding boxes, weights or an autotuned grid); a slot
+   * reloaded with data that plans the same replays as it is */
+  int stale = !G->exec || c->bufgen != G->bufgen;
+  for (int i = 0; i < G->n && !stale; i++) {
+    const fcfcg_count_item *it = G->item + i;
+    slot_t *A = c->slot + it->slot_a, *B = c->slot + it->slot_b;
+    const int empty = (A->n == 0 || B->n == 0);
+    if (empty != G->empty[i]) stale = 1;
+    if (empty || stale) continue;
+    count_plan P;
+    int rc = count_plan_make(c, A, B, it->isauto, it->withwt, G->precision,
+                             0, c->sten, c->stD, &P);
+    if (rc) return rc;
+    P.L.sten = G->plan[i].L.sten;
+    P.L.stenD = G->plan[i].L.stenD;
+    stale = (c->bufgen != G->bufgen) || memcmp(&P, G->plan + i, sizeof P);
+  }
+  if (stale) {
     int rc = graph_build(G);
     if (rc) return rc;
   }
@@ -1456,6 +1482,14 @@ int fcfcg_graph_run(fcfcg_graph *G) {
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev[0], c->ev[4]);
   c->stats.ms_total = ms;
+  return FCFCG_OK;
+}
+
+int fcfcg_graph_info(const fcfcg_graph *G, int *captures,
+    uint64_t *launches) {
+  if (!G) return FCFCG_ERR_ARG;
+  if (captures) *captures = G->captures;
+  if (launches) *launches = G->launches;
   return FCFCG_OK;
 }
 

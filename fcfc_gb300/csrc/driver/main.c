@@ -6,7 +6,9 @@
  * src/fcfc/2pt/fcfc.c): read the configuration (load_conf.c), set up the
  * bins (cf_setup), and for every entry of PAIR_COUNT read the catalogues
  * (tree_create: ASCII reading, RA/Dec/z conversion for FCFC_2PT, rescaling
- * on the device), count the pairs (count_pairs -> fcfcg_count), normalise
+ * on the device), count the pairs (count_pairs -> fcfcg_count; when the
+ * run's catalogues fit the context's 8 slots, all its counts -- DD, DR,
+ * RR, ... -- go through one CUDA graph, fcfcg_graph_*), normalise
  * and save them (eval_pairs, save_res) or read an existing pair-count file
  * back (OVERWRITE <= 1, check_output); then evaluate CF_ESTIMATOR and write
  * the correlation function, its multipoles or w_p (eval_cf).
@@ -14,7 +16,8 @@
  * Built twice by fcfc_gb300/build.py: as FCFC_2PT_BOX_GPU and, with
  * -DFCFCG_SURVEY, as FCFC_2PT_GPU.
  *
- *   FCFC_2PT_BOX_GPU -c fcfc_2pt_box.conf [--fp64] [--with-mu-one] [-v]
+ *   FCFC_2PT_BOX_GPU -c fcfc_2pt_box.conf [--fp64] [--with-mu-one]
+ *                    [--no-graph] [-v]
  */
 #define _POSIX_C_SOURCE 200809L
 #include <ctype.h>
@@ -38,6 +41,12 @@
 #endif
 
 #define MAXCAT 26
+
+#ifdef FCFCG_SURVEY
+#define CNVT(i) (cnvt[(i)])   /* COORD_CONVERT of catalogue i */
+#else
+#define CNVT(i) 0
+#endif
 
 /* ------------------------------------------------------------------------ */
 /* Configuration: KEY = value | [v1, v2, ...]; '#' comments outside quotes;  */
@@ -236,9 +245,69 @@ static double *read_bins(const char *fname, int *nbin) {
   return e;
 }
 
+/* Read catalogue i (ASCII, FCFC's keys) into a slot of the context. */
+static void load_cat(fcfcg_ctx *ctx, const conf_t *C, int i, int slot,
+    int weighted, int cnvt, const fcfcg_cosmo *cosmo, char label,
+    int verbose) {
+  const char *pos[3] = {conf_str(C, "POSITION", 3 * i),
+                        conf_str(C, "POSITION", 3 * i + 1),
+                        conf_str(C, "POSITION", 3 * i + 2)};
+  const char *fmtr = conf_str(C, "ASCII_FORMATTER", i);
+  if (!fmtr || !*fmtr) die("ASCII_FORMATTER is not set for catalogue %c", label);
+  const char *cm = conf_str(C, "ASCII_COMMENT", i);
+  const char *sel = conf_str(C, "SELECTION", i);
+  double *xyz[3], *w = NULL;
+  size_t n;
+  char err[512];
+  if (cat_read_ascii(conf_str(C, "CATALOG", i), fmtr, pos,
+                     weighted ? conf_str(C, "WEIGHT", i) : NULL,
+                     (sel && *sel) ? sel : NULL, conf_long(C, "ASCII_SKIP", i, 0),
+                     (cm && *cm) ? cm[0] : 0, xyz, &w, &n, err, sizeof err))
+    die("%s", err);
+  int rc;
+  if (cnvt)
+    rc = fcfcg_load_catalog_radecz(ctx, slot, n, xyz[0], xyz[1], xyz[2], w,
+                                   cosmo);
+  else
+    rc = fcfcg_load_catalog(ctx, slot, n, xyz[0], xyz[1], xyz[2], w);
+  check(ctx, rc, "loading a catalogue");
+  free(xyz[0]);
+  free(xyz[1]);
+  free(xyz[2]);
+  free(w);
+  if (verbose) printf("catalogue %c: %zu objects\n", label, n);
+}
+
+/* eval_pairs after the count: double auto counts, normalise, write the
+ * pair-count file (src/fcfc/2pt_box/eval_cf.c:117-167). */
+static void finish_pair(fcfcg_ctx *ctx, const char *fn, int ofmt, int isauto,
+    int wt, int sa, int sb, long ntot, int64_t *icnt, double *wcnt,
+    double *nc) {
+  size_t na, nb;
+  double wa, wbs;
+  fcfcg_catalog_info(ctx, sa, &na, &wa);
+  fcfcg_catalog_info(ctx, sb, &nb, &wbs);
+  const double norm = wt ? fcfcg_norm(isauto, 1, wa, wbs)
+                         : fcfcg_norm(isauto, 0, (double) na, (double) nb);
+  for (long j = 0; j < ntot; j++) {
+    if (wt) {
+      if (isauto) wcnt[j] *= 2;
+      nc[j] = wcnt[j] / norm;
+    } else {
+      if (isauto) icnt[j] *= 2;
+      nc[j] = (double) icnt[j] / norm;
+    }
+  }
+  uint64_t ntr[2] = {na, nb};
+  double wtr[2] = {wa, wbs};
+  check(ctx, fcfcg_write_paircount(ctx, fn, ofmt, isauto, wt, ntr, wtr, norm,
+                                   nc, wt ? NULL : icnt, wt ? wcnt : NULL),
+        "writing a pair-count file");
+}
+
 int main(int argc, char **argv) {
   const char *cfile = NULL;
-  int prec = FCFCG_PREC_FP32_RECHECK, mu_one = 0, verbose = 0;
+  int prec = FCFCG_PREC_FP32_RECHECK, mu_one = 0, verbose = 0, graph = 1;
   for (int i = 1; i < argc; i++) {
     if ((!strcmp(argv[i], "-c") || !strcmp(argv[i], "--conf")) && i + 1 < argc)
       cfile = argv[++i];
@@ -250,8 +319,10 @@ int main(int argc, char **argv) {
       mu_one = 1;
     else if (!strcmp(argv[i], "-v"))
       verbose = 1;
+    else if (!strcmp(argv[i], "--no-graph"))
+      graph = 0;
     else {
-      printf("Usage: %s -c CONFIG [--fp64] [--with-mu-one] [-v]\n"
+      printf("Usage: %s -c CONFIG [--fp64] [--with-mu-one] [--no-graph] [-v]\n"
              "FCFC's configuration keys; the pairs are counted on the GPU.\n",
              PROG);
       return strcmp(argv[i], "-h") && strcmp(argv[i], "--help") ? 1 : 0;
@@ -366,13 +437,14 @@ int main(int argc, char **argv) {
   double *wcnt = malloc(sizeof(double) * ntot);
   double *tmp = malloc(sizeof(double) * ntot);
   char labels[2 * 64 + 1];
-  int loaded[MAXCAT] = {0};
   int weighted[MAXCAT];
   for (int i = 0; i < ncat; i++) {
     const char *w = conf_str(&C, "WEIGHT", i);
     weighted[i] = (conf_len(&C, "WEIGHT") && w && *w);
   }
   if (npair > 64) die("too many pairs");
+  /* the pairs; those with an existing file (OVERWRITE <= 1) are read back */
+  int pia[64], pib[64], todo[64], ntodo = 0;
   for (int k = 0; k < npair; k++) {
     const char *pr = conf_str(&C, "PAIR_COUNT", k);
     const char *fn = conf_str(&C, "PAIR_COUNT_FILE", k);
@@ -385,8 +457,8 @@ int main(int argc, char **argv) {
       if (label[i] == pr[1]) ib = i;
     }
     if (ia < 0 || ib < 0) die("unknown catalogue label in PAIR_COUNT `%s'", pr);
-    const int isauto = (ia == ib);
-    const int wt = weighted[ia] || weighted[ib];
+    pia[k] = ia;
+    pib[k] = ib;
     if (file_exists(fn) && ovw <= 1) {
       int au, ww;
       uint64_t nt[2];
@@ -397,78 +469,95 @@ int main(int argc, char **argv) {
       if (verbose) printf("read %s from `%s'\n", pr, fn);
       continue;
     }
-    const int need[2] = {ia, ib};
-    for (int q = 0; q < 2; q++) {
-      const int i = need[q];
-      if (loaded[i]) continue;
-      const char *pos[3] = {conf_str(&C, "POSITION", 3 * i),
-                            conf_str(&C, "POSITION", 3 * i + 1),
-                            conf_str(&C, "POSITION", 3 * i + 2)};
-      const char *fmtr = conf_str(&C, "ASCII_FORMATTER", i);
-      if (!fmtr || !*fmtr) die("ASCII_FORMATTER is not set for catalogue %c",
-                               label[i]);
-      const char *cm = conf_str(&C, "ASCII_COMMENT", i);
-      const char *sel = conf_str(&C, "SELECTION", i);
-      double *xyz[3], *w = NULL;
-      size_t n;
-      char err[512];
-      if (cat_read_ascii(conf_str(&C, "CATALOG", i), fmtr, pos,
-                         weighted[i] ? conf_str(&C, "WEIGHT", i) : NULL,
-                         (sel && *sel) ? sel : NULL,
-                         conf_long(&C, "ASCII_SKIP", i, 0),
-                         (cm && *cm) ? cm[0] : 0, xyz, &w, &n, err,
-                         sizeof err))
-        die("%s", err);
-#ifdef FCFCG_SURVEY
-      if (cnvt[i])
-        rc = fcfcg_load_catalog_radecz(ctx, i % 8, n, xyz[0], xyz[1], xyz[2],
-                                       w, &cosmo);
-      else
-#endif
-        rc = fcfcg_load_catalog(ctx, i % 8, n, xyz[0], xyz[1], xyz[2], w);
-      check(ctx, rc, "loading a catalogue");
-      free(xyz[0]);
-      free(xyz[1]);
-      free(xyz[2]);
-      free(w);
-      /* slots are per catalogue index modulo 8: drop what this evicts */
-      for (int j = 0; j < ncat; j++)
-        if (j != i && j % 8 == i % 8) loaded[j] = 0;
-      loaded[i] = 1;
-      if (verbose) printf("catalogue %c: %zu objects\n", label[i], n);
-    }
-    if (!loaded[ia] || !loaded[ib])
-      die("catalogues %c and %c share a slot: at most 8 catalogues per pair "
-          "set", label[ia], label[ib]);
-    const int sa = ia % 8, sb = ib % 8;
-    rc = fcfcg_count(ctx, sa, sb, isauto, wt, prec, icnt, wcnt);
-    check(ctx, rc, "counting pairs");
-    size_t na, nb;
-    double wa, wbs;
-    fcfcg_catalog_info(ctx, sa, &na, &wa);
-    fcfcg_catalog_info(ctx, sb, &nb, &wbs);
-    const double norm = wt ? fcfcg_norm(isauto, 1, wa, wbs)
-                           : fcfcg_norm(isauto, 0, (double) na, (double) nb);
-    double *nc = ncnt_all + (size_t) k * ntot;
-    for (long j = 0; j < ntot; j++) {
-      if (wt) {
-        if (isauto) wcnt[j] *= 2;
-        nc[j] = wcnt[j] / norm;
-      } else {
-        if (isauto) icnt[j] *= 2;
-        nc[j] = (double) icnt[j] / norm;
+    todo[ntodo++] = k;
+  }
+  /* the catalogues the counts need, in order of first use */
+  int slot_of[MAXCAT], use[MAXCAT], nuse = 0;
+  for (int i = 0; i < ncat; i++) slot_of[i] = -1;
+  for (int t = 0; t < ntodo; t++) {
+    const int need[2] = {pia[todo[t]], pib[todo[t]]};
+    for (int q = 0; q < 2; q++)
+      if (slot_of[need[q]] < 0) {
+        slot_of[need[q]] = nuse;
+        use[nuse++] = need[q];
       }
+  }
+  const fcfcg_cosmo *cs = NULL;
+#ifdef FCFCG_SURVEY
+  cs = &cosmo;
+#endif
+  if (ntodo > 0 && nuse <= 8 && graph) {
+    /* every count at once: the catalogues in slots 0 .. nuse - 1, the
+     * counts (DD, DR, RR, ...) captured and run as one CUDA graph */
+    for (int u = 0; u < nuse; u++)
+      load_cat(ctx, &C, use[u], u, weighted[use[u]], CNVT(use[u]), cs,
+               label[use[u]], verbose);
+    fcfcg_count_item items[64];
+    int64_t *ic = malloc(sizeof(int64_t) * (size_t) ntodo * ntot);
+    double *wc = malloc(sizeof(double) * (size_t) ntodo * ntot);
+    if (!ic || !wc) die("out of memory");
+    for (int t = 0; t < ntodo; t++) {
+      const int k = todo[t];
+      memset(items + t, 0, sizeof items[t]);
+      items[t].slot_a = slot_of[pia[k]];
+      items[t].slot_b = slot_of[pib[k]];
+      items[t].isauto = (pia[k] == pib[k]);
+      items[t].withwt = weighted[pia[k]] || weighted[pib[k]];
+      if (items[t].withwt) items[t].wcnt = wc + (size_t) t * ntot;
+      else items[t].icnt = ic + (size_t) t * ntot;
     }
-    uint64_t ntr[2] = {na, nb};
-    double wtr[2] = {wa, wbs};
-    check(ctx, fcfcg_write_paircount(ctx, fn, ofmt, isauto, wt, ntr, wtr, norm,
-                                     nc, wt ? NULL : icnt, wt ? wcnt : NULL),
-          "writing a pair-count file");
+    fcfcg_graph *gr = NULL;
+    check(ctx, fcfcg_graph_create(ctx, items, ntodo, prec, &gr),
+          "capturing the counts");
+    check(ctx, fcfcg_graph_run(gr), "counting pairs");
     if (verbose) {
       fcfcg_stats st;
       fcfcg_stats_get(ctx, &st);
-      printf("%s: %llu pairs in range, %.3f ms on the device\n", pr,
-             (unsigned long long) st.in_range, st.ms_total);
+      printf("%d counts in one CUDA graph: %.3f ms on the device\n", ntodo,
+             st.ms_total);
+    }
+    fcfcg_graph_destroy(gr);
+    for (int t = 0; t < ntodo; t++) {
+      const int k = todo[t];
+      finish_pair(ctx, conf_str(&C, "PAIR_COUNT_FILE", k), ofmt,
+                  items[t].isauto, items[t].withwt, items[t].slot_a,
+                  items[t].slot_b, ntot, ic + (size_t) t * ntot,
+                  wc + (size_t) t * ntot, ncnt_all + (size_t) k * ntot);
+    }
+    free(ic);
+    free(wc);
+  } else {
+    /* one count at a time, catalogue i in slot i % 8 */
+    int loaded[MAXCAT] = {0};
+    for (int t = 0; t < ntodo; t++) {
+      const int k = todo[t], ia = pia[k], ib = pib[k];
+      const char *pr = conf_str(&C, "PAIR_COUNT", k);
+      const int need[2] = {ia, ib};
+      for (int q = 0; q < 2; q++) {
+        const int i = need[q];
+        if (loaded[i]) continue;
+        load_cat(ctx, &C, i, i % 8, weighted[i], CNVT(i), cs, label[i],
+                 verbose);
+        /* slots are per catalogue index modulo 8: drop what this evicts */
+        for (int j = 0; j < ncat; j++)
+          if (j != i && j % 8 == i % 8) loaded[j] = 0;
+        loaded[i] = 1;
+      }
+      if (!loaded[ia] || !loaded[ib])
+        die("catalogues %c and %c share a slot: at most 8 catalogues per pair "
+            "set", label[ia], label[ib]);
+      const int sa = ia % 8, sb = ib % 8, isauto = (ia == ib);
+      const int wt = weighted[ia] || weighted[ib];
+      rc = fcfcg_count(ctx, sa, sb, isauto, wt, prec, icnt, wcnt);
+      check(ctx, rc, "counting pairs");
+      if (verbose) {
+        fcfcg_stats st;
+        fcfcg_stats_get(ctx, &st);
+        printf("%s: %llu pairs in range, %.3f ms on the device\n", pr,
+               (unsigned long long) st.in_range, st.ms_total);
+      }
+      finish_pair(ctx, conf_str(&C, "PAIR_COUNT_FILE", k), ofmt, isauto, wt,
+                  sa, sb, ntot, icnt, wcnt, ncnt_all + (size_t) k * ntot);
     }
   }
 

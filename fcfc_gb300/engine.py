@@ -414,6 +414,14 @@ class CountGraph:
         self.pc._check(self.pc.lib.fcfcg_graph_run(self.h))
         return [r.copy() for r in self.out]
 
+    def info(self):
+        """(times captured, kernel launches per run)."""
+        n = C.c_int()
+        k = C.c_uint64()
+        self.pc._check(self.pc.lib.fcfcg_graph_info(self.h, C.byref(n),
+                                                    C.byref(k)))
+        return n.value, k.value
+
     def close(self):
         if self.h and self.pc.h:
             self.pc.lib.fcfcg_graph_destroy(self.h)

@@ -291,9 +291,12 @@ int fcfcg_count(fcfcg_ctx *ctx, int slot_a, int slot_b, int isauto,
  * and the copy of the histogram to pinned host memory, with no host
  * synchronisation in between; fcfcg_graph_run then writes each item's
  * icnt or wcnt exactly as fcfcg_count would.  The graph reads the context's
- * catalogue slots when it runs: reloading a slot (or a count that makes
- * the context reallocate a buffer) makes the next run capture the graph
- * again, transparently.  Items use user slots (0 .. FCFCG_MAX_SLOT - 1).
+ * catalogue slots when it runs, so reloading them (e.g. a new realisation
+ * of the same survey) needs no new graph: each run re-plans the items on
+ * the host and captures the graph again, transparently, only when a plan
+ * changed (catalogue sizes, bounds, weights, the autotuned grid) or the
+ * context reallocated a buffer.  Items use user slots
+ * (0 .. FCFCG_MAX_SLOT - 1).
  * Destroy a graph before its context.  fcfcg_stats after a run describes
  * the last item, with ms_total the whole replay.
  */
@@ -310,6 +313,9 @@ typedef struct fcfcg_graph fcfcg_graph;
 int fcfcg_graph_create(fcfcg_ctx *ctx, const fcfcg_count_item *items,
     int nitem, int precision, fcfcg_graph **graph);
 int fcfcg_graph_run(fcfcg_graph *graph);
+/* How many times the graph was captured, and kernel launches per run. */
+int fcfcg_graph_info(const fcfcg_graph *graph, int *captures,
+    uint64_t *launches);
 void fcfcg_graph_destroy(fcfcg_graph *graph);
 
 /*

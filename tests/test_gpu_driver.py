@@ -47,3 +47,28 @@ def test_driver_matches_upstream_outputs(name, tmp_path):
                                        atol=1e-12)
         else:
             assert open(got).read() == open(ref).read(), fn
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_driver_graph_and_per_count_paths_write_the_same_files(name, tmp_path):
+    """All counts of a run in one CUDA graph (the default) or one fcfcg_count
+    at a time (--no-graph): byte-identical files, weighted ones included
+    (the weighted sums are exact fixed-point sums either way)."""
+    case = Case(name)
+    exe = os.path.join(BIN, "FCFC_2PT_BOX_GPU" if case.box else "FCFC_2PT_GPU")
+    out = {}
+    for mode in ("graph", "no-graph"):
+        d = tmp_path / mode
+        d.mkdir()
+        conf = _write_conf(case, str(d))
+        cmd = [exe, "-c", conf] + (["--with-mu-one"] if case.mu_one else [])
+        if mode == "no-graph":
+            cmd.append("--no-graph")
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        out[mode] = {f: open(os.path.join(d, f), "rb").read()
+                     for f in sorted(os.listdir(d))
+                     if f.endswith((".bin", ".txt"))}
+    assert out["graph"].keys() == out["no-graph"].keys()
+    for f in out["graph"]:
+        assert out["graph"][f] == out["no-graph"][f], f

@@ -84,15 +84,22 @@ def test_box_graph_and_reload():
     pairs = [(0, None, False), (0, 1, True), (1, None, False)]
     g = pc.count_graph(pairs)
     _same(g.run(), _plain(pc, pairs, 0))
-    # reload slot 0 with other data of the same size: the next run captures
-    # the graph again and counts the new catalogue
+    assert g.info()[0] == 1 and g.info()[1] > 0
+    # the same catalogue loaded again plans the same: a replay, no capture
+    pc.load(0, x1, w1)
+    _same(g.run(), _plain(pc, pairs, 0))
+    assert g.info()[0] == 1
+    # other data of the same size: counted correctly (captured again only
+    # when the plan differs)
     x3 = synth.uniform_box(len(x1), L, seed=8)
     pc.load(0, x3, w1[::-1].copy())
     _same(g.run(), _plain(pc, pairs, 0))
-    # and with a larger catalogue (buffers reallocated)
+    # a larger catalogue (buffers reallocated): captured again
     x4 = synth.neyman_scott(900, L, 20.0, 4.0, seed=9)
     pc.load(0, x4, synth.lognormal_weights(len(x4), 0.3, seed=10))
+    n0 = g.info()[0]
     got = g.run()
+    assert g.info()[0] == n0 + 1
     _same(got, _plain(pc, pairs, 0))
     assert got[0].sum() > 0
     # an empty catalogue: zeros, and the other items still count
