@@ -104,7 +104,7 @@ def build_drivers():
         jobs.append(["gcc", "-O2", "-std=c11", "-ffp-contract=off",
                      "-fno-fast-math", "-Wall", *defs, "-o", out, *src,
                      "-L", LIBDIR, "-lfcfcg", "-Wl,-rpath,$ORIGIN/../lib",
-                     "-lm"])
+                     "-lm", "-lpthread"])
     with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         list(ex.map(_run, jobs))
 
