@@ -30,6 +30,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import shutil
 import subprocess
 import sys
 import threading
@@ -638,6 +639,100 @@ def cpu_baseline_sample(x, w, box):
                       (len(x), box, n_in, dt)}
 
 
+def run_cli(args, rank, world, local, dist):
+    """FCFC's command line flow end to end: the 2e6-object Neyman-Scott box
+    written as an ASCII catalogue (x y z w, %.17g), then FCFC_2PT_BOX_GPU run
+    on it twice per step -- weighted DD in (s, mu) with xi and multipoles,
+    and in (s_perp, pi) with w_p -- each a fresh process that reads the file,
+    counts and writes FCFC's files.  Wall time per step, process start-up
+    and device initialisation included."""
+    import re
+    import subprocess
+    import tempfile
+    box = BOX / 2 if args.small else BOX
+    npar = 20000 // 8 if args.small else 20000
+    x, w = workload(box=box, nparent=npar, seed=1 + rank)
+    n = len(x)
+    d = tempfile.mkdtemp(prefix="fcfcg_cli_")
+    cat = os.path.join(d, "ns.txt")
+    np.savetxt(cat, np.column_stack([x, w]), fmt="%.17g")
+    np.savetxt(os.path.join(d, "sbin.txt"),
+               np.column_stack([LOGBINS[:-1], LOGBINS[1:]]), fmt="%.17g")
+    common = ["CATALOG = [%s]" % cat, "CATALOG_LABEL = [D]",
+              'ASCII_FORMATTER = ["%lf %lf %lf %lf"]',
+              "POSITION = [$1, $2, $3]", "WEIGHT = [$4]",
+              "BOX_SIZE = %.17g" % box, "DATA_STRUCT = 0", "OVERWRITE = 2",
+              "PAIR_COUNT = [DD]", 'CF_ESTIMATOR = ["DD / @@ - 1"]']
+    confs = {
+        "smu": common + ["BINNING_SCHEME = 1", "SEP_BIN_MIN = 0",
+                         "SEP_BIN_MAX = 200", "SEP_BIN_SIZE = 5",
+                         "MU_BIN_NUM = 100",
+                         "PAIR_COUNT_FILE = [%s]" % os.path.join(d, "dd_smu.bin"),
+                         "CF_OUTPUT_FILE = [%s]" % os.path.join(d, "xi_smu.txt"),
+                         "MULTIPOLE = [0, 2, 4]",
+                         "MULTIPOLE_FILE = [%s]" % os.path.join(d, "mp.txt")],
+        "spi": common + ["BINNING_SCHEME = 2",
+                         "SEP_BIN_FILE = %s" % os.path.join(d, "sbin.txt"),
+                         "PI_BIN_MIN = 0", "PI_BIN_MAX = 40", "PI_BIN_SIZE = 1",
+                         "PAIR_COUNT_FILE = [%s]" % os.path.join(d, "dd_spi.bin"),
+                         "CF_OUTPUT_FILE = [%s]" % os.path.join(d, "xi_spi.txt"),
+                         "PROJECTED_CF = T",
+                         "PROJECTED_FILE = [%s]" % os.path.join(d, "wp.txt")],
+    }
+    for k, lines in confs.items():
+        open(os.path.join(d, k + ".conf"), "w").write("\n".join(lines) + "\n")
+    exe = os.path.join(os.path.dirname(os.path.abspath(__file__)), "fcfc_gb300",
+                       "bin", "FCFC_2PT_BOX_GPU")
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES=str(local))
+
+    def step():
+        reads = []
+        for k in ("smu", "spi"):
+            r = subprocess.run([exe, "-c", os.path.join(d, k + ".conf"), "-v"],
+                               capture_output=True, text=True, env=env)
+            if r.returncode:
+                raise RuntimeError(r.stdout + r.stderr)
+            reads += [float(v) for v in re.findall(r"read ([0-9.]+) s", r.stdout)]
+        return reads
+    # in-range pairs of the two runs (unweighted counts through the library)
+    import fcfc_gb300 as fg
+    pairs = 0
+    for kw in (dict(bintype=fg.BIN_SMU, smin=0, smax=200, ds=5, nmu=100),
+               dict(bintype=fg.BIN_SPI, sedges=LOGBINS, pmin=0, pmax=40, dpi=1)):
+        pc = fg.PairCounter("box", box=box, device=local, **kw)
+        pc.load(0, x)
+        pairs += int(pc.count_pairs(0).sum())
+        pc.close()
+    for _ in range(max(args.warmup, 1)):
+        step()
+    t0 = time.perf_counter()
+    reads = []
+    for _ in range(args.steps):
+        reads += step()
+    wall = (time.perf_counter() - t0) / args.steps
+    ms_step = max_over_ranks(wall * 1e3, dist)
+    out = {"metric": METRIC + " (command line, end to end)",
+           "value": pairs * world / (ms_step * 1e-3), "unit": UNIT,
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+f64-recheck", "data": "synthetic",
+           "config": {"workload": "cli_ns_box_%d" % n, "n_points": n,
+                      "catalogue_bytes": os.path.getsize(cat),
+                      "runs_per_step": "FCFC_2PT_BOX_GPU (s,mu) + (s_perp,pi)",
+                      "pairs_per_step": pairs,
+                      "ascii_read_s_mean": float(np.mean(reads)),
+                      "parallelism": "replicas" if world > 1 else "1 GPU"},
+           "e2e": {"value": pairs * world / (ms_step * 1e-3), "unit": UNIT,
+                   "ms_per_step": ms_step,
+                   "h2d_bytes_per_step": 2 * n * 32, "d2h_bytes_per_step": 0}}
+    if dist:
+        dist.barrier()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    shutil.rmtree(d, ignore_errors=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -648,10 +743,12 @@ def main():
                     help="quarter-size box (for profiler captures)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="ns_box_2e6",
-                    choices=["ns_box_2e6", "mocks256", "survey", "adjoint"],
+                    choices=["ns_box_2e6", "mocks256", "survey", "adjoint",
+                             "cli"],
                     help="mocks256: 256 mock boxes in one persistent launch; "
                          "survey: DD/DR/RR of 1e6 data and 1e7 randoms; "
-                         "adjoint: dL/dw of a Landy-Szalay loss")
+                         "adjoint: dL/dw of a Landy-Szalay loss; "
+                         "cli: FCFC_2PT_BOX_GPU end to end on an ASCII file")
     args = ap.parse_args()
     rank, world, local = env_rank()
     dist = None
@@ -670,6 +767,8 @@ def main():
         return run_survey(args, rank, world, local, dist)
     if args.workload == "adjoint":
         return run_adjoint(args, rank, world, local, dist)
+    if args.workload == "cli":
+        return run_cli(args, rank, world, local, dist)
     import torch
     import fcfc_gb300 as fg
     torch.cuda.set_device(local)

@@ -28,6 +28,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <sys/stat.h>
+#include <time.h>
 
 #include "../../../include/fcfcg.h"
 #include "catalog.h"
@@ -259,11 +260,14 @@ static void load_cat(fcfcg_ctx *ctx, const conf_t *C, int i, int slot,
   double *xyz[3], *w = NULL;
   size_t n;
   char err[512];
+  struct timespec t0, t1, t2;
+  clock_gettime(CLOCK_MONOTONIC, &t0);
   if (cat_read_ascii(conf_str(C, "CATALOG", i), fmtr, pos,
                      weighted ? conf_str(C, "WEIGHT", i) : NULL,
                      (sel && *sel) ? sel : NULL, conf_long(C, "ASCII_SKIP", i, 0),
                      (cm && *cm) ? cm[0] : 0, xyz, &w, &n, err, sizeof err))
     die("%s", err);
+  clock_gettime(CLOCK_MONOTONIC, &t1);
   int rc;
   if (cnvt)
     rc = fcfcg_load_catalog_radecz(ctx, slot, n, xyz[0], xyz[1], xyz[2], w,
@@ -275,7 +279,13 @@ static void load_cat(fcfcg_ctx *ctx, const conf_t *C, int i, int slot,
   free(xyz[1]);
   free(xyz[2]);
   free(w);
-  if (verbose) printf("catalogue %c: %zu objects\n", label, n);
+  clock_gettime(CLOCK_MONOTONIC, &t2);
+  if (verbose)
+    printf("catalogue %c: %zu objects (read %.3f s, to the device %.3f s)\n",
+           label, n, (double) (t1.tv_sec - t0.tv_sec) +
+                         1e-9 * (double) (t1.tv_nsec - t0.tv_nsec),
+           (double) (t2.tv_sec - t1.tv_sec) +
+               1e-9 * (double) (t2.tv_nsec - t1.tv_nsec));
 }
 
 /* eval_pairs after the count: double auto counts, normalise, write the

@@ -166,9 +166,11 @@ def read_bins_file(path):
 
 def run(conf: dict, geometry: str = "box", device: int = -1,
         precision: int = capi.PREC_FP32_RECHECK, verbose: bool = False,
-        with_mu_one: bool = False):
+        with_mu_one: bool = False, graph: bool = True):
     """Run one FCFC job.  Returns a dict with counts, xi, multipoles, wp.
-    with_mu_one: behave as FCFC built with -DWITH_MU_ONE."""
+    with_mu_one: behave as FCFC built with -DWITH_MU_ONE.  graph: when the
+    catalogues fit the 8 slots, count every pair through one CUDA graph
+    (the same counts as one at a time)."""
     box = geometry == "box"
     files = _arr(conf, "CATALOG")
     ncat = len(files)
@@ -222,62 +224,106 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
                       dpi=float(conf["PI_BIN_SIZE"]))
 
     pc = PairCounter(with_mu_one=with_mu_one, **kw)
-    # catalogues, loaded on first use
-    loaded = {}
 
-    def slot_of(lab):
-        i = labels.index(lab)
-        if i not in loaded:
-            p3 = pos[3 * i: 3 * i + 3]
-            w = wts[i] if wts and wts[i] not in (None, "", "''", '""') else None
-            x, ww = read_catalog(files[i], fmtr[i] if fmtr else None, p3, w,
-                                 skip[i], cmt[i] if cmt else None,
-                                 sel[i] if sel and sel[i] not in ("", "''", '""')
-                                 else None)
-            if cnvt[i]:
-                pc.load_radecz(i, x, ww, **cosmo)
-            else:
-                pc.load(i, x, ww)
-            loaded[i] = (len(x), ww is not None)
-        return i
+    def load_cat(i, slot):
+        p3 = pos[3 * i: 3 * i + 3]
+        w = wts[i] if wts and wts[i] not in (None, "", "''", '""') else None
+        x, ww = read_catalog(files[i], fmtr[i] if fmtr else None, p3, w,
+                             skip[i], cmt[i] if cmt else None,
+                             sel[i] if sel and sel[i] not in ("", "''", '""')
+                             else None)
+        if cnvt[i]:
+            pc.load_radecz(slot, x, ww, **cosmo)
+        else:
+            pc.load(slot, x, ww)
 
     weighted_cat = {}
     for i, lab in enumerate(labels):
         w = wts[i] if wts else None
         weighted_cat[lab] = w not in (None, "", "''", '""')
 
+    # pairs with an existing file (OVERWRITE <= 1) are read back; the others
+    # are counted
+    done, todo = {}, []
+    for k, pair in enumerate(pairs):
+        if os.path.exists(pcout[k]) and ovw <= 1:
+            done[k] = pc.read_paircount(pcout[k])
+        else:
+            todo.append(k)
+    need = []            # catalogues the counts use, in order of first use
+    for k in todo:
+        for lab in pairs[k][:2]:
+            i = labels.index(lab)
+            if i not in need:
+                need.append(i)
+    counts, slots = {}, {}
+    if todo and len(need) <= 8 and graph:
+        # every count at once: DD, DR, RR, ... replayed from one CUDA graph
+        slot = {i: s for s, i in enumerate(need)}
+        for i in need:
+            load_cat(i, slot[i])
+        items = []
+        for k in todo:
+            a, bl = pairs[k][0], pairs[k][1]
+            sa, sb = slot[labels.index(a)], slot[labels.index(bl)]
+            slots[k] = (sa, sb)
+            items.append((sa, None if a == bl else sb,
+                          weighted_cat[a] or weighted_cat[bl]))
+        g = pc.count_graph(items, precision=precision)
+        try:
+            for k, c in zip(todo, g.run()):
+                counts[k] = c
+        finally:
+            g.close()
+    else:
+        # one count at a time, catalogue i in slot i % 8
+        loaded = {}
+        for k in todo:
+            a, bl = pairs[k][0], pairs[k][1]
+            for lab in (a, bl):
+                i = labels.index(lab)
+                if loaded.get(i % 8) != i:
+                    load_cat(i, i % 8)
+                    loaded[i % 8] = i
+            ia, ib = labels.index(a), labels.index(bl)
+            if loaded.get(ia % 8) != ia or loaded.get(ib % 8) != ib:
+                raise FCFCGError(capi.ERR_CFG, "catalogues %s and %s share a "
+                                 "slot: at most 8 catalogues per pair set"
+                                 % (a, bl))
+            sa, sb = ia % 8, ib % 8
+            slots[k] = (sa, sb)
+            counts[k] = pc.count_pairs(sa, None if a == bl else sb,
+                                       weighted=weighted_cat[a] or
+                                       weighted_cat[bl], precision=precision)
+
     ncnt_all = []
     out = {"counts": {}, "norm": {}}
     for k, pair in enumerate(pairs):
-        a, bl = pair[0], pair[1]
-        isauto = a == bl
-        weighted = weighted_cat[a] or weighted_cat[bl]
-        fn = pcout[k]
-        if os.path.exists(fn) and ovw <= 1:
-            r = pc.read_paircount(fn)
+        if k in done:
+            r = done[k]
             ncnt_all.append(r["ncnt"])
             out["counts"][pair] = r["cnt"]
             out["norm"][pair] = r["norm"]
             continue
-        sa = slot_of(a)
-        sb = slot_of(bl)
-        cnt = pc.count_pairs(sa, None if isauto else sb, weighted=weighted,
-                             precision=precision)
+        a, bl = pair[0], pair[1]
+        isauto = a == bl
+        weighted = weighted_cat[a] or weighted_cat[bl]
+        sa, sb = slots[k]
         na, wa = pc.catalog_info(sa)
         nb, wb = pc.catalog_info(sb)
         if weighted:
             n1, n2 = wa, wb
         else:
             n1, n2 = float(na), float(nb)
-        cnt2, norm, ncnt = pc.normalise(cnt, isauto, weighted, n1, n2)
-        pc.write_paircount(fn, ofmt, isauto, weighted,
+        cnt2, norm, ncnt = pc.normalise(counts[k], isauto, weighted, n1, n2)
+        pc.write_paircount(pcout[k], ofmt, isauto, weighted,
                            [na] if isauto else [na, nb],
                            [wa] if isauto else [wa, wb], norm, ncnt, cnt2)
         ncnt_all.append(ncnt)
         out["counts"][pair] = cnt2
         out["norm"][pair] = norm
         if verbose:
-            print("counted %s: %s" % (pair, pc.stats()))
+            print("counted %s" % pair)
 
     rr = pc.analytic_rr() if box else None
     if est:
@@ -317,12 +363,14 @@ def main(argv=None):
     ap.add_argument("--with-mu-one", action="store_true",
                     help="mu = 1 in the last mu bin, as FCFC built with "
                          "-DWITH_MU_ONE")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="one count per pair instead of one CUDA graph")
     ap.add_argument("-v", "--verbose", action="store_true")
     a = ap.parse_args(argv)
     conf = parse_conf(open(a.conf).read())
     run(conf, "survey" if a.survey else "box",
         precision=capi.PREC_FP64 if a.fp64 else capi.PREC_FP32_RECHECK,
-        verbose=a.verbose, with_mu_one=a.with_mu_one)
+        verbose=a.verbose, with_mu_one=a.with_mu_one, graph=not a.no_graph)
     return 0
 
 

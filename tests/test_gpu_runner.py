@@ -135,3 +135,24 @@ def test_resume_reads_existing_counts(tmp_path):
     assert open(str(tmp_path / "DD.bin"), "rb").read() == first
     assert os.path.exists(str(tmp_path / "xi.txt"))
     np.testing.assert_array_equal(out["counts"]["DD"], case.pcfile("DD").cnt)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_run_graph_and_per_count_paths_write_the_same_files(name, tmp_path):
+    """Every count through one CUDA graph (default) or one count_pairs per
+    pair: byte-identical files, weighted ones included."""
+    from fcfc_gb300 import runner
+    case = Case(name)
+    out = {}
+    for graph in (True, False):
+        d = tmp_path / ("graph" if graph else "plain")
+        d.mkdir()
+        conf = runner.parse_conf(open(_write_conf(case, str(d))).read())
+        runner.run(conf, "box" if case.box else "survey",
+                   with_mu_one=case.mu_one, graph=graph)
+        out[graph] = {f: open(os.path.join(d, f), "rb").read()
+                      for f in sorted(os.listdir(d))
+                      if not f.endswith(".conf")}   # holds the directory
+    assert out[True].keys() == out[False].keys()
+    for f in out[True]:
+        assert out[True][f] == out[False][f], f
