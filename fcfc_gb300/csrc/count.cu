@@ -723,6 +723,7 @@ __global__ void __launch_bounds__(CT32_THREADS, BIN == FCFCG_BIN_SMU ? 3 : 4)
 k_count32(const fcfcg_launch L) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t sh_chunk;
+  __shared__ uint32_t sh_blk;   /* next neighbour block of the chunk */
   __shared__ MockSh sh_mock;   /* batched launch: the current catalogue */
   int cur = -1;
   uint16_t *fs = (uint16_t *) smem;
@@ -787,13 +788,15 @@ k_count32(const fcfcg_launch L) {
   const int2 *__restrict__ Bwq = (const int2 *) L.B.wq;
   const int4 *__restrict__ sten = (const int4 *) L.sten;
   const float4 *__restrict__ stD = (const float4 *) L.stenD;
-  const int nwarp = CT32_THREADS / 32;
   unsigned long long n_cand = 0, n_in64 = 0, n_q64 = 0, n_inline = 0;
   const uint32_t nchunk = L.nchunk_dev ? __ldg(L.nchunk_dev) : L.nchunk;
 
   for (;;) {
     __syncthreads();    /* the previous chunk is done with a / pre / bst */
-    if (threadIdx.x == 0) sh_chunk = atomicAdd(L.chunk_head, 1u);
+    if (threadIdx.x == 0) {
+      sh_chunk = atomicAdd(L.chunk_head, 1u);
+      sh_blk = 0;
+    }
     __syncthreads();
     const uint32_t c = sh_chunk;
     if (c >= nchunk) break;
@@ -891,8 +894,14 @@ k_count32(const fcfcg_launch L) {
     if (warp == 0 && lane == 0) n_cand += (unsigned long long) m * total;
     uint32_t n_in = 0, n_q = 0;
 
-    for (uint32_t base = (uint32_t) warp * 32; base < total;
-         base += (uint32_t) nwarp * 32) {
+    /* the warps take the chunk's blocks of 32 neighbour points as they
+     * become free (their work varies), so they reach the next chunk's
+     * barrier together */
+    for (;;) {
+      uint32_t blk = 0;
+      if (lane == 0) blk = atomicAdd(&sh_blk, 1u);
+      const uint32_t base = __shfl_sync(FULLMASK, blk, 0) * 32u;
+      if (base >= total) break;
       const uint32_t p = base + (uint32_t) lane;
       float bx = 0.f, by = 0.f, bz = 0.f;
       int ilim = 0;
