@@ -22,6 +22,7 @@ typedef struct {
   double *x, *y, *z, *s, *w;       /* rescaled FP64 (device) */
   double xabs, s2abs;              /* max |coordinate|, max |x|^2 (host) */
   double bmin[3], bmax[3];         /* bounding box (rescaled) */
+  double vol;                      /* survey: occupied volume (rescaled) */
   /* sorted copy for the current grid */
   size_t scap;
   float *l4;
@@ -326,6 +327,61 @@ int fcfcg_set_cells_per_smax(fcfcg_ctx *c, int k) {
 /* ------------------------------------------------------------------------ */
 /* Catalogues.                                                               */
 
+/*
+ * The volume a survey catalogue occupies (its bounding box can be several
+ * times larger): the cells of a coarse grid over the box, sized to hold
+ * ~2 objects at the box's mean density, that hold an object.  With M cells
+ * of the footprint and n objects spread over them, K = M (1 - exp(-n / M))
+ * cells are occupied on average; M is solved for from the count K.
+ */
+static int occupied_volume(fcfcg_ctx *c, slot_t *s) {
+  double ext[3], V = 1;
+  for (int k = 0; k < 3; k++) {
+    ext[k] = fmax(s->bmax[k] - s->bmin[k], 1e-9 * fmax(1.0, s->xabs));
+    V *= ext[k];
+  }
+  double cell = cbrt(2.0 * V / (double) s->n);
+  int dim[3];
+  size_t tot;
+  for (;;) {
+    tot = 1;
+    for (int k = 0; k < 3; k++) {
+      double d = ceil(ext[k] / cell);
+      dim[k] = (int) (d < 1 ? 1 : (d > 4096 ? 4096 : d));
+      tot *= (size_t) dim[k];
+    }
+    if (tot <= ((size_t) 1 << 24)) break;
+    cell *= 1.26;
+  }
+  double inv[3];
+  for (int k = 0; k < 3; k++) inv[k] = dim[k] / ext[k];
+  const size_t nw = (tot + 31) / 32;
+  GROW(c->cfill, c->cfill_cap, sizeof(uint32_t) * nw);
+  unsigned long long *dcount = c->d_stats + 6;
+  CKK(fcfcg_k_occupancy(c->stream, s->n, s->x, s->y, s->z, s->bmin, dim, inv,
+                        c->cfill, nw, dcount));
+  c->launches += 2;
+  unsigned long long K = 0;
+  CK(cudaMemcpyAsync(&K, dcount, sizeof K, cudaMemcpyDeviceToHost,
+                     c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  const double n = (double) s->n, T = (double) tot;
+  double M;
+  if (T * -expm1(-n / T) <= (double) K) {
+    M = T;
+  } else {
+    double lo = (double) K, hi = T;
+    for (int it = 0; it < 100; it++) {
+      const double mid = 0.5 * (lo + hi);
+      if (mid * -expm1(-n / mid) < (double) K) lo = mid;
+      else hi = mid;
+    }
+    M = 0.5 * (lo + hi);
+  }
+  s->vol = M * (V / T);
+  return FCFCG_OK;
+}
+
 static int load_common(fcfcg_ctx *c, int slot, size_t n, const double *x,
     const double *y, const double *z, const double *w, int on_device,
     const fcfcg_cosmo *cosmo) {
@@ -456,6 +512,8 @@ static int load_common(fcfcg_ctx *c, int slot, size_t n, const double *x,
   /* the sum of the weights, summed on the device in a fixed order (FCFC
    * sums with an OpenMP reduction, whose order varies with the threads) */
   s->sumw = w ? wsum : (double) n;
+  s->vol = 0;
+  if (survey && n) return occupied_volume(c, s);
   return FCFCG_OK;
 }
 
@@ -535,18 +593,12 @@ static int tune_key(double density, const double reach[3]) {
 
 static double box_volume(const double v[3]) { return v[0] * v[1] * v[2]; }
 
+/* Cells per maximum separation: about 24 objects of the chunk side per
+ * cell, 1 to 8.  (Timed over k = 1..8 on boxes and surveys of 1e5 to 1e7
+ * objects, the fastest refinement held 15 to 50 objects per cell.) */
 static int pick_k(double density, double reach) {
-  /* cells of at least ~48 points where possible, between 1 and 4 cells per
-   * maximum separation */
-  int k = 1;
-  for (int t = 4; t >= 1; t--) {
-    double cw = reach / t;
-    if (density * cw * cw * cw >= 48.0) {
-      k = t;
-      break;
-    }
-  }
-  return k;
+  const int k = (int) floor(reach * cbrt(density / 24.0) + 0.5);
+  return k < 1 ? 1 : (k > 8 ? 8 : k);
 }
 
 /* Largest separation that counts, per axis and in 3D (rescaled). */
@@ -592,7 +644,9 @@ static int grid_setup(fcfcg_ctx *c, grid_t *g, const slot_t *A,
   }
   double ext[3] = {hi[0] - lo[0], hi[1] - lo[1], hi[2] - lo[2]};
   double vol = box_volume(ext);
-  double density = (double) B->n / (vol > 0 ? vol : 1);
+  /* density of the chunk side, in the volume it occupies */
+  if (!box && A->vol > 0 && A->vol < vol) vol = A->vol;
+  double density = (double) A->n / (vol > 0 ? vol : 1);
   g->key = tune_key(density, g->reach);
   int k = c->kcell;
   if (!k) k = (c->tuned_k && c->tuned_key == g->key) ? c->tuned_k
@@ -1523,7 +1577,8 @@ int fcfcg_autotune(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
   const int saved = c->kcell;
   int bk = 0, key = 0, rc = FCFCG_OK;
   double bms = 1e300;
-  for (int k = 1; k <= 5; k++) {
+  /* k = 1..8, until two refinements in a row are slower than the best */
+  for (int k = 1; k <= 8 && (!bk || k <= bk + 2); k++) {
     c->kcell = k;
     double ms = 0;
     for (int rep = 0; rep < 2 && rc == FCFCG_OK; rep++) {
@@ -2143,7 +2198,8 @@ int fcfcg_autotune_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs,
   const int saved = c->kcell;
   int bk = 0, rc = FCFCG_OK;
   double bms = 1e300;
-  for (int k = 1; k <= 5 && rc == FCFCG_OK; k++) {
+  /* k = 1..8, until two refinements in a row are slower than the best */
+  for (int k = 1; k <= 8 && rc == FCFCG_OK && (!bk || k <= bk + 2); k++) {
     c->kcell = k;
     double ms = 0;
     for (int rep = 0; rep < 2 && rc == FCFCG_OK; rep++) {

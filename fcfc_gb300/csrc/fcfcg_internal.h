@@ -207,6 +207,12 @@ int fcfcg_k_bbox(void *stream, size_t n, const double *x, const double *y,
     const double *z, unsigned long long *bits6);
 int fcfcg_k_count(void *stream, const fcfcg_launch *L, int precision,
     int nsm, size_t *smem_used);
+/* Bits of the coarse cells (dim, cells of 1 / inv_cell from lo) that hold
+ * an object, and their number (count). */
+int fcfcg_k_occupancy(void *stream, size_t n, const double *x,
+    const double *y, const double *z, const double lo[3], const int dim[3],
+    const double inv_cell[3], uint32_t *bits, size_t nw,
+    unsigned long long *count);
 /* FP64 recheck of the queued pairs; the kernels read the queue length on
  * the device, nq_bound (>= it) only sizes the grid. */
 int fcfcg_k_recheck(void *stream, const fcfcg_launch *L, uint32_t nq_bound);

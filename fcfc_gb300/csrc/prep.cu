@@ -444,6 +444,54 @@ extern "C" int fcfcg_k_chunks(void *stream, const uint32_t *cstart,
   return 0;
 }
 
+/* Occupancy of a coarse grid over a catalogue's bounding box: one bit per
+ * cell that holds an object (the occupied-volume estimate of a survey). */
+__global__ void k_occupy(size_t n, const double *__restrict__ x,
+    const double *__restrict__ y, const double *__restrict__ z, double lox,
+    double loy, double loz, double icx, double icy, double icz, int nx,
+    int ny, int nz, uint32_t *__restrict__ bits) {
+  for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n;
+       i += (size_t) gridDim.x * blockDim.x) {
+    int cx = (int) floor((x[i] - lox) * icx);
+    int cy = (int) floor((y[i] - loy) * icy);
+    int cz = (int) floor((z[i] - loz) * icz);
+    cx = cx < 0 ? 0 : (cx >= nx ? nx - 1 : cx);
+    cy = cy < 0 ? 0 : (cy >= ny ? ny - 1 : cy);
+    cz = cz < 0 ? 0 : (cz >= nz ? nz - 1 : cz);
+    const size_t c = ((size_t) cz * ny + cy) * nx + cx;
+    atomicOr(bits + (c >> 5), 1u << (c & 31));
+  }
+}
+
+__global__ void k_popc(size_t nw, const uint32_t *__restrict__ bits,
+    unsigned long long *count) {
+  unsigned long long t = 0;
+  for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < nw;
+       i += (size_t) gridDim.x * blockDim.x)
+    t += (unsigned long long) __popc(bits[i]);
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  if ((threadIdx.x & 31) == 0 && t) atomicAdd(count, t);
+}
+
+extern "C" int fcfcg_k_occupancy(void *stream, size_t n, const double *x,
+    const double *y, const double *z, const double lo[3], const int dim[3],
+    const double inv_cell[3], uint32_t *bits, size_t nw,
+    unsigned long long *count) {
+  cudaStream_t st = (cudaStream_t) stream;
+  cudaError_t e = cudaMemsetAsync(bits, 0, sizeof(uint32_t) * nw, st);
+  if (!e) e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), st);
+  if (e) return (int) e;
+  if (n) {
+    k_occupy<<<grid_for(n, PREP_THREADS), PREP_THREADS, 0, st>>>(
+        n, x, y, z, lo[0], lo[1], lo[2], inv_cell[0], inv_cell[1],
+        inv_cell[2], dim[0], dim[1], dim[2], bits);
+    if ((e = cudaGetLastError())) return (int) e;
+  }
+  k_popc<<<grid_for(nw, PREP_THREADS), PREP_THREADS, 0, st>>>(nw, bits,
+                                                               count);
+  return (int) cudaGetLastError();
+}
+
 __global__ void k_unsort(size_t n, const uint32_t *__restrict__ sid,
     const double *__restrict__ in, double *__restrict__ out) {
   for (size_t p = blockIdx.x * (size_t) blockDim.x + threadIdx.x; p < n;

@@ -182,7 +182,7 @@ class PairCounter:
         self._check(self.lib.fcfcg_set_cells_per_smax(self.h, int(k)))
 
     def autotune(self, a: int, b: int | None = None, weighted=False):
-        """Time the FP32 count at 1..5 cells per maximum separation and keep
+        """Time the FP32 count at 1..8 cells per maximum separation and keep
         the fastest for catalogues of this density; returns (k, ms)."""
         isauto = b is None or b == a
         k = C.c_int()

@@ -204,8 +204,9 @@ typedef struct {
 int fcfcg_count_batch(fcfcg_ctx *ctx, fcfcg_job *jobs, int njobs,
     int withwt, int precision, int on_device);
 
-/* Time fcfcg_count_batch at 1..5 cells per maximum separation and keep the
- * fastest for batches of this mean density (as fcfcg_autotune). */
+/* Time fcfcg_count_batch at 1..8 cells per maximum separation (stopping
+ * two past the fastest) and keep the fastest for batches of this mean
+ * density (as fcfcg_autotune). */
 int fcfcg_autotune_batch(fcfcg_ctx *ctx, fcfcg_job *jobs, int njobs,
     int withwt, int on_device, int *best_k, double *best_ms);
 
@@ -342,15 +343,19 @@ int fcfcg_adjoint(fcfcg_ctx *ctx, int slot_a, int slot_b, int isauto,
 
 int fcfcg_stats_get(const fcfcg_ctx *ctx, fcfcg_stats *out);
 
-/* Grid refinement: cells per maximum separation (0 = automatic). */
+/* Grid refinement: cells per maximum separation, 1..8 (0 = automatic:
+ * about 24 objects of the first catalogue per cell, counted in the volume
+ * it occupies -- for a survey estimated at load time, not its bounding
+ * box). */
 int fcfcg_set_cells_per_smax(fcfcg_ctx *ctx, int k);
 
 /*
  * Autotune the grid refinement for this binning and catalogue pair: times
- * the FP32 count at 1..5 cells per maximum separation and keeps the fastest
- * for catalogues of the same number density (key: log2 of the mean number
- * of objects within the maximum separation box).  Later automatic counts of
- * matching density use it.
+ * the FP32 count at 1..8 cells per maximum separation (stopping two past
+ * the fastest) and keeps the fastest for catalogues of the same number
+ * density (key: log2 of the mean number of objects of the first catalogue
+ * within the maximum separation box).  Later automatic counts of matching
+ * density use it.
  */
 int fcfcg_autotune(fcfcg_ctx *ctx, int slot_a, int slot_b, int isauto,
     int withwt, int *best_k, double *best_ms);
