@@ -235,10 +235,15 @@ class PairCounter:
                 if weighted:
                     J.w = C.cast(C.c_void_p(weights[j]), capi._dp)
             else:
-                a = np.asarray(cats[j], np.float64)
-                cols = [np.ascontiguousarray(a[:, k]) for k in range(3)]
+                c = cats[j]
+                if isinstance(c, (tuple, list)) and len(c) == 3:
+                    # columns x, y, z already (no copy when contiguous FP64)
+                    cols = [np.ascontiguousarray(v, np.float64) for v in c]
+                else:
+                    a = np.asarray(c, np.float64)
+                    cols = [np.ascontiguousarray(a[:, k]) for k in range(3)]
                 keep += cols
-                J.n = len(a)
+                J.n = len(cols[0])
                 J.x, J.y, J.z = (c.ctypes.data_as(capi._dp) for c in cols)
                 if weighted:
                     w = np.ascontiguousarray(weights[j], np.float64)
@@ -257,8 +262,9 @@ class PairCounter:
                     precision=PREC_FP32_RECHECK, on_device=False):
         """DD counts (undoubled) of many periodic boxes in one launch.
 
-        cats: N_j x 3 host arrays, or with on_device (x_ptr, y_ptr, z_ptr, n)
-        tuples of device FP64 pointers; boxes: BOX_SIZE per catalogue;
+        cats: N_j x 3 host arrays or (x, y, z) host column arrays, or with
+        on_device (x_ptr, y_ptr, z_ptr, n) tuples of device FP64 pointers;
+        boxes: BOX_SIZE per catalogue;
         weights: per-catalogue arrays (device pointers with on_device).
         Returns (counts, status, sumw) lists."""
         jobs, keep, outs = self._jobs(cats, boxes, weights, weighted, on_device)

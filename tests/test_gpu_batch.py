@@ -125,3 +125,16 @@ def test_batch_autotune_keeps_counts():
     assert pc.stats()["cells_per_smax"] == k
     for a, b in zip(ref, got):
         assert np.array_equal(a, b)
+
+
+def test_batch_accepts_column_arrays():
+    """Host catalogues given as (x, y, z) columns count as the N x 3 arrays."""
+    import fcfc_gb300 as fg
+    cats, boxes, wts = _mocks(6, seed=77)
+    pc = fg.PairCounter("box", **dict(CONFIGS[0], box=max(boxes)))
+    a, st_a, _ = pc.count_batch(cats, boxes, wts, weighted=True)
+    cols = [tuple(np.ascontiguousarray(c[:, k]) for k in range(3)) for c in cats]
+    b, st_b, _ = pc.count_batch(cols, boxes, wts, weighted=True)
+    assert list(st_a) == list(st_b)
+    for x, y in zip(a, b):
+        np.testing.assert_array_equal(x, y)
