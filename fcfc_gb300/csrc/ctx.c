@@ -40,6 +40,7 @@ struct fcfcg_ctx {
   fcfcg_bins bins;
   int host_only;
   int device, nsm;
+  int pageable;                  /* kernels may read pageable host memory */
   cudaStream_t stream;
   char err[512];
   int kcell;
@@ -234,6 +235,11 @@ int fcfcg_create(const fcfcg_binning *cfg, int device, fcfcg_ctx **out) {
   c->device = device;
   CK(cudaSetDevice(device));
   CK(cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device));
+  /* Grace: the GPU reads the host's pageable memory coherently (at the
+   * NVLink-C2C rate), so host catalogues go straight into the preparation
+   * kernels instead of through one copy per array */
+  CK(cudaDeviceGetAttribute(&c->pageable, cudaDevAttrPageableMemoryAccess,
+                            device));
   CK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   for (int i = 0; i < 5; i++) CK(cudaEventCreate(&c->ev[i]));
   const fcfcg_bins *b = &c->bins;
@@ -414,7 +420,7 @@ static int load_common(fcfcg_ctx *c, int slot, size_t n, const double *x,
   s->grid_valid = 0;
   double *tx = NULL, *ty = NULL, *tz = NULL, *tw = NULL;
   const double *ix = x, *iy = y, *iz = z, *iw = w;
-  if (!on_device && n) {
+  if (!on_device && n && !c->pageable) {
     /* stage raw input in the output arrays, then rescale in place */
     CK(cudaMemcpyAsync(s->x, x, sizeof(double) * n, cudaMemcpyHostToDevice,
                        c->stream));
@@ -1803,7 +1809,7 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
     const size_t o = base[a], n = J->n;
     const double *ix = J->x, *iy = J->y, *iz = J->z;
     const double *iw = withwt ? J->w : NULL;
-    if (!on_device) {
+    if (!on_device && !c->pageable) {
       BCK(cudaMemcpyAsync(S->x + o, J->x, sizeof(double) * n,
                           cudaMemcpyHostToDevice, c->stream));
       BCK(cudaMemcpyAsync(S->y + o, J->y, sizeof(double) * n,
