@@ -430,25 +430,32 @@ __device__ __forceinline__ void enqueue(const fcfcg_launch &L,
  */
 #define ADJ_MAGIC 6755399441055744.0         /* 1.5 * 2^52 */
 #define ADJ_MAGIC_BITS 0x4338000000000000ll
-#define ADJ_SPILL (1ll << 61)
 
 __device__ __forceinline__ long long adj_term(double w, double g) {
   return __double_as_longlong(__fma_rn(w, g, ADJ_MAGIC)) - ADJ_MAGIC_BITS;
 }
 
-/* Add a term to a chunk point's 64-bit accumulator.  The thread whose add
- * carries it across +-2^61 moves 2^61 to the point's FP64 gradient (an
- * exact transfer), so with terms below 2^51 the accumulator cannot wrap. */
-__device__ __forceinline__ void adj_acc(unsigned long long *acc, long long v,
+/* Add a term to a chunk point's accumulator: two 32-bit words, value
+ * hi 2^32 + lo (lo unsigned, hi signed), as the weighted histograms keep
+ * theirs -- native 32-bit shared atomics, the carry out of lo read from the
+ * returned value.  The thread whose add carries hi across +-2^30 moves 2^62
+ * to the point's FP64 gradient (an exact transfer), so with terms below
+ * 2^51 the words cannot wrap. */
+__device__ __forceinline__ void adj_acc(uint32_t *lo, int *hi, long long v,
     double *dst, double unit) {
-  const long long old = (long long) atomicAdd(acc, (unsigned long long) v);
-  const long long nw = old + v;
-  if (nw >= ADJ_SPILL && old < ADJ_SPILL) {
-    atomicAdd(acc, (unsigned long long) (-ADJ_SPILL));
-    atomicAdd(dst, (double) ADJ_SPILL * unit);
-  } else if (nw <= -ADJ_SPILL && old > -ADJ_SPILL) {
-    atomicAdd(acc, (unsigned long long) ADJ_SPILL);
-    atomicAdd(dst, -(double) ADJ_SPILL * unit);
+  const uint32_t vl = (uint32_t) v;
+  const uint32_t old = atomicAdd(lo, vl);
+  const int h = (int) (v >> 32) + (((old + vl) < old) ? 1 : 0);
+  if (h) {
+    const int oh = atomicAdd(hi, h);
+    const int nh = oh + h;
+    if (nh >= HI_LIMIT && oh < HI_LIMIT) {
+      atomicSub(hi, HI_LIMIT);
+      atomicAdd(dst, ldexp(unit, 62));
+    } else if (nh <= -HI_LIMIT && oh > -HI_LIMIT) {
+      atomicAdd(hi, HI_LIMIT);
+      atomicAdd(dst, -ldexp(unit, 62));
+    }
   }
 }
 
@@ -511,7 +518,8 @@ struct Stage {
   uint16_t *bt;     /* per warp, 32: stencil entry */
   uint16_t *q;      /* per warp, QCAP: queued pairs */
   /* adjoint only: gradient sums in units of 2^-S, FP64 weights */
-  unsigned long long *ga;   /* FCHUNK */
+  unsigned long long *ga;   /* FCHUNK x 8 bytes: the 32-bit lo words of
+                               the chunk points, then their hi words */
   double *wa;               /* FCHUNK */
   long long *gb;            /* per warp, 32: the neighbour points */
   double *wb;               /* per warp, 32 */
@@ -653,7 +661,8 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
     /* d/dw_a of w_a w_b g[bin] is w_b g[bin], and the other way round; the
      * neighbour side is summed across the warp by the caller */
     const double g = L.hist_smem ? ((const double *) h)[bin] : __ldg(L.gfix + bin);
-    adj_acc(S.ga + i, adj_term(S.wb[src], g), L.dA + ai, L.gunit);
+    adj_acc((uint32_t *) S.ga + i, (int *) S.ga + FCHUNK + i,
+            adj_term(S.wb[src], g), L.dA + ai, L.gunit);
     gbv = adj_term(S.wa[i], g);
     return;
   }
@@ -1033,10 +1042,13 @@ k_count32(const fcfcg_launch L) {
     if (ADJ) {
       /* the chunk is done: its points' gradients out */
       __syncthreads();
+      uint32_t *glo = (uint32_t *) S.ga;
+      int *ghi = (int *) S.ga + FCHUNK;
       for (int k = threadIdx.x; k < m; k += blockDim.x) {
-        const long long v = (long long) S.ga[k];
+        const long long v = (long long) ghi[k] * 4294967296ll + glo[k];
         if (v != 0) atomicAdd(L.dA + first + k, (double) v * L.gunit);
-        S.ga[k] = 0;
+        glo[k] = 0;
+        ghi[k] = 0;
       }
     }
     n_in64 += n_in;

@@ -330,8 +330,8 @@ void fcfcg_graph_destroy(fcfcg_graph *graph);
  * The pair bins are recomputed, exactly as the count bins them (FP32 windows
  * with the FP64 recheck).  Each product w_j g[b] is rounded once (one
  * FP64 fused multiply-add) to an integer multiple of 2^-S, where S makes
- * max|w| max|g| 2^S <= 2^50; those integers are summed exactly (64-bit,
- * with exact spills to FP64), so every gradient is within
+ * max|w| max|g| 2^S <= 2^50; those integers are summed exactly (in
+ * 32-bit word pairs, with exact spills to FP64), so every gradient is within
  * n 2^-49 max|w| max|g| (plus the rounding of the final FP64 additions) of
  * the exact sum of its n products.  Catalogues
  * without weights count as unit weights.  Where the count falls back to the
