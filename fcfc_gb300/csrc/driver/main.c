@@ -362,6 +362,13 @@ int main(int argc, char **argv) {
   fcfcg_binning b;
   memset(&b, 0, sizeof b);
   b.geometry = GEOM;
+  /* DATA_STRUCT: FCFC's k-d tree (0) or ball tree (1); both map to the
+   * engine's cell grid, other values are rejected as FCFC does
+   * (load_conf.c:825-834) */
+  {
+    const long ds = conf_long(&C, "DATA_STRUCT", 0, 0);
+    if (ds != 0 && ds != 1) die("invalid DATA_STRUCT: %ld", ds);
+  }
   b.bintype = (int) conf_long(&C, "BINNING_SCHEME", 0, 0);
   b.with_mu_one = mu_one;
   double *sedges = NULL, *pedges = NULL;

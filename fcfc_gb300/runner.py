@@ -181,6 +181,11 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
     skip = _arr(conf, "ASCII_SKIP", ncat, default=[0] * ncat)
     cmt = _arr(conf, "ASCII_COMMENT", ncat)
     sel = _arr(conf, "SELECTION", ncat)
+    # DATA_STRUCT: k-d tree (0) or ball tree (1), both the cell grid here;
+    # other values rejected as FCFC does (load_conf.c:825-834)
+    if int(conf.get("DATA_STRUCT", 0)) not in (0, 1):
+        raise FCFCGError(capi.ERR_CFG, "invalid DATA_STRUCT: %s"
+                         % conf["DATA_STRUCT"])
     bintype = int(conf.get("BINNING_SCHEME", 0))
     pairs = _arr(conf, "PAIR_COUNT")
     pcout = _arr(conf, "PAIR_COUNT_FILE")

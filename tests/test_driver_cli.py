@@ -29,6 +29,8 @@ def test_config_errors(drivers, tmp_path):
         ("CATALOG = [a.txt]\nPOSITION = [$1, $2]\n", "POSITION"),
         ("CATALOG = [a.txt]\nCATALOG_TYPE = [1]\nPOSITION = [$1, $2, $3]\n",
          "ASCII"),
+        ("CATALOG = [a.txt]\nPOSITION = [$1, $2, $3]\nDATA_STRUCT = 2\n",
+         "DATA_STRUCT"),
     ]
     for text, word in cases:
         conf.write_text(text)
@@ -38,3 +40,14 @@ def test_config_errors(drivers, tmp_path):
     r = subprocess.run([drivers[0], "-c", str(tmp_path / "missing.conf")],
                        capture_output=True, text=True)
     assert r.returncode != 0
+
+
+def test_runner_rejects_data_struct():
+    """The Python run flow rejects DATA_STRUCT values FCFC rejects (0 and 1,
+    its k-d and ball trees, both map to the cell grid), before device work."""
+    from fcfc_gb300 import runner
+    from fcfc_gb300.capi import FCFCGError
+    conf = runner.parse_conf("CATALOG = [a.txt]\nPOSITION = [$1, $2, $3]\n"
+                             "DATA_STRUCT = 2\nPAIR_COUNT = [AA]\n")
+    with pytest.raises(FCFCGError, match="DATA_STRUCT"):
+        runner.run(conf, "box")
