@@ -719,8 +719,9 @@ __device__ __forceinline__ uint32_t scan_chunk(const fcfcg_launch &L,
  *
  * A CTA holds one chunk (<= 64 points of a cell).  The non-empty neighbour
  * cells of the stencil are laid end to end (a prefix sum per chunk); the
- * warps take blocks of 32 consecutive neighbour points in turn, and each
- * lane compares its point with every chunk point (broadcast from shared
+ * warps take blocks of 32 consecutive neighbour points from a shared
+ * counter, and each lane compares its point with every chunk point
+ * (broadcast from shared
  * memory), recording those inside the outer range as mask bits.  A block's
  * in-range pairs are then compacted into the warp queue and binned 32 at a
  * time, every lane busy.
