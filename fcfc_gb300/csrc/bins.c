@@ -165,8 +165,80 @@ static int axis_bin(const fcfcg_axis *a, double v) {
   return k;
 }
 
-int fcfcg_axis_ftab(fcfcg_axis *a, int unused) {
-  (void) unused;
+/* FP32 bit pattern of a positive double rounded to float, and back. */
+static uint32_t fbits(double v) {
+  const float f = (float) v;
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  return u;
+}
+
+static double bits_value(uint32_t u) {
+  float f;
+  memcpy(&f, &u, 4);
+  return (double) f;
+}
+
+/* Flags and start bin of the table cell [x0, x1) (see FCFCG_FTAB_*). */
+static unsigned ftab_cell(const fcfcg_axis *a, double x0, double x1) {
+  const double w = x1 - x0;
+  const int first = a->min0 ? 1 : 0;
+  int b = axis_bin(a, x0);
+  unsigned v = (b < 0) ? FCFCG_FTAB_BIN_MASK : (unsigned) b;
+  int inside = 0;
+  for (int k = first; k <= a->nbin; k++) {
+    const double e = a->edge[k];
+    if (e >= x0 - 0.5 * w && e <= x0) v |= FCFCG_FTAB_LO;
+    if (e >= x1 && e <= x1 + 0.5 * w) v |= FCFCG_FTAB_HI;
+    if (e > x0 && e < x1) inside++;
+  }
+  if (inside == 1) v |= FCFCG_FTAB_CX1;
+  else if (inside > 1) v |= FCFCG_FTAB_CXM;
+  return v;
+}
+
+/*
+ * Bit-pattern table: cell c holds the positive FP32 values whose bit
+ * pattern >> sh is c, i.e. a fixed fraction 2^(sh - 23) of each octave --
+ * what bins spaced in ratio (log bins) need.  The coarsest sh from 19 (16
+ * cells per octave) down to 8 (2^15) that fits the table and has no cell
+ * holding several edges; the axis is left alone when there is none, or when
+ * it starts at zero.
+ */
+static int axis_ftab_log(fcfcg_axis *a) {
+  if (a->min0 || !(a->vmin > 0)) return 0;
+  for (int sh = 19; sh >= 8; sh--) {
+    /* from at least one whole cell below the lowest edge to one above the
+     * highest, as the uniform tables */
+    const long lo = (long) (fbits(a->vmin) >> sh) - 2;
+    const long hi = (long) (fbits(a->vmax) >> sh) + 3;
+    const long m = hi - lo;
+    if (lo < 1 || m > FCFCG_FTAB_MAXLEN) break;   /* finer: too long */
+    uint16_t *t = malloc(sizeof(uint16_t) * m);
+    if (!t) return FCFCG_ERR_MEMORY;
+    int multi = 0;
+    for (long c = 0; c < m && !multi; c++) {
+      const double x0 = bits_value((uint32_t) (lo + c) << sh);
+      const double x1 = bits_value((uint32_t) (lo + c + 1) << sh);
+      t[c] = (uint16_t) ftab_cell(a, x0, x1);
+      multi = (t[c] & FCFCG_FTAB_CXM) != 0;
+    }
+    if (multi) {
+      free(t);
+      continue;
+    }
+    free(a->ftab);
+    a->ftab = t;
+    a->foff = lo;
+    a->nftab = m;
+    a->fshift = 0;
+    a->flog = sh;
+    return 0;
+  }
+  return 0;
+}
+
+int fcfcg_axis_ftab(fcfcg_axis *a, int allow_log) {
   /* cell width: the smallest power of two (>= 1 unit) that keeps the table
    * within FCFCG_FTAB_MAXLEN cells */
   int sh = 0;
@@ -187,29 +259,27 @@ int fcfcg_axis_ftab(fcfcg_axis *a, int unused) {
   a->fedge = malloc(sizeof(float) * (a->nbin + 1));
   if (!a->ftab || !a->fedge) return FCFCG_ERR_MEMORY;
   for (int k = 0; k <= a->nbin; k++) a->fedge[k] = (float) a->edge[k];
-  const int first = a->min0 ? 1 : 0;
+  int multi = 0;
   for (long c = 0; c < m; c++) {
     const double x0 = (double) (lo + c) * w, x1 = x0 + w;
-    int b = axis_bin(a, x0);
-    unsigned v = (b < 0) ? FCFCG_FTAB_BIN_MASK : (unsigned) b;
-    int inside = 0;
-    for (int k = first; k <= a->nbin; k++) {
-      const double e = a->edge[k];
-      if (e >= x0 - 0.5 * w && e <= x0) v |= FCFCG_FTAB_LO;
-      if (e >= x1 && e <= x1 + 0.5 * w) v |= FCFCG_FTAB_HI;
-      if (e > x0 && e < x1) inside++;
-    }
-    if (inside == 1) v |= FCFCG_FTAB_CX1;
-    else if (inside > 1) v |= FCFCG_FTAB_CXM;
-    a->ftab[c] = (uint16_t) v;
+    a->ftab[c] = (uint16_t) ftab_cell(a, x0, x1);
+    multi |= (a->ftab[c] & FCFCG_FTAB_CXM) != 0;
   }
   a->foff = lo;
   a->nftab = m;
   a->fshift = sh;
+  a->flog = 0;
+  /* cells holding several edges send every value in them to the FP64
+   * recheck: bins that are not linear get a bit-pattern table if that
+   * resolves them */
+  if (multi && allow_log) return axis_ftab_log(a);
   return FCFCG_OK;
 }
 
-static int axis_finish(fcfcg_axis *a, const double *edge, int n, int hybrid) {
+/* allow_log: the kernels can use a bit-pattern FP32 table for this axis
+ * (the s_perp axis of (s_perp, pi) in a box) */
+static int axis_finish(fcfcg_axis *a, const double *edge, int n, int hybrid,
+    int allow_log) {
   a->nbin = n;
   a->tabtype = hybrid ? FCFCG_TAB_HYBRID : FCFCG_TAB_INT;
   a->edge = malloc(sizeof(double) * (n + 1));
@@ -221,7 +291,7 @@ static int axis_finish(fcfcg_axis *a, const double *edge, int n, int hybrid) {
   a->rtab = hybrid ? lut_hybrid(edge, n, &a->nrtab, &a->roff)
                    : lut_int(edge, n, &a->nrtab, &a->roff);
   if (!a->rtab) return FCFCG_ERR_CF;
-  if (n <= FCFCG_FTAB_MAXBIN) return fcfcg_axis_ftab(a, 0);
+  if (n <= FCFCG_FTAB_MAXBIN) return fcfcg_axis_ftab(a, allow_log);
   return FCFCG_OK;
 }
 
@@ -393,9 +463,12 @@ int fcfcg_bins_setup(const fcfcg_binning *cfg, fcfcg_bins *b, char *err,
       b->box_raw[k] = cfg->box[k];
       b->box[k] = cfg->box[k] * fac;
     }
-  if ((rc = axis_finish(&b->s, s2, ns, hybrid)))
+  /* a bit-pattern s_perp table pays in a box, where s_perp^2 comes from
+   * dx and dy alone; a survey's s_perp^2 = s^2 - pi^2 carries the rounding
+   * of s^2, so small s_perp stays ambiguous whatever the table */
+  if ((rc = axis_finish(&b->s, s2, ns, hybrid, spi && box)))
     FAIL(rc, "failed to create the separation lookup table");
-  if (spi && (rc = axis_finish(&b->p, box ? pb : p2, np, hybrid)))
+  if (spi && (rc = axis_finish(&b->p, box ? pb : p2, np, hybrid, 0)))
     FAIL(rc, "failed to create the pi lookup table");
   free(sb);
   free(s2);

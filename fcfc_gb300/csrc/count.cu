@@ -29,6 +29,11 @@
 
 #include "fcfcg_internal.h"
 
+/* Kernel binning codes: the public FCFCG_BIN_* plus (s_perp, pi) whose
+ * s_perp table is indexed by FP32 bit pattern (bins spaced in ratio). */
+#define BIN_SPIL 3
+#define IS_SPI(B) ((B) == FCFCG_BIN_SPI || (B) == BIN_SPIL)
+
 #define CT_THREADS 256
 #define FULLMASK 0xffffffffu
 
@@ -268,21 +273,34 @@ __device__ int ref_bin_pair(const fcfcg_launch &L, uint32_t a, uint32_t b,
  * range; *amb is set when an edge lies within E of v.  A cell with one edge
  * inside compares v with that edge (fe: the edges rounded to FP32).
  * CHECK_NAN: the value may be NaN (survey geometry). */
-template <bool CHECK_NAN>
+template <bool CHECK_NAN, bool LOG>
 __device__ __forceinline__ unsigned ftab_bin(const uint16_t *tab, int off,
     int ntab, float inv, const float *fe, int nbin, float v, float E,
-    bool &amb) {
+    bool &amb, int lg, float vamb) {
   if (CHECK_NAN && !(v == v)) {
     amb = true;
     return FCFCG_FTAB_BIN_MASK;
   }
-  const float u = v * inv;
-  const int i = __float2int_rz(u);
-  const int t = i - off;
-  if ((unsigned) t >= (unsigned) ntab) return FCFCG_FTAB_BIN_MASK;
-  const unsigned e = tab[t];
-  const float fr = u - (float) i;
-  const float Eu = E * inv;
+  int i;
+  float fr, Eu;
+  if (LOG) {
+    /* bit-pattern table: cell = FP32 bits >> lg, a fixed fraction of the
+     * octave; below vamb the window is wider than half a cell */
+    amb |= v < vamb;
+    const uint32_t bits = __float_as_uint(v);
+    i = (int) (bits >> lg);
+    if ((unsigned) (i - off) >= (unsigned) ntab) return FCFCG_FTAB_BIN_MASK;
+    fr = __uint2float_rz(bits & ((1u << lg) - 1u)) * inv;
+    /* 1 / cell width: 2^(23 - lg) / 2^exponent(v) */
+    Eu = E * __uint_as_float((277u - (uint32_t) lg - (bits >> 23)) << 23);
+  } else {
+    const float u = v * inv;
+    i = __float2int_rz(u);
+    if ((unsigned) (i - off) >= (unsigned) ntab) return FCFCG_FTAB_BIN_MASK;
+    fr = u - (float) i;
+    Eu = E * inv;
+  }
+  const unsigned e = tab[i - off];
   const unsigned m = FCFCG_FTAB_CXM | (fr <= Eu ? FCFCG_FTAB_LO : 0u) |
                      (fr >= 1.f - Eu ? FCFCG_FTAB_HI : 0u);
   amb |= (e & m) != 0u;
@@ -576,12 +594,17 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
   const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
   bool amb = false;
   int bin = -1;
-  if (BIN == FCFCG_BIN_SPI && GEOM == FCFCG_GEOM_BOX) {
+  if (IS_SPI(BIN) && GEOM == FCFCG_GEOM_BOX) {
     const float sp2 = fmaf(dy, dy, dx * dx);
     const float pi = fabsf(dz);
     amb = !(sp2 >= L.tiny);
-    unsigned sb = ftab_bin<false>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb, sp2, L.Emax, amb);
-    unsigned pbn = ftab_bin<false>(fp, L.fpoff, L.nfp, L.fpinv, fpe, L.npb, pi, L.P0, amb);
+    /* with a bit-pattern table (log bins, narrow near zero) the window of
+     * s_perp^2 follows s_perp; otherwise its value at s_perp max (tiny sp2
+     * is ambiguous anyway) */
+    const float Es = (BIN == BIN_SPIL)
+        ? fmaf(L.K2, sp2, fmaf(L.K1, sp2 * rsqrtf(sp2), L.K0)) : L.Emax;
+    unsigned sb = ftab_bin<false, BIN == BIN_SPIL>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb, sp2, Es, amb, L.fslog, L.fsamb);
+    unsigned pbn = ftab_bin<false, false>(fp, L.fpoff, L.nfp, L.fpinv, fpe, L.npb, pi, L.P0, amb, L.fplog, L.fpamb);
     if (!amb) {
       if (sb == FCFCG_FTAB_BIN_MASK || pbn == FCFCG_FTAB_BIN_MASK) return;
       bin = (int) sb + (int) pbn * L.ns;
@@ -590,7 +613,7 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
     const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     amb = !(s2 >= L.tiny);
     if (BIN == FCFCG_BIN_ISO) {
-      unsigned sb = ftab_bin<false>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb, s2, L.Emax, amb);
+      unsigned sb = ftab_bin<false, BIN == BIN_SPIL>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb, s2, L.Emax, amb, L.fslog, L.fsamb);
       if (!amb) {
         if (sb == FCFCG_FTAB_BIN_MASK) return;
         bin = (int) sb;
@@ -617,8 +640,8 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
         }
         const float Eq = fmaf(L.Q1, rs, fmaf(L.Q2, q, L.Q0));
         int qi = mu_bin(q, Eq, amb);
-        unsigned sb = ftab_bin<GEOM == FCFCG_GEOM_SURVEY>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb,
-                                                            s2, E, amb);
+        unsigned sb = ftab_bin<GEOM == FCFCG_GEOM_SURVEY, false>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb,
+                                                            s2, E, amb, L.fslog, L.fsamb);
         if (!amb) {
           if (qi >= L.nmu) {
             if (!L.mu_one) return;
@@ -634,9 +657,9 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
         const float pi2 = __fdividef(dm * dm, mm);
         const float sp2 = s2 - pi2;
         const float Ep = fmaf(L.P2, s2, fmaf(L.P1, s, L.P0));
-        unsigned pbn = ftab_bin<true>(fp, L.fpoff, L.nfp, L.fpinv, fpe, L.npb, pi2, Ep, amb);
-        unsigned sb = ftab_bin<true>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb,
-                                     sp2 < 0.f ? 0.f : sp2, E + Ep, amb);
+        unsigned pbn = ftab_bin<true, false>(fp, L.fpoff, L.nfp, L.fpinv, fpe, L.npb, pi2, Ep, amb, L.fplog, L.fpamb);
+        unsigned sb = ftab_bin<true, BIN == BIN_SPIL>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb,
+                                     sp2 < 0.f ? 0.f : sp2, E + Ep, amb, L.fslog, L.fsamb);
         if (!amb) {
           if (sb == FCFCG_FTAB_BIN_MASK || pbn == FCFCG_FTAB_BIN_MASK) return;
           bin = (int) sb + (int) pbn * L.ns;
@@ -689,7 +712,7 @@ __device__ __forceinline__ uint32_t scan_chunk_(const fcfcg_launch &L,
     const float4 pa = a[i];
     const float dx = pa.x - bx, dy = pa.y - by, dz = pa.z - bz;
     bool inr;
-    if (BIN == FCFCG_BIN_SPI && GEOM == FCFCG_GEOM_BOX) {
+    if (IS_SPI(BIN) && GEOM == FCFCG_GEOM_BOX) {
       const float v = fmaf(dy, dy, dx * dx);
       inr = (fabsf(dz) < p_lim) & (v < s_lim);
     } else {
@@ -1205,6 +1228,8 @@ static kfun_t pick32(int geom, int bin, int wt, int batch, int adj) {
     K32A(FCFCG_GEOM_SURVEY, FCFCG_BIN_ISO)
     K32A(FCFCG_GEOM_SURVEY, FCFCG_BIN_SMU)
     K32A(FCFCG_GEOM_SURVEY, FCFCG_BIN_SPI)
+    K32A(FCFCG_GEOM_BOX, BIN_SPIL)
+    K32A(FCFCG_GEOM_SURVEY, BIN_SPIL)
 #undef K32A
     return 0;
   }
@@ -1217,6 +1242,7 @@ static kfun_t pick32(int geom, int bin, int wt, int batch, int adj) {
     K32B(FCFCG_BIN_ISO)
     K32B(FCFCG_BIN_SMU)
     K32B(FCFCG_BIN_SPI)
+    K32B(BIN_SPIL)
 #undef K32B
     return 0;
   }
@@ -1230,6 +1256,8 @@ static kfun_t pick32(int geom, int bin, int wt, int batch, int adj) {
   K32(FCFCG_GEOM_SURVEY, FCFCG_BIN_ISO)
   K32(FCFCG_GEOM_SURVEY, FCFCG_BIN_SMU)
   K32(FCFCG_GEOM_SURVEY, FCFCG_BIN_SPI)
+  K32(FCFCG_GEOM_BOX, BIN_SPIL)
+  K32(FCFCG_GEOM_SURVEY, BIN_SPIL)
 #undef K32
   return 0;
 }
@@ -1256,8 +1284,10 @@ extern "C" int fcfcg_k_count(void *stream, const fcfcg_launch *L,
                ? (size_t) L->ntot * (L->withwt ? 8 : 4) : 0;
     threads = CT_THREADS;
   } else {
-    f = pick32(L->geometry, L->bintype, L->withwt, L->mocks != NULL,
-               L->adjoint);
+    f = pick32(L->geometry,
+               (L->bintype == FCFCG_BIN_SPI && L->fslog) ? BIN_SPIL
+                                                          : L->bintype,
+               L->withwt, L->mocks != NULL, L->adjoint);
     size_t tab = fcfcg_k_count32_tab_bytes(L->nfs, L->nfp, L->nsb, L->npb);
     smem = tab + (L->hist_smem ? (size_t) L->ntot * (L->withwt ? 8 : 4) : 0);
     smem = ((smem + 15) & ~(size_t) 15) +

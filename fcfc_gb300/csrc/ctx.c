@@ -813,6 +813,14 @@ static int slot_sort(fcfcg_ctx *c, slot_t *s, const grid_t *g) {
   return FCFCG_OK;
 }
 
+/* Lower end of cell c of a bit-pattern table (FP32 bits c << sh). */
+static double ftab_cell_value(long c, int sh) {
+  const uint32_t u = (uint32_t) c << sh;
+  float f;
+  memcpy(&f, &u, 4);
+  return (double) f;
+}
+
 /* Rounding bounds of the FP32 path; returns 0 when the FP32 windows stay
  * below half a table unit, i.e. the FP32 path applies. */
 static int fp32_bounds(const fcfcg_ctx *c, const grid_t *g, double dmax,
@@ -880,10 +888,55 @@ static int fp32_bounds(const fcfcg_ctx *c, const grid_t *g, double dmax,
   if (b->bintype == FCFCG_BIN_SPI &&
       (b->p.nbin > FCFCG_FTAB_MAXBIN || !b->p.ftab))
     return -1;
-  /* windows below half a table cell */
-  if (!(Es < 0.45 * ldexp(1.0, b->s.fshift))) return -1;
-  if (b->bintype == FCFCG_BIN_SPI && !(Ep < 0.45 * ldexp(1.0, b->p.fshift)))
+  /* windows below half a table cell: over the whole uniform tables; for a
+   * bit-pattern table, whose cells shrink with the value, from a threshold
+   * up -- values below it are sent to the recheck */
+  L->fsamb = L->fpamb = -1.f;
+  if (b->s.flog) {
+    /* the window the s-axis lookups use at value v (an upper bound) */
+    const int varies = (b->bintype != FCFCG_BIN_ISO);
+    const double p2 = (b->bintype == FCFCG_BIN_SPI && !box) ? b->p.vmax : 0;
+    double amb = -1;
+    for (long c = b->s.nftab - 1; c >= 0; c--) {
+      const double x0 = ftab_cell_value(b->s.foff + c, b->s.flog);
+      const double x1 = ftab_cell_value(b->s.foff + c + 1, b->s.flog);
+      double W = L->Emax;
+      if (varies) {
+        const double v = x1 + p2;
+        W = (double) L->K2 * v + (double) L->K1 * sqrt(v) + (double) L->K0;
+        if (p2 > 0)
+          W += (double) L->P2 * v + (double) L->P1 * sqrt(v) + (double) L->P0;
+        W *= 1.01;
+      }
+      if (!(W < 0.45 * (x1 - x0))) {
+        amb = x1;
+        break;
+      }
+    }
+    L->fsamb = (float) amb;
+    if (amb > 0 && (double) L->fsamb < amb)   /* round up: still ambiguous */
+      L->fsamb = nextafterf(L->fsamb, INFINITY);
+  } else if (!(Es < 0.45 * ldexp(1.0, b->s.fshift))) {
     return -1;
+  }
+  if (b->bintype == FCFCG_BIN_SPI) {
+    if (b->p.flog) {
+      double amb = -1;
+      for (long c = b->p.nftab - 1; c >= 0; c--) {
+        const double x0 = ftab_cell_value(b->p.foff + c, b->p.flog);
+        const double x1 = ftab_cell_value(b->p.foff + c + 1, b->p.flog);
+        if (!(Ep * 1.01 < 0.45 * (x1 - x0))) {
+          amb = x1;
+          break;
+        }
+      }
+      L->fpamb = (float) amb;
+      if (amb > 0 && (double) L->fpamb < amb)
+        L->fpamb = nextafterf(L->fpamb, INFINITY);
+    } else if (!(Ep < 0.45 * ldexp(1.0, b->p.fshift))) {
+      return -1;
+    }
+  }
   /* Values beyond either end of an FP32 table need no check: a table runs
    * from at least one cell below its lowest edge to at least one cell above
    * its highest (fcfcg_axis_ftab), so an FP32 value outside it is more than
@@ -947,14 +1000,16 @@ static void launch_fp32_tables(const fcfcg_ctx *c, fcfcg_launch *L) {
   L->fs = c->d_fs;
   L->nfs = (int) b->s.nftab;
   L->fsoff = (int) b->s.foff;
-  L->fsinv = (float) ldexp(1.0, -b->s.fshift);
+  L->fslog = b->s.flog;
+  L->fsinv = (float) ldexp(1.0, b->s.flog ? -b->s.flog : -b->s.fshift);
   L->fse = c->d_fse;
   L->nsb = b->s.nbin;
   if (b->bintype == FCFCG_BIN_SPI) {
     L->fp = c->d_fp;
     L->nfp = (int) b->p.nftab;
     L->fpoff = (int) b->p.foff;
-    L->fpinv = (float) ldexp(1.0, -b->p.fshift);
+    L->fplog = b->p.flog;
+    L->fpinv = (float) ldexp(1.0, b->p.flog ? -b->p.flog : -b->p.fshift);
     L->fpe = c->d_fpe;
     L->npb = b->p.nbin;
   }

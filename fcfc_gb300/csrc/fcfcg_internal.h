@@ -43,6 +43,9 @@ typedef struct {
   uint16_t *ftab;        /* FP32 window table (host) */
   long nftab, foff;      /* cells, index of the first cell */
   int fshift;            /* cell width 2^fshift units */
+  int flog;              /* > 0: cells are the FP32 bit pattern >> flog
+                            (2^(23 - flog) cells per octave), for bins
+                            that are not linear; 0: uniform cells */
   float *fedge;          /* nbin + 1 edges rounded to FP32 (host) */
   double vmin, vmax;     /* edge[0], edge[nbin] */
   int min0;              /* edge[0] == 0: no lower range check (smin0) */
@@ -64,8 +67,9 @@ typedef struct {
 int fcfcg_bins_setup(const fcfcg_binning *cfg, fcfcg_bins *b, char *err,
     size_t errlen);
 void fcfcg_bins_release(fcfcg_bins *b);
-/* Build the FP32 window table of an axis (ftab / foff / nftab). */
-int fcfcg_axis_ftab(fcfcg_axis *a, int vmin_is_floor);
+/* Build the FP32 window table of an axis (ftab / foff / nftab); allow_log:
+ * a bit-pattern table may replace a uniform one with multi-edge cells. */
+int fcfcg_axis_ftab(fcfcg_axis *a, int allow_log);
 /* Accessors of the opaque context used by the post-processing code. */
 const fcfcg_bins *fcfcg_ctx_bins(const fcfcg_ctx *c);
 const double *fcfcg_ctx_box_raw(const fcfcg_ctx *c);
@@ -117,7 +121,11 @@ typedef struct {
   /* FP32 tables (copied to shared memory) */
   const uint16_t *fs, *fp;
   int nfs, nfp, fsoff, fpoff;
-  float fsinv, fpinv;          /* 1 / cell width of the FP32 tables */
+  float fsinv, fpinv;          /* 1 / cell width of the FP32 tables, or
+                                  2^-flog for bit-pattern tables */
+  int fslog, fplog;            /* the axes' flog (0: uniform cells) */
+  float fsamb, fpamb;          /* bit-pattern tables: values below are
+                                  ambiguous (the window exceeds the cell) */
   const float *fse, *fpe;      /* FP32 edges (nbin + 1 each) */
   int nsb, npb;                /* bins of the s and pi axes */
   float s_lim, p_lim;          /* values at/above: out of range for sure */
