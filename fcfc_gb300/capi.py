@@ -38,7 +38,8 @@ class BinsInfo(C.Structure):
     _fields_ = [("ns", C.c_int), ("nmu", C.c_int), ("np", C.c_int),
                 ("ntot", C.c_int64), ("tabtype", C.c_int),
                 ("rescale", C.c_double), ("box_rescaled", C.c_double * 3),
-                ("nstab", C.c_int64), ("nptab", C.c_int64)]
+                ("nstab", C.c_int64), ("nptab", C.c_int64),
+                ("ftab_cells_per_octave", C.c_int)]
 
 
 class Cosmo(C.Structure):

@@ -277,7 +277,7 @@ int fcfcg_axis_ftab(fcfcg_axis *a, int allow_log) {
 }
 
 /* allow_log: the kernels can use a bit-pattern FP32 table for this axis
- * (the s_perp axis of (s_perp, pi) in a box) */
+ * (the s or s_perp axis in a box) */
 static int axis_finish(fcfcg_axis *a, const double *edge, int n, int hybrid,
     int allow_log) {
   a->nbin = n;
@@ -463,10 +463,10 @@ int fcfcg_bins_setup(const fcfcg_binning *cfg, fcfcg_bins *b, char *err,
       b->box_raw[k] = cfg->box[k];
       b->box[k] = cfg->box[k] * fac;
     }
-  /* a bit-pattern s_perp table pays in a box, where s_perp^2 comes from
-   * dx and dy alone; a survey's s_perp^2 = s^2 - pi^2 carries the rounding
+  /* a bit-pattern s table pays in a box (log bins; the kernels have
+   * variants for it); a survey's s_perp^2 = s^2 - pi^2 carries the rounding
    * of s^2, so small s_perp stays ambiguous whatever the table */
-  if ((rc = axis_finish(&b->s, s2, ns, hybrid, spi && box)))
+  if ((rc = axis_finish(&b->s, s2, ns, hybrid, box)))
     FAIL(rc, "failed to create the separation lookup table");
   if (spi && (rc = axis_finish(&b->p, box ? pb : p2, np, hybrid, 0)))
     FAIL(rc, "failed to create the pi lookup table");

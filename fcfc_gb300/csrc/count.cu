@@ -29,10 +29,17 @@
 
 #include "fcfcg_internal.h"
 
-/* Kernel binning codes: the public FCFCG_BIN_* plus (s_perp, pi) whose
- * s_perp table is indexed by FP32 bit pattern (bins spaced in ratio). */
+/* Kernel binning codes: the public FCFCG_BIN_* (0 iso, 1 (s,mu), 2
+ * (s_perp,pi)), and the same binnings with an FP32 table of s^2 or s_perp^2
+ * indexed by bit pattern (bins spaced in ratio, boxes only): 3 (s_perp,pi),
+ * 4 iso, 5 (s,mu). */
 #define BIN_SPIL 3
+#define BIN_ISOL 4
+#define BIN_SMUL 5
 #define IS_SPI(B) ((B) == FCFCG_BIN_SPI || (B) == BIN_SPIL)
+#define IS_ISO(B) ((B) == FCFCG_BIN_ISO || (B) == BIN_ISOL)
+#define IS_SMU(B) ((B) == FCFCG_BIN_SMU || (B) == BIN_SMUL)
+#define LOGTAB(B) ((B) >= BIN_SPIL)
 
 #define CT_THREADS 256
 #define FULLMASK 0xffffffffu
@@ -601,9 +608,9 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
     /* with a bit-pattern table (log bins, narrow near zero) the window of
      * s_perp^2 follows s_perp; otherwise its value at s_perp max (tiny sp2
      * is ambiguous anyway) */
-    const float Es = (BIN == BIN_SPIL)
+    const float Es = LOGTAB(BIN)
         ? fmaf(L.K2, sp2, fmaf(L.K1, sp2 * rsqrtf(sp2), L.K0)) : L.Emax;
-    unsigned sb = ftab_bin<false, BIN == BIN_SPIL>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb, sp2, Es, amb, L.fslog, L.fsamb);
+    unsigned sb = ftab_bin<false, LOGTAB(BIN)>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb, sp2, Es, amb, L.fslog, L.fsamb);
     unsigned pbn = ftab_bin<false, false>(fp, L.fpoff, L.nfp, L.fpinv, fpe, L.npb, pi, L.P0, amb, L.fplog, L.fpamb);
     if (!amb) {
       if (sb == FCFCG_FTAB_BIN_MASK || pbn == FCFCG_FTAB_BIN_MASK) return;
@@ -612,8 +619,12 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
   } else {
     const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
     amb = !(s2 >= L.tiny);
-    if (BIN == FCFCG_BIN_ISO) {
-      unsigned sb = ftab_bin<false, BIN == BIN_SPIL>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb, s2, L.Emax, amb, L.fslog, L.fsamb);
+    if (IS_ISO(BIN)) {
+      /* with a bit-pattern table the window follows s (log bins near zero
+       * are narrower than its value at s max) */
+      const float Es = LOGTAB(BIN)
+          ? fmaf(L.K2, s2, fmaf(L.K1, s2 * rsqrtf(s2), L.K0)) : L.Emax;
+      unsigned sb = ftab_bin<false, LOGTAB(BIN)>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb, s2, Es, amb, L.fslog, L.fsamb);
       if (!amb) {
         if (sb == FCFCG_FTAB_BIN_MASK) return;
         bin = (int) sb;
@@ -629,7 +640,7 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
         my = fmaf(2.f, pb.y, c2y) + dy;
         mz = fmaf(2.f, pb.z, c2z) + dz;
       }
-      if (BIN == FCFCG_BIN_SMU) {
+      if (IS_SMU(BIN)) {
         float q;
         if (GEOM == FCFCG_GEOM_BOX) {
           q = L.fnmu * fabsf(dz) * rs;
@@ -640,7 +651,7 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
         }
         const float Eq = fmaf(L.Q1, rs, fmaf(L.Q2, q, L.Q0));
         int qi = mu_bin(q, Eq, amb);
-        unsigned sb = ftab_bin<GEOM == FCFCG_GEOM_SURVEY, false>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb,
+        unsigned sb = ftab_bin<GEOM == FCFCG_GEOM_SURVEY, LOGTAB(BIN)>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb,
                                                             s2, E, amb, L.fslog, L.fsamb);
         if (!amb) {
           if (qi >= L.nmu) {
@@ -658,7 +669,7 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
         const float sp2 = s2 - pi2;
         const float Ep = fmaf(L.P2, s2, fmaf(L.P1, s, L.P0));
         unsigned pbn = ftab_bin<true, false>(fp, L.fpoff, L.nfp, L.fpinv, fpe, L.npb, pi2, Ep, amb, L.fplog, L.fpamb);
-        unsigned sb = ftab_bin<true, BIN == BIN_SPIL>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb,
+        unsigned sb = ftab_bin<true, LOGTAB(BIN)>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb,
                                      sp2 < 0.f ? 0.f : sp2, E + Ep, amb, L.fslog, L.fsamb);
         if (!amb) {
           if (sb == FCFCG_FTAB_BIN_MASK || pbn == FCFCG_FTAB_BIN_MASK) return;
@@ -752,7 +763,7 @@ __device__ __forceinline__ uint32_t scan_chunk(const fcfcg_launch &L,
 /* (s, mu) binning keeps more values live: 3 CTAs per SM (85 registers)
  * measure faster there, 4 CTAs (64 registers) for the other binnings. */
 template <int GEOM, int BIN, int WT, int BATCH, int ADJ>
-__global__ void __launch_bounds__(CT32_THREADS, BIN == FCFCG_BIN_SMU ? 3 : 4)
+__global__ void __launch_bounds__(CT32_THREADS, IS_SMU(BIN) ? 3 : 4)
 k_count32(const fcfcg_launch L) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t sh_chunk;
@@ -1229,7 +1240,8 @@ static kfun_t pick32(int geom, int bin, int wt, int batch, int adj) {
     K32A(FCFCG_GEOM_SURVEY, FCFCG_BIN_SMU)
     K32A(FCFCG_GEOM_SURVEY, FCFCG_BIN_SPI)
     K32A(FCFCG_GEOM_BOX, BIN_SPIL)
-    K32A(FCFCG_GEOM_SURVEY, BIN_SPIL)
+    K32A(FCFCG_GEOM_BOX, BIN_ISOL)
+    K32A(FCFCG_GEOM_BOX, BIN_SMUL)
 #undef K32A
     return 0;
   }
@@ -1243,6 +1255,8 @@ static kfun_t pick32(int geom, int bin, int wt, int batch, int adj) {
     K32B(FCFCG_BIN_SMU)
     K32B(FCFCG_BIN_SPI)
     K32B(BIN_SPIL)
+    K32B(BIN_ISOL)
+    K32B(BIN_SMUL)
 #undef K32B
     return 0;
   }
@@ -1257,7 +1271,8 @@ static kfun_t pick32(int geom, int bin, int wt, int batch, int adj) {
   K32(FCFCG_GEOM_SURVEY, FCFCG_BIN_SMU)
   K32(FCFCG_GEOM_SURVEY, FCFCG_BIN_SPI)
   K32(FCFCG_GEOM_BOX, BIN_SPIL)
-  K32(FCFCG_GEOM_SURVEY, BIN_SPIL)
+  K32(FCFCG_GEOM_BOX, BIN_ISOL)
+  K32(FCFCG_GEOM_BOX, BIN_SMUL)
 #undef K32
   return 0;
 }
@@ -1284,10 +1299,11 @@ extern "C" int fcfcg_k_count(void *stream, const fcfcg_launch *L,
                ? (size_t) L->ntot * (L->withwt ? 8 : 4) : 0;
     threads = CT_THREADS;
   } else {
-    f = pick32(L->geometry,
-               (L->bintype == FCFCG_BIN_SPI && L->fslog) ? BIN_SPIL
-                                                          : L->bintype,
-               L->withwt, L->mocks != NULL, L->adjoint);
+    /* a bit-pattern s table selects the kernel's log variant */
+    const int bin = !L->fslog ? L->bintype
+        : (L->bintype == FCFCG_BIN_SPI ? BIN_SPIL
+           : (L->bintype == FCFCG_BIN_ISO ? BIN_ISOL : BIN_SMUL));
+    f = pick32(L->geometry, bin, L->withwt, L->mocks != NULL, L->adjoint);
     size_t tab = fcfcg_k_count32_tab_bytes(L->nfs, L->nfp, L->nsb, L->npb);
     smem = tab + (L->hist_smem ? (size_t) L->ntot * (L->withwt ? 8 : 4) : 0);
     smem = ((smem + 15) & ~(size_t) 15) +

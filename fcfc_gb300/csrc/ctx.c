@@ -299,6 +299,7 @@ int fcfcg_bins_info_get(const fcfcg_ctx *c, fcfcg_bins_info *o) {
   for (int k = 0; k < 3; k++) o->box_rescaled[k] = b->box[k];
   o->nstab = b->s.nrtab;
   o->nptab = (b->bintype == FCFCG_BIN_SPI) ? b->p.nrtab : 0;
+  o->ftab_cells_per_octave = b->s.flog ? 1 << (23 - b->s.flog) : 0;
   return FCFCG_OK;
 }
 
@@ -893,8 +894,9 @@ static int fp32_bounds(const fcfcg_ctx *c, const grid_t *g, double dmax,
    * up -- values below it are sent to the recheck */
   L->fsamb = L->fpamb = -1.f;
   if (b->s.flog) {
-    /* the window the s-axis lookups use at value v (an upper bound) */
-    const int varies = (b->bintype != FCFCG_BIN_ISO);
+    /* the window the s-axis lookups use at value v (an upper bound): with
+     * a bit-pattern table every kernel variant takes it per pair */
+    const int varies = 1;
     const double p2 = (b->bintype == FCFCG_BIN_SPI && !box) ? b->p.vmax : 0;
     double amb = -1;
     for (long c = b->s.nftab - 1; c >= 0; c--) {

@@ -102,6 +102,9 @@ typedef struct {
   double rescale;        /* coordinate rescale factor */
   double box_rescaled[3];
   int64_t nstab, nptab;  /* lookup-table lengths */
+  int ftab_cells_per_octave;  /* the FP32 s (or s_perp) window table: cells
+                                 per octave of a bit-pattern table (log bins
+                                 in a box), 0 for a uniform table */
 } fcfcg_bins_info;
 
 /* Counters of the last fcfcg_count() call. */

@@ -185,3 +185,29 @@ def test_config_errors():
         with pytest.raises(fg.FCFCGError) as e:
             fg.PairCounter(host_only=True, **kw)
         assert e.value.code == fg.capi.ERR_CFG
+
+
+def test_fp32_table_kind():
+    """Log s bins in a box get a bit-pattern FP32 window table (a fixed
+    number of cells per octave, at most one edge per cell); linear bins and
+    surveys keep the uniform table."""
+    import fcfc_gb300 as fg
+    log = np.geomspace(0.1, 50, 31)
+    cases = [
+        (dict(geometry="box", bintype=0, box=200.0, sedges=log), True),
+        (dict(geometry="box", bintype=1, box=200.0, sedges=log, nmu=10), True),
+        (dict(geometry="box", bintype=2, box=200.0, sedges=log, pmin=0,
+              pmax=20, dpi=1), True),
+        (dict(geometry="survey", bintype=2, sedges=log, pmin=0, pmax=20,
+              dpi=1), False),
+        (dict(geometry="box", bintype=1, box=200.0, smin=0, smax=50, ds=5,
+              nmu=10), False),
+    ]
+    for kw, want in cases:
+        pc = fg.PairCounter(host_only=True, **kw)
+        cpo = pc.info.ftab_cells_per_octave
+        assert (cpo > 0) == want, (kw, cpo)
+        if want:
+            # edges a factor 1.23 apart: 16 cells per octave resolve them
+            assert 16 <= cpo <= 1 << 15
+        pc.close()

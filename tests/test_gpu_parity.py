@@ -91,6 +91,7 @@ CONFIGS = [
     ("box_spi_log", "box", 2, dict(sedges=np.geomspace(0.2, 30, 16), pmin=0,
                                    pmax=25, dpi=2.5)),
     ("box_iso_log", "box", 0, dict(sedges=np.geomspace(0.05, 30, 25))),
+    ("box_smu_log", "box", 1, dict(sedges=np.geomspace(0.1, 40, 30), nmu=12)),
 ]
 
 
