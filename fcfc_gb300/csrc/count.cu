@@ -935,6 +935,9 @@ k_count32(const fcfcg_launch L) {
     }
     __syncthreads();
     const uint32_t total = S.pre[L.nsten];
+    /* neighbour positions [0, pin): cells whose pairs with the chunk's cell
+     * all lie within the outer range (their stencil entries come first) */
+    const uint32_t pin = S.pre[L.nin];
     if (warp == 0 && lane == 0) n_cand += (unsigned long long) m * total;
     uint32_t n_in = 0, n_q = 0;
 
@@ -994,12 +997,23 @@ k_count32(const fcfcg_launch L) {
                                    __int_as_float(wq.y), 0.f);
         }
       }
-      /* compare with every chunk point (two 32-point halves) */
-      const uint32_t m0 = scan_chunk<GEOM, BIN>(L, S.a, 0, min(m, 32), ilim,
-                                                bx, by, bz);
-      const uint32_t m1 = (m > 32) ? scan_chunk<GEOM, BIN>(L, S.a, 32, m,
-                                                          ilim, bx, by, bz)
-                                   : 0u;
+      /* compare with every chunk point (two 32-point halves); in weighted
+       * counts a block wholly in cells within range takes every chunk point
+       * (below ilim) without a test -- the binning checks each pair anyway
+       * (measured: 1-2 % faster weighted; the unweighted kernel's code runs
+       * 6 % slower with the branch, so it keeps the test) */
+      uint32_t m0, m1;
+      if (WT && base + 32u <= pin) {
+        const int lim = min(ilim, m);
+        m0 = (lim <= 0) ? 0u : (lim >= 32 ? ~0u : (1u << lim) - 1u);
+        m1 = (lim <= 32) ? 0u
+                         : (lim >= 64 ? ~0u : (1u << (lim - 32)) - 1u);
+      } else {
+        m0 = scan_chunk<GEOM, BIN>(L, S.a, 0, min(m, 32), ilim, bx, by, bz);
+        m1 = (m > 32) ? scan_chunk<GEOM, BIN>(L, S.a, 32, m, ilim, bx, by,
+                                              bz)
+                      : 0u;
+      }
       /* compact the block's in-range pairs into the queue, QCAP per round */
       const uint32_t cnt = __popc(m0) + __popc(m1);
       uint32_t inc = cnt;

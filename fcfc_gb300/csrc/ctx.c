@@ -684,11 +684,17 @@ static int grid_setup(fcfcg_ctx *c, grid_t *g, const slot_t *A,
 }
 
 /* Cell offsets whose cell pairs can hold a counted pair; half of them (with
- * the zero offset) for auto counts.  D = -offset * cell width. */
+ * the zero offset) for auto counts.  D = -offset * cell width.  The offsets
+ * whose cell pairs lie entirely within the counting range (for cells up to
+ * cw_far wide; NULL: the grid's) come first, nin of them: their candidates
+ * need no distance test (the binning still checks every pair). */
 static int stencil_build(fcfcg_ctx *c, const grid_t *g, int isauto, int *sten,
-    float *stD, int *nsten, double *dmax) {
+    float *stD, int *nsten, double *dmax, const double *cw_far, int *nin) {
   const fcfcg_bins *b = &c->bins;
   const int box = (b->geometry == FCFCG_GEOM_BOX);
+  if (!cw_far) cw_far = g->cw;
+  unsigned char *ins = malloc(FCFCG_MAX_STENCIL);
+  if (!ins) return FCFCG_ERR_MEMORY;
   const double margin = 1 + 1e-9;
   int r[3];
   for (int d = 0; d < 3; d++) {
@@ -729,8 +735,19 @@ static int stencil_build(fcfcg_ctx *c, const grid_t *g, int isauto, int *sten,
         }
         if (cnt >= FCFCG_MAX_STENCIL) {
           set_err(c, "cell stencil too large");
+          free(ins);
           return FCFCG_ERR_UNSUPPORTED;
         }
+        /* every pair of the cell pair within range (outer limits only) */
+        double fz[3];
+        for (int d = 0; d < 3; d++) fz[d] = (abs(o[d]) + 1) * cw_far[d];
+        if (b->bintype == FCFCG_BIN_SPI && box)
+          ins[cnt] = (fz[0] * fz[0] + fz[1] * fz[1] < b->s.vmax) &&
+                     (fz[2] < b->p.vmax);
+        else
+          ins[cnt] = (fz[0] * fz[0] + fz[1] * fz[1] + fz[2] * fz[2] <
+                      ((b->bintype == FCFCG_BIN_SPI) ? b->s.vmax + b->p.vmax
+                                                     : b->s.vmax));
         sten[4 * cnt + 0] = ox;
         sten[4 * cnt + 1] = oy;
         sten[4 * cnt + 2] = oz;
@@ -743,7 +760,32 @@ static int stencil_build(fcfcg_ctx *c, const grid_t *g, int isauto, int *sten,
         stD[4 * cnt + 3] = 0;
         cnt++;
       }
+  /* the offsets within range first (stable) */
+  int *ts = malloc(sizeof(int) * 4 * (cnt ? cnt : 1));
+  float *td = malloc(sizeof(float) * 4 * (cnt ? cnt : 1));
+  if (!ts || !td) {
+    free(ts);
+    free(td);
+    free(ins);
+    return FCFCG_ERR_MEMORY;
+  }
+  int k = 0;
+  for (int pass = 1; pass >= 0; pass--)
+    for (int t = 0; t < cnt; t++)
+      if (ins[t] == pass) {
+        memcpy(ts + 4 * k, sten + 4 * t, sizeof(int) * 4);
+        memcpy(td + 4 * k, stD + 4 * t, sizeof(float) * 4);
+        k++;
+      }
+  int n1 = 0;
+  for (int t = 0; t < cnt; t++) n1 += ins[t];
+  memcpy(sten, ts, sizeof(int) * 4 * cnt);
+  memcpy(stD, td, sizeof(float) * 4 * cnt);
+  free(ts);
+  free(td);
+  free(ins);
   *nsten = cnt;
+  *nin = n1;
   return FCFCG_OK;
 }
 
@@ -1065,7 +1107,7 @@ typedef struct {
   int hwa, hwb;
   int isauto, withwt, prec;
   grid_t g;
-  int nsten;
+  int nsten, nin;                /* stencil entries, those within range */
   uint32_t ncell;
   size_t st;                     /* scan scratch length of the chunk list */
   fcfcg_launch L;                /* stencil pointers: set by the caller */
@@ -1090,7 +1132,8 @@ static int count_plan_make(fcfcg_ctx *c, slot_t *A, slot_t *B, int isauto,
   grid_t *g = &P->g;
   if ((rc = grid_setup(c, g, A, B))) return rc;
   double dmax = 0;
-  if ((rc = stencil_build(c, g, isauto, sten, stD, &P->nsten, &dmax)))
+  if ((rc = stencil_build(c, g, isauto, sten, stD, &P->nsten, &dmax, NULL,
+                         &P->nin)))
     return rc;
   if ((rc = slot_reserve(c, A, g))) return rc;
   if (B != A && (rc = slot_reserve(c, B, g))) return rc;
@@ -1115,6 +1158,7 @@ static int count_plan_make(fcfcg_ctx *c, slot_t *A, slot_t *B, int isauto,
     L->lof[d] = (float) g->lo[d];
   }
   L->nsten = P->nsten;
+  L->nin = P->nin;
   L->tzero = -1;
   for (int t = 0; t < P->nsten; t++)
     if (!sten[4 * t] && !sten[4 * t + 1] && !sten[4 * t + 2]) L->tzero = t;
@@ -2012,7 +2056,9 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
     free(hbase);
     goto out;
   }
-  if ((rc = stencil_build(c, &gmin, 1, c->sten, c->stD, &nsten, &dmin))) {
+  int nin = 0;
+  if ((rc = stencil_build(c, &gmin, 1, c->sten, c->stD, &nsten, &dmin,
+                          gmax.cw, &nin))) {
     free(wexp);
     free(hbase);
     goto out;
@@ -2143,6 +2189,7 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
   const size_t hbytes = (size_t) b->ntot * (withwt ? 8 : 4);
   L.hist_smem = (tabbytes + stage + hbytes <= 200 * 1024);
   L.nsten = nsten;
+  L.nin = nin;
   L.tzero = -1;
   for (int t = 0; t < nsten; t++)
     if (!c->sten[4 * t] && !c->sten[4 * t + 1] && !c->sten[4 * t + 2])

@@ -106,6 +106,7 @@ typedef struct {
   float cwf[3], lof[3];
   /* stencil: nsten entries of int4 (ox, oy, oz, 0) and float4 (-o * cw) */
   int nsten;
+  int nin;          /* the first nin entries: cell pairs within range */
   const int *sten;
   const float *stenD;
   /* chunks: uint4 (cell, first sorted index, count, 0); their number is
