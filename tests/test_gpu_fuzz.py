@@ -12,7 +12,7 @@ from oracle import fcfc_oracle as fo
 
 pytestmark = pytest.mark.gpu
 
-NCASE = 48
+NCASE = 96
 
 
 def _bins(rng, geom, bt):
