@@ -937,21 +937,19 @@ static int fp32_bounds(const fcfcg_ctx *c, const grid_t *g, double dmax,
   L->fsamb = L->fpamb = -1.f;
   if (b->s.flog) {
     /* the window the s-axis lookups use at value v (an upper bound): with
-     * a bit-pattern table every kernel variant takes it per pair */
-    const int varies = 1;
+     * a bit-pattern table every kernel variant takes it per pair (only
+     * boxes get such tables, so p2, for a survey's s_perp^2 = s^2 - pi^2,
+     * is 0 today) */
     const double p2 = (b->bintype == FCFCG_BIN_SPI && !box) ? b->p.vmax : 0;
     double amb = -1;
     for (long c = b->s.nftab - 1; c >= 0; c--) {
       const double x0 = ftab_cell_value(b->s.foff + c, b->s.flog);
       const double x1 = ftab_cell_value(b->s.foff + c + 1, b->s.flog);
-      double W = L->Emax;
-      if (varies) {
-        const double v = x1 + p2;
-        W = (double) L->K2 * v + (double) L->K1 * sqrt(v) + (double) L->K0;
-        if (p2 > 0)
-          W += (double) L->P2 * v + (double) L->P1 * sqrt(v) + (double) L->P0;
-        W *= 1.01;
-      }
+      const double v = x1 + p2;
+      double W = (double) L->K2 * v + (double) L->K1 * sqrt(v) + (double) L->K0;
+      if (p2 > 0)
+        W += (double) L->P2 * v + (double) L->P1 * sqrt(v) + (double) L->P0;
+      W *= 1.01;
       if (!(W < 0.45 * (x1 - x0))) {
         amb = x1;
         break;
