@@ -2,7 +2,9 @@
 refinement (1 to 8 cells per maximum separation), clustered or uniform
 catalogues, weights, auto and cross counts.  The FP32 + FP64-recheck path
 must give exactly the all-FP64 path's integer counts, and its weighted sums
-within 1e-10; every tenth case is also checked against the oracle."""
+within 1e-10; every tenth case is also checked against the oracle.  The
+adjoint is checked against the oracle's per-object gradients over random
+binnings and geometries as well."""
 import zlib
 
 import numpy as np
@@ -114,5 +116,55 @@ def test_fp32_recheck_equals_fp64(case):
         # only a fine refinement can make a stencil beyond the limit, and it
         # is refused cleanly
         assert k >= 6 and "stencil" in str(e), (k, str(e))
+    finally:
+        pc.close()
+
+
+@pytest.mark.parametrize("case", range(16))
+def test_adjoint_random_matches_oracle(case):
+    """Weight gradients (fcfcg_adjoint) over random binnings and geometries,
+    log bins included (the bit-pattern table variants in boxes), against the
+    oracle's per-object FP64 gradients."""
+    import fcfc_gb300 as fg
+    from fcfc_gb300 import synth
+    rng = np.random.default_rng(zlib.crc32(b"adj%d" % case))
+    geom = "box" if case % 2 == 0 else "survey"
+    bt = int(rng.integers(0, 3))
+    kw = _bins(rng, geom, bt)
+    if geom == "box":
+        L = float(rng.uniform(100, 200))
+        a = synth.neyman_scott(int(rng.integers(10, 60)), L, 30, 3.0,
+                               seed=int(rng.integers(1 << 30)))
+        b = synth.uniform_box(int(rng.integers(500, 2000)), L,
+                              seed=int(rng.integers(1 << 30)))
+        pc = fg.PairCounter("box", bt, box=L, **kw)
+        ob = fo.Bins(False, bt, box=L, **_oracle_kw(kw))
+    else:
+        sk = dict(ra=(150.0, 160.0), dec=(10.0, 18.0), zmu=0.5, zsig=0.05,
+                  zr=(0.45, 0.55))
+        a = synth.radecz_to_xyz(synth.survey_radecz(
+            int(rng.integers(500, 2500)), seed=int(rng.integers(1 << 30)),
+            **sk))
+        b = synth.radecz_to_xyz(synth.survey_radecz(
+            int(rng.integers(500, 2500)), seed=int(rng.integers(1 << 30)),
+            **sk))
+        pc = fg.PairCounter("survey", bt, **kw)
+        ob = fo.Bins(True, bt, **_oracle_kw(kw))
+    wa = rng.lognormal(0, 0.3, len(a))
+    wb = rng.uniform(0.5, 1.5, len(b))
+    pc.load(0, a, wa)
+    pc.load(1, b, wb)
+    g = rng.normal(size=pc.ntot)
+    try:
+        got, _ = pc.adjoint(0, None, g)
+        want, _ = ob.adjoint(a, g, wa=wa)
+        np.testing.assert_allclose(got, want, rtol=1e-10,
+                                   atol=1e-12 * max(1.0, np.abs(want).max()))
+        got_a, got_b = pc.adjoint(0, 1, g)
+        want_a, want_b = ob.adjoint(a, g, b=b, wa=wa, wb=wb)
+        np.testing.assert_allclose(got_a, want_a, rtol=1e-10,
+                                   atol=1e-12 * max(1.0, np.abs(want_a).max()))
+        np.testing.assert_allclose(got_b, want_b, rtol=1e-10,
+                                   atol=1e-12 * max(1.0, np.abs(want_b).max()))
     finally:
         pc.close()
