@@ -40,6 +40,8 @@
 #define IS_ISO(B) ((B) == FCFCG_BIN_ISO || (B) == BIN_ISOL)
 #define IS_SMU(B) ((B) == FCFCG_BIN_SMU || (B) == BIN_SMUL)
 #define LOGTAB(B) ((B) >= BIN_SPIL)
+/* survey (s_perp, pi): the scan applies the line-of-sight prefilter */
+#define LOSCUT(G, B) ((G) == FCFCG_GEOM_SURVEY && (B) == FCFCG_BIN_SPI)
 
 #define CT_THREADS 256
 #define FULLMASK 0xffffffffu
@@ -711,11 +713,14 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
 }
 
 /* Compare a neighbour point (one per lane) with chunk points [i0, i1):
- * bit i - i0 of the result marks a candidate inside the outer range. */
+ * bit i - i0 of the result marks a candidate inside the outer range.  For
+ * survey (s_perp, pi) counts (u, lh, lP) is the lane's line-of-sight
+ * prefilter: a pair is dropped when |d.u| >= lP + lh s^2, where its pi
+ * exceeds pi_max for sure. */
 template <int GEOM, int BIN, bool LIMIT>
 __device__ __forceinline__ uint32_t scan_chunk_(const fcfcg_launch &L,
     const float4 *a, int i0, int i1, int ilim, float bx, float by,
-    float bz) {
+    float bz, float ux, float uy, float uz, float lh, float lP) {
   uint32_t msk = 0;
   const float s_lim = L.s_lim, p_lim = L.p_lim;
 #pragma unroll 4
@@ -726,6 +731,10 @@ __device__ __forceinline__ uint32_t scan_chunk_(const fcfcg_launch &L,
     if (IS_SPI(BIN) && GEOM == FCFCG_GEOM_BOX) {
       const float v = fmaf(dy, dy, dx * dx);
       inr = (fabsf(dz) < p_lim) & (v < s_lim);
+    } else if (LOSCUT(GEOM, BIN)) {
+      const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+      const float t = fmaf(dz, uz, fmaf(dy, uy, dx * ux));
+      inr = (v < s_lim) & (fabsf(t) < fmaf(v, lh, lP));
     } else {
       const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
       inr = v < s_lim;
@@ -740,10 +749,12 @@ __device__ __forceinline__ uint32_t scan_chunk_(const fcfcg_launch &L,
 template <int GEOM, int BIN>
 __device__ __forceinline__ uint32_t scan_chunk(const fcfcg_launch &L,
     const float4 *a, int i0, int i1, int ilim, float bx, float by,
-    float bz) {
+    float bz, float ux, float uy, float uz, float lh, float lP) {
   if (__all_sync(FULLMASK, ilim >= i1))
-    return scan_chunk_<GEOM, BIN, false>(L, a, i0, i1, ilim, bx, by, bz);
-  return scan_chunk_<GEOM, BIN, true>(L, a, i0, i1, ilim, bx, by, bz);
+    return scan_chunk_<GEOM, BIN, false>(L, a, i0, i1, ilim, bx, by, bz, ux,
+                                         uy, uz, lh, lP);
+  return scan_chunk_<GEOM, BIN, true>(L, a, i0, i1, ilim, bx, by, bz, ux, uy,
+                                      uz, lh, lP);
 }
 
 /*
@@ -951,6 +962,7 @@ k_count32(const fcfcg_launch L) {
       if (base >= total) break;
       const uint32_t p = base + (uint32_t) lane;
       float bx = 0.f, by = 0.f, bz = 0.f;
+      float ux = 0.f, uy = 0.f, uz = 0.f, lh = 0.f, lP = 0.f;
       int ilim = 0;
       uint32_t bjl = 0;
       if (p < total) {
@@ -985,6 +997,22 @@ k_count32(const fcfcg_launch L) {
         bx = pb.x - D.x;
         by = pb.y - D.y;
         bz = pb.z - D.z;
+        if (LOSCUT(GEOM, BIN)) {
+          /* x_b = (bx, by, bz) + c_A: its direction and 1 / |x_b| */
+          const float xx = fmaf(0.5f, c2x, bx), xy = fmaf(0.5f, c2y, by),
+                      xz = fmaf(0.5f, c2z, bz);
+          const float r2 = fmaf(xz, xz, fmaf(xy, xy, xx * xx));
+          if (r2 > L.los_r2min) {
+            const float ir = rsqrtf(r2);
+            ux = xx * ir;
+            uy = xy * ir;
+            uz = xz * ir;
+            lh = L.los_h * ir;
+            lP = fmaf(L.los_pr, ir, L.los_p);
+          } else {
+            lP = FLT_MAX;   /* near the observer: no prefilter */
+          }
+        }
         ilim = m;
         if (L.isauto && t == L.tzero) ilim = min(m, (int) jc - aoff);
         S.b[lane] = make_float4(bx, by, bz, __uint_as_float(bj));
@@ -1003,15 +1031,16 @@ k_count32(const fcfcg_launch L) {
        * (measured: 1-2 % faster weighted; the unweighted kernel's code runs
        * 6 % slower with the branch, so it keeps the test) */
       uint32_t m0, m1;
-      if (WT && base + 32u <= pin) {
+      if (WT && !LOSCUT(GEOM, BIN) && base + 32u <= pin) {
         const int lim = min(ilim, m);
         m0 = (lim <= 0) ? 0u : (lim >= 32 ? ~0u : (1u << lim) - 1u);
         m1 = (lim <= 32) ? 0u
                          : (lim >= 64 ? ~0u : (1u << (lim - 32)) - 1u);
       } else {
-        m0 = scan_chunk<GEOM, BIN>(L, S.a, 0, min(m, 32), ilim, bx, by, bz);
+        m0 = scan_chunk<GEOM, BIN>(L, S.a, 0, min(m, 32), ilim, bx, by, bz,
+                                   ux, uy, uz, lh, lP);
         m1 = (m > 32) ? scan_chunk<GEOM, BIN>(L, S.a, 32, m, ilim, bx, by,
-                                              bz)
+                                              bz, ux, uy, uz, lh, lP)
                       : 0u;
       }
       /* compact the block's in-range pairs into the queue, QCAP per round */

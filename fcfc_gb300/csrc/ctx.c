@@ -922,6 +922,19 @@ static int fp32_bounds(const fcfcg_ctx *c, const grid_t *g, double dmax,
       Es = L->K2 * r2 + L->K1 * sqrt(r2) + L->K0 + Ep;
       L->s_lim = (float) (r2 + Es + 1e-6 * (1 + r2));
       L->p_lim = 0;
+      /* line-of-sight prefilter.  With m = x_a + x_b = 2 x_b + d,
+       * pi = |d.m| / |m| and |m| <= 2 |x_b| + s, pi < pi_max implies
+       *   |d.u_b| < pi_max + (pi_max s + s^2) / (2 |x_b|),
+       * and s <= Rs, the outer range.  The constants carry a factor
+       * 1 + 2^-8 and an absolute slack far above the FP32 rounding of d,
+       * u_b and |x_b| (below 1e-5 relative where the test applies,
+       * |x_b| >= Rs) */
+      const double pm = sqrt(b->p.vmax), Rs = sqrt((double) L->s_lim);
+      const double f = 1 + ldexp(1.0, -8);
+      L->los_p = (float) (pm * f + ldexp(Rs, -12) + 1e-6);
+      L->los_pr = (float) (0.5 * f * pm * Rs);
+      L->los_h = (float) (0.5 * f);
+      L->los_r2min = (float) (Rs * Rs);
     }
   } else {
     L->s_lim = (float) (smax2 + Es + 1e-6 * (1 + smax2));

@@ -130,6 +130,10 @@ typedef struct {
   const float *fse, *fpe;      /* FP32 edges (nbin + 1 each) */
   int nsb, npb;                /* bins of the s and pi axes */
   float s_lim, p_lim;          /* values at/above: out of range for sure */
+  /* survey (s_perp, pi): a pair with |d.u_b| >= los_p + (los_pr + los_h
+   * s^2) / |x_b| (u_b = x_b / |x_b|) has pi >= pi_max for sure; the test
+   * is skipped for |x_b|^2 <= los_r2min */
+  float los_p, los_pr, los_h, los_r2min;
   float K0, K1, K2;            /* E(s^2) = K2 s^2 + K1 s + K0 */
   float P0, P1, P2;            /* E(pi) (box) or E(pi^2) (survey) */
   float Q0, Q1, Q2;            /* E(q), q = nmu mu: Q1 / s + Q2 q + Q0 */

@@ -176,6 +176,53 @@ def test_survey_vs_oracle(cfg, weighted):
                        "%s DR prec %d" % (name, prec))
 
 
+def test_survey_spi_line_of_sight_prefilter():
+    """(s_perp, pi) in a survey: the FP32 kernel drops pairs whose pi is
+    beyond pi_max for sure, judging the line of sight by one point's
+    direction.  Objects around the observer (where that test is switched
+    off), at the origin itself, and pairs placed with pi just inside and
+    just outside pi_max must give the oracle's counts."""
+    import fcfc_gb300 as fg
+    rng = np.random.default_rng(41)
+    pmax, spmax = 30.0, 30.0
+    ball = rng.normal(size=(2500, 3))
+    ball *= (80.0 * rng.random(2500) ** (1 / 3) / np.linalg.norm(ball, axis=1))[:, None]
+    far = rng.normal(size=(1500, 3))
+    far *= (rng.uniform(250, 400, 1500) / np.linalg.norm(far, axis=1))[:, None]
+    # pairs straddling pi = pi_max along their own line of sight
+    n = 400
+    u = rng.normal(size=(n, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    xb = u * rng.uniform(100, 2000, n)[:, None]
+    perp = rng.normal(size=(n, 3))
+    perp -= (perp * u).sum(1)[:, None] * u
+    perp /= np.linalg.norm(perp, axis=1)[:, None]
+    dpi = pmax + rng.choice([-1e-3, -1e-7, 0.0, 1e-7, 1e-3, 0.5], n)
+    dpi *= rng.choice([-1.0, 1.0], n)
+    d = dpi[:, None] * u + perp * rng.uniform(0, spmax, n)[:, None]
+    # x_a - x_b = d with the pair's line of sight x_a + x_b along u:
+    # x_a = c + d / 2, x_b = c - d / 2 for a centre c on u
+    xa2, xb2 = xb + 0.5 * d, xb - 0.5 * d
+    x = np.concatenate([ball, [[0.0, 0.0, 0.0]], far, xa2, xb2])
+    y = np.concatenate([rng.normal(size=(2000, 3)) * 40.0, xb2])
+    w = rng.uniform(0.3, 1.7, len(x))
+    kw = dict(smin=0, smax=spmax, ds=3, pmin=0, pmax=pmax, dpi=3)
+    pc = fg.PairCounter("survey", 2, **kw)
+    lib = fg.capi.load_library()
+    ob = fo.Bins(True, 2, ns=lib.fcfcg_linear_nbin(0, spmax, 3), smin=0, ds=3,
+                 np_=lib.fcfcg_linear_nbin(0, pmax, 3), pmin=0, dpi=3)
+    pc.load(0, x, w)
+    pc.load(1, y, None)
+    for weighted in (False, True):
+        _assert_counts(pc.count_pairs(0, weighted=weighted, precision=0),
+                       ob.count(x, wa=w, weighted=weighted), weighted,
+                       "los DD")
+        assert pc.stats()["precision_used"] == 0
+        _assert_counts(pc.count_pairs(0, 1, weighted=weighted, precision=0),
+                       ob.count(x, y, wa=w, weighted=weighted), weighted,
+                       "los DR")
+
+
 def test_edge_cases():
     """Empty and single-object catalogues, duplicate points (s = 0), points
     on the box faces and on cell boundaries."""
