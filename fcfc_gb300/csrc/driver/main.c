@@ -21,6 +21,7 @@
  */
 #define _POSIX_C_SOURCE 200809L
 #include <ctype.h>
+#include <pthread.h>
 #include <math.h>
 #include <stdarg.h>
 #include <stdint.h>
@@ -246,46 +247,97 @@ static double *read_bins(const char *fname, int *nbin) {
   return e;
 }
 
-/* Read catalogue i (ASCII, FCFC's keys) into a slot of the context. */
-static void load_cat(fcfcg_ctx *ctx, const conf_t *C, int i, int slot,
-    int weighted, int cnvt, const fcfcg_cosmo *cosmo, char label,
-    int verbose) {
+/* Catalogue i read from its ASCII file into host arrays. */
+typedef struct {
+  const conf_t *C;
+  int i, weighted;
+  char label;
+  double *xyz[3], *w;
+  size_t n;
+  double secs;      /* reading time */
+  int rc;
+  char err[512];
+} cat_host_t;
+
+static double elapsed(const struct timespec *a, const struct timespec *b) {
+  return (double) (b->tv_sec - a->tv_sec) +
+         1e-9 * (double) (b->tv_nsec - a->tv_nsec);
+}
+
+static void read_cat(cat_host_t *r) {
+  const conf_t *C = r->C;
+  const int i = r->i;
   const char *pos[3] = {conf_str(C, "POSITION", 3 * i),
                         conf_str(C, "POSITION", 3 * i + 1),
                         conf_str(C, "POSITION", 3 * i + 2)};
   const char *fmtr = conf_str(C, "ASCII_FORMATTER", i);
-  if (!fmtr || !*fmtr) die("ASCII_FORMATTER is not set for catalogue %c", label);
   const char *cm = conf_str(C, "ASCII_COMMENT", i);
   const char *sel = conf_str(C, "SELECTION", i);
-  double *xyz[3], *w = NULL;
-  size_t n;
-  char err[512];
-  struct timespec t0, t1, t2;
+  struct timespec t0, t1;
+  r->w = NULL;
+  if (!fmtr || !*fmtr) {
+    snprintf(r->err, sizeof r->err,
+             "ASCII_FORMATTER is not set for catalogue %c", r->label);
+    r->rc = 1;
+    return;
+  }
   clock_gettime(CLOCK_MONOTONIC, &t0);
-  if (cat_read_ascii(conf_str(C, "CATALOG", i), fmtr, pos,
-                     weighted ? conf_str(C, "WEIGHT", i) : NULL,
-                     (sel && *sel) ? sel : NULL, conf_long(C, "ASCII_SKIP", i, 0),
-                     (cm && *cm) ? cm[0] : 0, xyz, &w, &n, err, sizeof err))
-    die("%s", err);
+  r->rc = cat_read_ascii(conf_str(C, "CATALOG", i), fmtr, pos,
+                         r->weighted ? conf_str(C, "WEIGHT", i) : NULL,
+                         (sel && *sel) ? sel : NULL,
+                         conf_long(C, "ASCII_SKIP", i, 0),
+                         (cm && *cm) ? cm[0] : 0, r->xyz, &r->w, &r->n,
+                         r->err, sizeof r->err);
+  clock_gettime(CLOCK_MONOTONIC, &t1);
+  r->secs = elapsed(&t0, &t1);
+}
+
+/* Host catalogue -> a slot of the context; the host arrays are freed. */
+static void upload_cat(fcfcg_ctx *ctx, cat_host_t *r, int slot, int cnvt,
+    const fcfcg_cosmo *cosmo, int verbose) {
+  if (r->rc) die("%s", r->err);
+  struct timespec t1, t2;
   clock_gettime(CLOCK_MONOTONIC, &t1);
   int rc;
   if (cnvt)
-    rc = fcfcg_load_catalog_radecz(ctx, slot, n, xyz[0], xyz[1], xyz[2], w,
-                                   cosmo);
+    rc = fcfcg_load_catalog_radecz(ctx, slot, r->n, r->xyz[0], r->xyz[1],
+                                   r->xyz[2], r->w, cosmo);
   else
-    rc = fcfcg_load_catalog(ctx, slot, n, xyz[0], xyz[1], xyz[2], w);
+    rc = fcfcg_load_catalog(ctx, slot, r->n, r->xyz[0], r->xyz[1], r->xyz[2],
+                            r->w);
   check(ctx, rc, "loading a catalogue");
-  free(xyz[0]);
-  free(xyz[1]);
-  free(xyz[2]);
-  free(w);
+  for (int k = 0; k < 3; k++) free(r->xyz[k]);
+  free(r->w);
   clock_gettime(CLOCK_MONOTONIC, &t2);
   if (verbose)
     printf("catalogue %c: %zu objects (read %.3f s, to the device %.3f s)\n",
-           label, n, (double) (t1.tv_sec - t0.tv_sec) +
-                         1e-9 * (double) (t1.tv_nsec - t0.tv_nsec),
-           (double) (t2.tv_sec - t1.tv_sec) +
-               1e-9 * (double) (t2.tv_nsec - t1.tv_nsec));
+           r->label, r->n, r->secs, elapsed(&t1, &t2));
+}
+
+static void load_cat(fcfcg_ctx *ctx, const conf_t *C, int i, int slot,
+    int weighted, int cnvt, const fcfcg_cosmo *cosmo, char label,
+    int verbose) {
+  cat_host_t r;
+  memset(&r, 0, sizeof r);
+  r.C = C;
+  r.i = i;
+  r.weighted = weighted;
+  r.label = label;
+  read_cat(&r);
+  upload_cat(ctx, &r, slot, cnvt, cosmo, verbose);
+}
+
+/* The catalogues of a run, read one after another on a helper thread while
+ * the main thread sets up the device (CUDA context, tables). */
+typedef struct {
+  cat_host_t *r;
+  int n;
+} prefetch_t;
+
+static void *prefetch_run(void *p) {
+  prefetch_t *P = (prefetch_t *) p;
+  for (int k = 0; k < P->n; k++) read_cat(P->r + k);
+  return NULL;
 }
 
 /* eval_pairs after the count: double auto counts, normalise, write the
@@ -316,6 +368,8 @@ static void finish_pair(fcfcg_ctx *ctx, const char *fn, int ofmt, int isauto,
 }
 
 int main(int argc, char **argv) {
+  struct timespec t_start, t_now;
+  clock_gettime(CLOCK_MONOTONIC, &t_start);
   const char *cfile = NULL;
   int prec = FCFCG_PREC_FP32_RECHECK, mu_one = 0, verbose = 0, graph = 1;
   for (int i = 1; i < argc; i++) {
@@ -401,9 +455,74 @@ int main(int argc, char **argv) {
       if (b.np < 1) die("invalid PI_BIN_MIN / PI_BIN_MAX / PI_BIN_SIZE");
     }
   }
+  /* the pairs, and which catalogues the counts need -- decided before the
+   * device set-up, so that reading the catalogues can overlap it */
+  const int npair = conf_len(&C, "PAIR_COUNT");
+  if (npair < 1) die("PAIR_COUNT is not set");
+  if (conf_len(&C, "PAIR_COUNT_FILE") < npair)
+    die("PAIR_COUNT_FILE needs one file per pair");
+  const int ofmt = (int) conf_long(&C, "OUTPUT_FORMAT", 0, 0);
+  const int ovw = (int) conf_long(&C, "OVERWRITE", 0, 0);
+  char labels[2 * 64 + 1];
+  int weighted[MAXCAT];
+  for (int i = 0; i < ncat; i++) {
+    const char *w = conf_str(&C, "WEIGHT", i);
+    weighted[i] = (conf_len(&C, "WEIGHT") && w && *w);
+  }
+  if (npair > 64) die("too many pairs");
+  /* pairs with an existing file (OVERWRITE <= 1) are read back */
+  int pia[64], pib[64], todo[64], ntodo = 0, existing[64];
+  for (int k = 0; k < npair; k++) {
+    const char *pr = conf_str(&C, "PAIR_COUNT", k);
+    const char *fn = conf_str(&C, "PAIR_COUNT_FILE", k);
+    if (!pr || strlen(pr) != 2) die("invalid PAIR_COUNT entry `%s'", pr ? pr : "");
+    labels[2 * k] = pr[0];
+    labels[2 * k + 1] = pr[1];
+    int ia = -1, ib = -1;
+    for (int i = 0; i < ncat; i++) {
+      if (label[i] == pr[0]) ia = i;
+      if (label[i] == pr[1]) ib = i;
+    }
+    if (ia < 0 || ib < 0) die("unknown catalogue label in PAIR_COUNT `%s'", pr);
+    pia[k] = ia;
+    pib[k] = ib;
+    existing[k] = file_exists(fn) && ovw <= 1;
+    if (!existing[k]) todo[ntodo++] = k;
+  }
+  /* the catalogues the counts need, in order of first use */
+  int slot_of[MAXCAT], use[MAXCAT], nuse = 0;
+  for (int i = 0; i < ncat; i++) slot_of[i] = -1;
+  for (int t = 0; t < ntodo; t++) {
+    const int need[2] = {pia[todo[t]], pib[todo[t]]};
+    for (int q = 0; q < 2; q++)
+      if (slot_of[need[q]] < 0) {
+        slot_of[need[q]] = nuse;
+        use[nuse++] = need[q];
+      }
+  }
+  /* every count at once when the catalogues fit the context's 8 slots:
+   * they are read on a helper thread meanwhile */
+  const int at_once = (ntodo > 0 && nuse <= 8 && graph);
+  cat_host_t pre[8];
+  prefetch_t pf = {pre, at_once ? nuse : 0};
+  pthread_t pf_tid;
+  int pf_started = 0;
+  memset(pre, 0, sizeof pre);
+  for (int u = 0; u < pf.n; u++) {
+    pre[u].C = &C;
+    pre[u].i = use[u];
+    pre[u].weighted = weighted[use[u]];
+    pre[u].label = label[use[u]];
+  }
+  if (pf.n > 0) pf_started = !pthread_create(&pf_tid, NULL, prefetch_run, &pf);
+
   fcfcg_ctx *ctx = NULL;
   int rc = fcfcg_create(&b, -1, &ctx);
   check(ctx, rc, "bin set-up");
+  if (verbose) {
+    clock_gettime(CLOCK_MONOTONIC, &t_now);
+    printf("bins and device set up at %.3f s\n", elapsed(&t_start, &t_now));
+  }
   fcfcg_bins_info info;
   check(ctx, fcfcg_bins_info_get(ctx, &info), "bin set-up");
   const long ntot = (long) info.ntot;
@@ -442,73 +561,39 @@ int main(int argc, char **argv) {
   }
 #endif
 
-  /* pairs and outputs */
-  const int npair = conf_len(&C, "PAIR_COUNT");
-  if (npair < 1) die("PAIR_COUNT is not set");
-  if (conf_len(&C, "PAIR_COUNT_FILE") < npair)
-    die("PAIR_COUNT_FILE needs one file per pair");
-  const int ofmt = (int) conf_long(&C, "OUTPUT_FORMAT", 0, 0);
-  const int ovw = (int) conf_long(&C, "OVERWRITE", 0, 0);
   double *ncnt_all = calloc((size_t) npair * ntot, sizeof(double));
   int64_t *icnt = malloc(sizeof(int64_t) * ntot);
   double *wcnt = malloc(sizeof(double) * ntot);
   double *tmp = malloc(sizeof(double) * ntot);
-  char labels[2 * 64 + 1];
-  int weighted[MAXCAT];
-  for (int i = 0; i < ncat; i++) {
-    const char *w = conf_str(&C, "WEIGHT", i);
-    weighted[i] = (conf_len(&C, "WEIGHT") && w && *w);
-  }
-  if (npair > 64) die("too many pairs");
-  /* the pairs; those with an existing file (OVERWRITE <= 1) are read back */
-  int pia[64], pib[64], todo[64], ntodo = 0;
+  if (!ncnt_all || !icnt || !wcnt || !tmp) die("out of memory");
   for (int k = 0; k < npair; k++) {
-    const char *pr = conf_str(&C, "PAIR_COUNT", k);
-    const char *fn = conf_str(&C, "PAIR_COUNT_FILE", k);
-    if (!pr || strlen(pr) != 2) die("invalid PAIR_COUNT entry `%s'", pr ? pr : "");
-    labels[2 * k] = pr[0];
-    labels[2 * k + 1] = pr[1];
-    int ia = -1, ib = -1;
-    for (int i = 0; i < ncat; i++) {
-      if (label[i] == pr[0]) ia = i;
-      if (label[i] == pr[1]) ib = i;
-    }
-    if (ia < 0 || ib < 0) die("unknown catalogue label in PAIR_COUNT `%s'", pr);
-    pia[k] = ia;
-    pib[k] = ib;
-    if (file_exists(fn) && ovw <= 1) {
-      int au, ww;
-      uint64_t nt[2];
-      double wtr[2], norm;
-      check(ctx, fcfcg_read_paircount(ctx, fn, &au, &ww, nt, wtr, &norm,
-                                      ncnt_all + (size_t) k * ntot, icnt, wcnt),
-            "reading an existing pair-count file");
-      if (verbose) printf("read %s from `%s'\n", pr, fn);
-      continue;
-    }
-    todo[ntodo++] = k;
-  }
-  /* the catalogues the counts need, in order of first use */
-  int slot_of[MAXCAT], use[MAXCAT], nuse = 0;
-  for (int i = 0; i < ncat; i++) slot_of[i] = -1;
-  for (int t = 0; t < ntodo; t++) {
-    const int need[2] = {pia[todo[t]], pib[todo[t]]};
-    for (int q = 0; q < 2; q++)
-      if (slot_of[need[q]] < 0) {
-        slot_of[need[q]] = nuse;
-        use[nuse++] = need[q];
-      }
+    if (!existing[k]) continue;
+    int au, ww;
+    uint64_t nt[2];
+    double wtr[2], norm;
+    check(ctx, fcfcg_read_paircount(ctx, conf_str(&C, "PAIR_COUNT_FILE", k),
+                                    &au, &ww, nt, wtr, &norm,
+                                    ncnt_all + (size_t) k * ntot, icnt, wcnt),
+          "reading an existing pair-count file");
+    if (verbose)
+      printf("read %s from `%s'\n", conf_str(&C, "PAIR_COUNT", k),
+             conf_str(&C, "PAIR_COUNT_FILE", k));
   }
   const fcfcg_cosmo *cs = NULL;
 #ifdef FCFCG_SURVEY
   cs = &cosmo;
 #endif
-  if (ntodo > 0 && nuse <= 8 && graph) {
+  if (at_once) {
     /* every count at once: the catalogues in slots 0 .. nuse - 1, the
      * counts (DD, DR, RR, ...) captured and run as one CUDA graph */
+    if (pf_started) pthread_join(pf_tid, NULL);
+    else prefetch_run(&pf);
+    if (verbose) {
+      clock_gettime(CLOCK_MONOTONIC, &t_now);
+      printf("catalogues read at %.3f s\n", elapsed(&t_start, &t_now));
+    }
     for (int u = 0; u < nuse; u++)
-      load_cat(ctx, &C, use[u], u, weighted[use[u]], CNVT(use[u]), cs,
-               label[use[u]], verbose);
+      upload_cat(ctx, pre + u, u, CNVT(use[u]), cs, verbose);
     fcfcg_count_item items[64];
     int64_t *ic = malloc(sizeof(int64_t) * (size_t) ntodo * ntot);
     double *wc = malloc(sizeof(double) * (size_t) ntodo * ntot);
@@ -530,8 +615,9 @@ int main(int argc, char **argv) {
     if (verbose) {
       fcfcg_stats st;
       fcfcg_stats_get(ctx, &st);
-      printf("%d counts in one CUDA graph: %.3f ms on the device\n", ntodo,
-             st.ms_total);
+      clock_gettime(CLOCK_MONOTONIC, &t_now);
+      printf("%d counts in one CUDA graph: %.3f ms on the device, done at "
+             "%.3f s\n", ntodo, st.ms_total, elapsed(&t_start, &t_now));
     }
     fcfcg_graph_destroy(gr);
     for (int t = 0; t < ntodo; t++) {
@@ -610,6 +696,10 @@ int main(int argc, char **argv) {
       if (wf) check(ctx, fcfcg_write_wp(ctx, wf, wp), "writing PROJECTED_FILE");
       free(wp);
     }
+  }
+  if (verbose) {
+    clock_gettime(CLOCK_MONOTONIC, &t_now);
+    printf("done at %.3f s\n", elapsed(&t_start, &t_now));
   }
   fcfcg_destroy(ctx);
   free(rr);
