@@ -32,7 +32,8 @@ from .engine import PairCounter
 
 def parse_conf(text: str) -> dict:
     """libcfg syntax: KEY = value or [a, b, ...]; '#' comments; '\\' joins
-    lines; values may be quoted."""
+    lines; values may be quoted.  A key given twice keeps its first value,
+    as libcfg does (src/lib/libcfg.c:1219-1232)."""
     out = {}
     text = re.sub(r"\\\s*\n", " ", text)
     for line in text.splitlines():
@@ -44,7 +45,7 @@ def parse_conf(text: str) -> dict:
         k, v = s.split("=", 1)
         k = k.strip()
         v = _strip_comment(v).strip()
-        if not v:
+        if not v or k in out:
             continue
         if v.startswith("["):
             inner = v[1:v.rindex("]")] if "]" in v else v[1:]

@@ -51,3 +51,74 @@ def test_runner_rejects_data_struct():
                              "DATA_STRUCT = 2\nPAIR_COUNT = [AA]\n")
     with pytest.raises(FCFCGError, match="DATA_STRUCT"):
         runner.run(conf, "box")
+
+
+def _base_conf(extra=""):
+    return ("CATALOG = [a.txt]\nPOSITION = [$1, $2, $3]\nBOX_SIZE = 100\n"
+            "BINNING_SCHEME = 0\nSEP_BIN_MIN = 0\nSEP_BIN_MAX = 10\n"
+            "SEP_BIN_SIZE = 1\n" + extra)
+
+
+def test_version_and_template(drivers):
+    for exe, key in zip(drivers, ("BOX_SIZE", "OMEGA_M")):
+        r = subprocess.run([exe, "-V"], capture_output=True, text=True)
+        assert r.returncode == 0 and r.stdout
+        r = subprocess.run([exe, "--template"], capture_output=True, text=True)
+        assert r.returncode == 0
+        for k in ("CATALOG", "POSITION", "SEP_BIN_MIN", "PAIR_COUNT_FILE",
+                  "VERBOSE", key):
+            assert "\n%s = " % k in r.stdout, k
+
+
+def test_command_line_beats_the_file(drivers, tmp_path):
+    """FCFC's option table and libcfg's rules: an option sets its key over
+    the file's value, in the -x VALUE, -x=VALUE, --long VALUE and
+    --long=VALUE forms."""
+    conf = tmp_path / "c.conf"
+    conf.write_text(_base_conf("DATA_STRUCT = 2\n"))
+    r = subprocess.run([drivers[0], "-c", str(conf)], capture_output=True,
+                       text=True)
+    assert r.returncode != 0 and "DATA_STRUCT" in r.stderr
+    for opt in (["-S", "0"], ["-S=1"], ["--data-struct", "0"],
+                ["--data-struct=1"]):
+        r = subprocess.run([drivers[0], "-c", str(conf)] + opt,
+                           capture_output=True, text=True)
+        # past the bins: the next missing key is reported
+        assert r.returncode != 0 and "PAIR_COUNT" in r.stderr, (opt, r.stderr)
+    # a command line value also wins when it comes before -c
+    r = subprocess.run([drivers[0], "--data-struct=0", "--conf", str(conf)],
+                       capture_output=True, text=True)
+    assert "PAIR_COUNT" in r.stderr, r.stderr
+
+
+def test_first_value_of_a_key_is_kept(drivers, tmp_path):
+    """A key given twice in the file keeps its first value (libcfg warns
+    about the duplicate); twice on the command line likewise."""
+    conf = tmp_path / "c.conf"
+    conf.write_text(_base_conf("DATA_STRUCT = 0\nDATA_STRUCT = 2\n"))
+    r = subprocess.run([drivers[0], "-c", str(conf)], capture_output=True,
+                       text=True)
+    assert "PAIR_COUNT" in r.stderr and "duplicate" in r.stderr, r.stderr
+    conf.write_text(_base_conf())
+    r = subprocess.run([drivers[0], "-c", str(conf), "-S", "3", "-S", "0"],
+                       capture_output=True, text=True)
+    assert "DATA_STRUCT" in r.stderr and "duplicate" in r.stderr, r.stderr
+
+
+def test_options_without_a_configuration_file(drivers, tmp_path):
+    """No readable configuration file: a warning, and the run goes on with
+    the command line's keys alone."""
+    r = subprocess.run([drivers[0], "-i", "a.txt", "-x", "[$1, $2, $3]",
+                        "-b", "100", "-B", "0", "--s-min", "0", "--s-max",
+                        "10", "--s-step=1"], capture_output=True, text=True,
+                       cwd=str(tmp_path))
+    assert r.returncode != 0
+    assert "configuration file" in r.stderr and "PAIR_COUNT" in r.stderr, \
+        r.stderr
+    # a value-less non-Boolean option is an error; an unknown one a warning
+    r = subprocess.run([drivers[0], "-B"], capture_output=True, text=True,
+                       cwd=str(tmp_path))
+    assert r.returncode != 0 and "argument not found" in r.stderr
+    r = subprocess.run([drivers[0], "--no-such-option", "-B", "0"],
+                       capture_output=True, text=True, cwd=str(tmp_path))
+    assert "unrecognised" in r.stderr and "CATALOG" in r.stderr

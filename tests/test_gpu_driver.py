@@ -72,3 +72,60 @@ def test_driver_graph_and_per_count_paths_write_the_same_files(name, tmp_path):
     assert out["graph"].keys() == out["no-graph"].keys()
     for f in out["graph"]:
         assert out["graph"][f] == out["no-graph"][f], f
+
+
+# FCFC's long options and the keys they set (src/fcfc/2pt_box/load_conf.c:
+# 477-515, src/fcfc/2pt/load_conf.c:512-553)
+LONG_OPTS = {
+    "CATALOG": "input", "CATALOG_LABEL": "label", "CATALOG_TYPE": "type",
+    "ASCII_SKIP": "skip", "ASCII_COMMENT": "comment",
+    "ASCII_FORMATTER": "formatter", "POSITION": "position",
+    "WEIGHT": "weight", "SELECTION": "select", "COORD_CONVERT": "convert",
+    "OMEGA_M": "omega-m", "OMEGA_LAMBDA": "omega-l", "DE_EOS_W": "eos-w",
+    "CMVDST_ERR": "cmvdst-err", "Z_CMVDST_FILE": "cmvdst-file",
+    "BOX_SIZE": "box", "DATA_STRUCT": "data-struct",
+    "BINNING_SCHEME": "bin", "PAIR_COUNT": "pair",
+    "PAIR_COUNT_FILE": "pair-output", "CF_ESTIMATOR": "cf",
+    "CF_OUTPUT_FILE": "cf-output", "MULTIPOLE": "multipole",
+    "MULTIPOLE_FILE": "mp-output", "PROJECTED_CF": "wp",
+    "PROJECTED_FILE": "wp-output", "SEP_BIN_FILE": "s-file",
+    "SEP_BIN_MIN": "s-min", "SEP_BIN_MAX": "s-max", "SEP_BIN_SIZE": "s-step",
+    "MU_BIN_NUM": "mu-num", "PI_BIN_FILE": "pi-file", "PI_BIN_MIN": "pi-min",
+    "PI_BIN_MAX": "pi-max", "PI_BIN_SIZE": "pi-step",
+    "OUTPUT_FORMAT": "out-format", "OVERWRITE": "overwrite",
+    "VERBOSE": "verbose",
+}
+
+
+@pytest.mark.parametrize("name", case_names())
+def test_driver_from_command_line_options_alone(name, tmp_path):
+    """Every key of the golden case given as FCFC's long option, with no
+    configuration file: the same files as the configuration-file run."""
+    case = Case(name)
+    exe = os.path.join(BIN, "FCFC_2PT_BOX_GPU" if case.box else "FCFC_2PT_GPU")
+    extra = ["--with-mu-one"] if case.mu_one else []
+    out = {}
+    for mode in ("file", "options"):
+        d = tmp_path / mode
+        d.mkdir()
+        conf = _write_conf(case, str(d))
+        inputs = set(os.listdir(d))
+        if mode == "file":
+            cmd = [exe, "-c", conf]
+        else:
+            cmd = [exe]
+            for line in open(conf).read().splitlines():
+                if "=" not in line or line.lstrip().startswith("#"):
+                    continue
+                key, val = (t.strip() for t in line.split("=", 1))
+                cmd.append("--%s=%s" % (LONG_OPTS[key], val))
+            os.remove(conf)
+        r = subprocess.run(cmd + extra, capture_output=True, text=True,
+                           cwd=str(d))
+        assert r.returncode == 0, r.stderr
+        out[mode] = {f: open(os.path.join(d, f), "rb").read()
+                     for f in sorted(os.listdir(d))
+                     if f not in inputs}
+    assert out["file"].keys() == out["options"].keys() and out["file"]
+    for f in out["file"]:
+        assert out["file"][f] == out["options"][f], f
