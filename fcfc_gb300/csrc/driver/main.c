@@ -10,7 +10,7 @@
  * run's catalogues fit the context's 8 slots, all its counts -- DD, DR,
  * RR, ... -- go through one CUDA graph, fcfcg_graph_*), normalise
  * and save them (eval_pairs, save_res) or read an existing pair-count file
- * back (OVERWRITE <= 1, check_output); then evaluate CF_ESTIMATOR and write
+ * back (OVERWRITE = 1, check_output); then evaluate CF_ESTIMATOR and write
  * the correlation function, its multipoles or w_p (eval_cf).
  *
  * Built twice by fcfc_gb300/build.py: as FCFC_2PT_BOX_GPU and, with
@@ -28,8 +28,8 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
-#include <sys/stat.h>
 #include <time.h>
+#include <unistd.h>
 
 #include "../../../include/fcfcg.h"
 #include "catalog.h"
@@ -229,11 +229,6 @@ static int is_true(const char *s) {
                s[0] == 'y');
 }
 
-static int file_exists(const char *f) {
-  struct stat st;
-  return stat(f, &st) == 0;
-}
-
 /* ------------------------------------------------------------------------ */
 
 static void check(fcfcg_ctx *ctx, int rc, const char *what) {
@@ -354,6 +349,58 @@ static void *prefetch_run(void *p) {
   prefetch_t *P = (prefetch_t *) p;
   for (int k = 0; k < P->n; k++) read_cat(P->r + k);
   return NULL;
+}
+
+/* FCFC's check_output (src/fcfc/2pt_box/load_conf.c:582-650) for one output
+ * file: 0 to write it, 1 to read it back (an existing pair-count file with
+ * 0 < OVERWRITE < force); FCFC's refusals end the run.  force: 2 for
+ * PAIR_COUNT_FILE, 1 for the correlation function outputs.  A negative
+ * OVERWRITE asks on the terminal, up to |OVERWRITE| times. */
+static int check_output(const char *fname, const char *key, int ovw,
+    int force) {
+  if (!fname || !*fname) die("the output file %s is not set", key);
+  if (access(fname, F_OK) == 0) {
+    if (ovw < 0) {
+      fprintf(stderr, "Warning: the output file %s exists: `%s'\n", key,
+              fname);
+      int decided = 0;
+      for (int i = 0; i < -ovw && !decided; i++) {
+        fprintf(stderr, "Are you going to overwrite it? (y/n): ");
+        const int ch = getchar();
+        if (ch == EOF) continue;
+        for (int c = ch; c != '\n' && c != EOF;) c = getchar();
+        if (ch == 'n' || ch == 'N') {
+          ovw = force - 1;
+          decided = 1;
+        } else if (ch == 'y' || ch == 'Y') {
+          ovw = force;
+          decided = 1;
+        }
+      }
+      if (!decided) die("too many failed inputs");
+    }
+    if (ovw <= 0) die("abort to avoid overwriting %s: `%s'", key, fname);
+    if (ovw < force) {
+      if (access(fname, R_OK)) die("cannot access %s: `%s'", key, fname);
+      return 1;
+    }
+    fprintf(stderr, "Warning: %s will be overwritten: `%s'\n", key, fname);
+    if (access(fname, W_OK)) die("cannot write to file: `%s'", fname);
+  } else {
+    const char *sl = strrchr(fname, '/');
+    if (sl && sl > fname) {
+      char *dir = strndup(fname, (size_t) (sl - fname));
+      if (!dir) die("out of memory");
+      if (access(dir, X_OK)) die("cannot access the directory `%s'", dir);
+      free(dir);
+    }
+  }
+  return 0;
+}
+
+static int cmp_int(const void *a, const void *b) {
+  const int x = *(const int *) a, y = *(const int *) b;
+  return (x > y) - (x < y);
 }
 
 /* eval_pairs after the count: double auto counts, normalise, write the
@@ -666,16 +713,56 @@ int main(int argc, char **argv) {
     if (!pr || strlen(pr) != 2) die("invalid PAIR_COUNT entry `%s'", pr ? pr : "");
     labels[2 * k] = pr[0];
     labels[2 * k + 1] = pr[1];
+    /* a pair read back from its file needs no catalogue
+     * (load_conf.c:877-896) */
+    existing[k] = check_output(fn, "PAIR_COUNT_FILE", ovw, 2);
     int ia = -1, ib = -1;
     for (int i = 0; i < ncat; i++) {
       if (label[i] == pr[0]) ia = i;
       if (label[i] == pr[1]) ib = i;
     }
-    if (ia < 0 || ib < 0) die("unknown catalogue label in PAIR_COUNT `%s'", pr);
+    if (!existing[k] && (ia < 0 || ib < 0))
+      die("unknown catalogue label in PAIR_COUNT `%s'", pr);
     pia[k] = ia;
     pib[k] = ib;
-    existing[k] = file_exists(fn) && ovw <= 1;
     if (!existing[k]) todo[ntodo++] = k;
+  }
+  /* the correlation function outputs (load_conf.c:899-965): one file per
+   * estimator, checked like the pair-count files; multipoles sorted, without
+   * duplicates, between 0 and 6 */
+  const int nest = conf_len(&C, "CF_ESTIMATOR");
+  int npole = 0, poles[7];
+  const int dowp = (b.bintype == FCFCG_BIN_SPI) &&
+                   is_true(conf_str(&C, "PROJECTED_CF", 0));
+  if (nest > 0) {
+    for (int e = 0; e < nest; e++) {
+      const char *ex = conf_str(&C, "CF_ESTIMATOR", e);
+      if (!ex || !*ex) die("unexpected empty CF_ESTIMATOR");
+    }
+    const char *outk[3] = {"CF_OUTPUT_FILE", NULL, NULL};
+    if (b.bintype == FCFCG_BIN_SMU && conf_len(&C, "MULTIPOLE") > 0) {
+      const int nin = conf_len(&C, "MULTIPOLE");
+      int *pl = malloc(sizeof(int) * (size_t) nin);
+      if (!pl) die("out of memory");
+      for (int j = 0; j < nin; j++)
+        pl[j] = (int) strtol(conf_str(&C, "MULTIPOLE", j), NULL, 10);
+      qsort(pl, (size_t) nin, sizeof(int), cmp_int);
+      if (pl[0] < 0 || pl[nin - 1] > 6)
+        die("MULTIPOLE must be between 0 and 6");
+      for (int j = 0; j < nin; j++)
+        if (j == 0 || pl[j] != pl[j - 1]) poles[npole++] = pl[j];
+      free(pl);
+      outk[1] = "MULTIPOLE_FILE";
+    }
+    if (dowp) outk[2] = "PROJECTED_FILE";
+    for (int q = 0; q < 3; q++) {
+      if (!outk[q]) continue;
+      const int nf = conf_len(&C, outk[q]);
+      if (nf == 0) die("%s is not set", outk[q]);
+      if (nf < nest) die("too few elements of %s", outk[q]);
+      for (int e = 0; e < nest; e++)
+        check_output(conf_str(&C, outk[q], e), outk[q], ovw, 1);
+    }
   }
   /* the catalogues the counts need, in order of first use */
   int slot_of[MAXCAT], use[MAXCAT], nuse = 0;
@@ -853,35 +940,29 @@ int main(int argc, char **argv) {
   }
 
   /* correlation functions */
-  const int nest = conf_len(&C, "CF_ESTIMATOR");
   double *rr = NULL;
 #ifndef FCFCG_SURVEY
   rr = malloc(sizeof(double) * ntot);
   check(ctx, fcfcg_analytic_rr(ctx, rr), "analytic RR");
 #endif
-  const int npole = conf_len(&C, "MULTIPOLE");
-  int poles[16];
-  for (int j = 0; j < npole && j < 16; j++)
-    poles[j] = (int) strtol(conf_str(&C, "MULTIPOLE", j), NULL, 10);
-  const int dowp = is_true(conf_str(&C, "PROJECTED_CF", 0));
   for (int e = 0; e < nest; e++) {
     const char *ex = conf_str(&C, "CF_ESTIMATOR", e);
     check(ctx, fcfcg_cf_eval(ex, npair, labels, ncnt_all, rr, ntot, tmp),
           "CF_ESTIMATOR");
-    const char *cf = conf_str(&C, "CF_OUTPUT_FILE", e);
-    if (cf) check(ctx, fcfcg_write_cf(ctx, cf, tmp), "writing CF_OUTPUT_FILE");
-    if (npole > 0 && b.bintype == FCFCG_BIN_SMU) {
+    check(ctx, fcfcg_write_cf(ctx, conf_str(&C, "CF_OUTPUT_FILE", e), tmp),
+          "writing CF_OUTPUT_FILE");
+    if (npole > 0) {
       double *mp = malloc(sizeof(double) * npole * b.ns);
       check(ctx, fcfcg_multipoles(ctx, tmp, npole, poles, mp), "multipoles");
-      const char *mf = conf_str(&C, "MULTIPOLE_FILE", e);
-      if (mf) check(ctx, fcfcg_write_multipoles(ctx, mf, npole, poles, mp),
-                    "writing MULTIPOLE_FILE");
+      check(ctx, fcfcg_write_multipoles(ctx, conf_str(&C, "MULTIPOLE_FILE", e),
+                                        npole, poles, mp),
+            "writing MULTIPOLE_FILE");
       free(mp);
-    } else if (dowp && b.bintype == FCFCG_BIN_SPI) {
+    } else if (dowp) {
       double *wp = malloc(sizeof(double) * b.ns);
       check(ctx, fcfcg_wp(ctx, tmp, wp), "w_p");
-      const char *wf = conf_str(&C, "PROJECTED_FILE", e);
-      if (wf) check(ctx, fcfcg_write_wp(ctx, wf, wp), "writing PROJECTED_FILE");
+      check(ctx, fcfcg_write_wp(ctx, conf_str(&C, "PROJECTED_FILE", e), wp),
+            "writing PROJECTED_FILE");
       free(wp);
     }
   }

@@ -5,8 +5,9 @@ pairs listed in PAIR_COUNT on the GPU, writes PAIR_COUNT_FILE, evaluates
 CF_ESTIMATOR into CF_OUTPUT_FILE, and the Legendre multipoles / projected
 correlation function into MULTIPOLE_FILE / PROJECTED_FILE -- the sequence of
 FCFC's eval_cf (src/fcfc/2pt_box/eval_cf.c:405, survey src/fcfc/2pt/eval_cf.c).
-Existing pair-count files are read back instead of recounted when OVERWRITE
-is 0 or 1, as FCFC's check_output decides (src/fcfc/2pt_box/load_conf.c:582-650).
+Outputs are checked first, as FCFC's check_output does
+(src/fcfc/2pt_box/load_conf.c:582-650): OVERWRITE = 0 refuses existing
+files, 1 reads existing pair-count files back instead of recounting them.
 
     python -m fcfc_gb300.runner --box -c fcfc_2pt_box.conf
     python -m fcfc_gb300.runner --survey -c fcfc_2pt.conf
@@ -165,6 +166,49 @@ def read_bins_file(path):
 
 # --------------------------------------------------------------------------
 
+def check_output(fname, key, ovw, force, ask=input):
+    """FCFC's check_output (src/fcfc/2pt_box/load_conf.c:582-650): False to
+    write the file, True to read it back (an existing pair-count file with
+    0 < OVERWRITE < force); FCFC's refusals raise.  force: 2 for
+    PAIR_COUNT_FILE, 1 for the correlation function outputs.  A negative
+    OVERWRITE asks (``ask``) up to |OVERWRITE| times."""
+    if not fname:
+        raise FCFCGError(capi.ERR_CFG, "the output file %s is not set" % key)
+    if os.path.exists(fname):
+        if ovw < 0:
+            for _ in range(-ovw):
+                try:
+                    a = ask("%s exists: `%s'; overwrite it? (y/n): "
+                            % (key, fname))[:1]
+                except EOFError:
+                    continue
+                if a in ("n", "N"):
+                    ovw = force - 1
+                    break
+                if a in ("y", "Y"):
+                    ovw = force
+                    break
+            else:
+                raise FCFCGError(capi.ERR_FILE, "too many failed inputs")
+        if ovw <= 0:
+            raise FCFCGError(capi.ERR_FILE, "abort to avoid overwriting %s: "
+                             "`%s'" % (key, fname))
+        if ovw < force:
+            if not os.access(fname, os.R_OK):
+                raise FCFCGError(capi.ERR_FILE, "cannot access %s: `%s'"
+                                 % (key, fname))
+            return True
+        if not os.access(fname, os.W_OK):
+            raise FCFCGError(capi.ERR_FILE, "cannot write to file: `%s'"
+                             % fname)
+    else:
+        d = os.path.dirname(fname)
+        if d and not os.access(d, os.X_OK):
+            raise FCFCGError(capi.ERR_FILE, "cannot access the directory `%s'"
+                             % d)
+    return False
+
+
 def run(conf: dict, geometry: str = "box", device: int = -1,
         precision: int = capi.PREC_FP32_RECHECK, verbose: bool = False,
         with_mu_one: bool = False, graph: bool = True):
@@ -192,7 +236,10 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
     pcout = _arr(conf, "PAIR_COUNT_FILE")
     est = _arr(conf, "CF_ESTIMATOR") or []
     cfout = _arr(conf, "CF_OUTPUT_FILE") or []
-    poles = [int(p) for p in (_arr(conf, "MULTIPOLE") or [])]
+    # sorted, without duplicates, 0 to 6 (load_conf.c:915-941)
+    poles = sorted({int(p) for p in (_arr(conf, "MULTIPOLE") or [])})
+    if poles and (poles[0] < 0 or poles[-1] > 6):
+        raise FCFCGError(capi.ERR_CFG, "MULTIPOLE must be between 0 and 6")
     mpout = _arr(conf, "MULTIPOLE_FILE") or []
     do_wp = _bool(conf.get("PROJECTED_CF", "F"))
     wpout = _arr(conf, "PROJECTED_FILE") or []
@@ -211,6 +258,22 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
         if any(cnvt):
             cosmo = cosmo_from_conf(conf)
 
+    # the outputs, checked as FCFC does before any counting: existing
+    # pair-count files with OVERWRITE = 1 are read back, the others counted
+    readback = [check_output(pcout[k] if k < len(pcout) else None,
+                             "PAIR_COUNT_FILE", ovw, 2)
+                for k in range(len(pairs))]
+    if est:
+        outs = [("CF_OUTPUT_FILE", cfout)]
+        if poles and bintype == BIN_SMU:
+            outs.append(("MULTIPOLE_FILE", mpout))
+        if do_wp and bintype == BIN_SPI:
+            outs.append(("PROJECTED_FILE", wpout))
+        for key, files_ in outs:
+            if len(files_) < len(est):
+                raise FCFCGError(capi.ERR_CFG, "too few elements of %s" % key)
+            for k in range(len(est)):
+                check_output(files_[k], key, ovw, 1)
     kw = dict(geometry=geometry, bintype=bintype, device=device)
     if box:
         b = [float(v) for v in _arr(conf, "BOX_SIZE")]
@@ -248,11 +311,9 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
         w = wts[i] if wts else None
         weighted_cat[lab] = w not in (None, "", "''", '""')
 
-    # pairs with an existing file (OVERWRITE <= 1) are read back; the others
-    # are counted
     done, todo = {}, []
     for k, pair in enumerate(pairs):
-        if os.path.exists(pcout[k]) and ovw <= 1:
+        if readback[k]:
             done[k] = pc.read_paircount(pcout[k])
         else:
             todo.append(k)

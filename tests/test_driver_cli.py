@@ -122,3 +122,84 @@ def test_options_without_a_configuration_file(drivers, tmp_path):
     r = subprocess.run([drivers[0], "--no-such-option", "-B", "0"],
                        capture_output=True, text=True, cwd=str(tmp_path))
     assert "unrecognised" in r.stderr and "CATALOG" in r.stderr
+
+
+def _pc_conf(tmp_path, extra):
+    return _base_conf("CATALOG_LABEL = [D]\nPAIR_COUNT = [DD]\n"
+                      "PAIR_COUNT_FILE = [%s]\n%s" % (tmp_path / "dd.bin", extra))
+
+
+def test_overwrite_rules(drivers, tmp_path):
+    """FCFC's check_output: OVERWRITE = 0 refuses an existing output, a
+    negative value asks on the terminal, a missing directory is an error --
+    all before any device work."""
+    conf = tmp_path / "c.conf"
+    (tmp_path / "dd.bin").write_bytes(b"x")
+    run = lambda inp=None: subprocess.run(
+        [drivers[0], "-c", str(conf)], capture_output=True, text=True,
+        input=inp)
+    conf.write_text(_pc_conf(tmp_path, "OVERWRITE = 0\n"))
+    r = run()
+    assert r.returncode != 0 and "abort to avoid overwriting" in r.stderr
+    conf.write_text(_pc_conf(tmp_path, "OVERWRITE = -2\n"))
+    for inp in ("", "x\nq\n"):
+        r = run(inp)
+        assert r.returncode != 0 and "too many failed inputs" in r.stderr, inp
+    # an answer: no refusal (the run goes on to the catalogue or the device)
+    for inp in ("n\n", "x\ny\n"):
+        r = run(inp)
+        assert "abort" not in r.stderr and "failed inputs" not in r.stderr, \
+            (inp, r.stderr)
+    # correlation function outputs: refused with 0, overwritten with 1
+    (tmp_path / "dd.bin").unlink()
+    (tmp_path / "xi.txt").write_text("old")
+    est = 'CF_ESTIMATOR = ["DD / @@ - 1"]\nCF_OUTPUT_FILE = [%s]\n' % (
+        tmp_path / "xi.txt")
+    conf.write_text(_pc_conf(tmp_path, est + "OVERWRITE = 0\n"))
+    r = run()
+    assert "abort to avoid overwriting CF_OUTPUT_FILE" in r.stderr, r.stderr
+    conf.write_text(_pc_conf(tmp_path, est + "OVERWRITE = 1\n"))
+    r = run()
+    assert "will be overwritten" in r.stderr and "abort" not in r.stderr
+    conf.write_text(_base_conf("CATALOG_LABEL = [D]\nPAIR_COUNT = [DD]\n"
+                               "PAIR_COUNT_FILE = [%s]\n"
+                               % (tmp_path / "no" / "dd.bin")))
+    r = run()
+    assert "cannot access the directory" in r.stderr, r.stderr
+
+
+def test_multipole_checks(drivers, tmp_path):
+    conf = tmp_path / "c.conf"
+    conf.write_text(_base_conf(
+        "MU_BIN_NUM = 10\nCATALOG_LABEL = [D]\nPAIR_COUNT = [DD]\n"
+        "PAIR_COUNT_FILE = [%s]\nCF_ESTIMATOR = [DD / @@ - 1]\n"
+        "CF_OUTPUT_FILE = [%s]\nMULTIPOLE = [0, 8]\nMULTIPOLE_FILE = [%s]\n"
+        % (tmp_path / "dd.bin", tmp_path / "xi.txt", tmp_path / "mp.txt")))
+    # (s, mu) from the command line, over the file's BINNING_SCHEME = 0
+    r = subprocess.run([drivers[0], "-c", str(conf), "-B", "1"],
+                       capture_output=True, text=True)
+    assert r.returncode != 0 and "MULTIPOLE must be" in r.stderr, r.stderr
+    r = subprocess.run([drivers[0], "-c", str(conf), "-B", "1", "-m", "[2, 0]",
+                        "-M", "[]"], capture_output=True, text=True)
+    assert r.returncode != 0 and "MULTIPOLE_FILE is not set" in r.stderr
+
+
+def test_runner_check_output(tmp_path):
+    from fcfc_gb300 import runner
+    from fcfc_gb300.capi import FCFCGError
+    f = tmp_path / "dd.bin"
+    assert runner.check_output(str(f), "PAIR_COUNT_FILE", 0, 2) is False
+    f.write_bytes(b"x")
+    with pytest.raises(FCFCGError, match="abort"):
+        runner.check_output(str(f), "PAIR_COUNT_FILE", 0, 2)
+    assert runner.check_output(str(f), "PAIR_COUNT_FILE", 1, 2) is True
+    assert runner.check_output(str(f), "PAIR_COUNT_FILE", 2, 2) is False
+    assert runner.check_output(str(f), "CF_OUTPUT_FILE", 1, 1) is False
+    answers = iter(["maybe", "n"])
+    assert runner.check_output(str(f), "PAIR_COUNT_FILE", -3, 2,
+                               ask=lambda _: next(answers)) is True
+    with pytest.raises(FCFCGError, match="failed inputs"):
+        runner.check_output(str(f), "PAIR_COUNT_FILE", -1, 2,
+                            ask=lambda _: "?")
+    with pytest.raises(FCFCGError, match="directory"):
+        runner.check_output(str(tmp_path / "no" / "x"), "CF_OUTPUT_FILE", 2, 1)

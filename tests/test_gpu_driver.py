@@ -129,3 +129,24 @@ def test_driver_from_command_line_options_alone(name, tmp_path):
     assert out["file"].keys() == out["options"].keys() and out["file"]
     for f in out["file"]:
         assert out["file"][f] == out["options"][f], f
+
+
+@pytest.mark.parametrize("runner", [False, True], ids=["driver", "runner"])
+def test_multipoles_sorted_without_duplicates(runner, tmp_path):
+    """MULTIPOLE = [4, 2, 0, 2] gives FCFC's file for [0, 2, 4]: FCFC sorts
+    the orders and drops duplicates (load_conf.c:915-941)."""
+    case = Case("box_smu_auto")
+    conf = _write_conf(case, str(tmp_path))
+    text = open(conf).read().replace("MULTIPOLE = [0, 2, 4]",
+                                     "MULTIPOLE = [4, 2, 0, 2]")
+    assert "[4, 2, 0, 2]" in text
+    open(conf, "w").write(text)
+    if runner:
+        from fcfc_gb300 import runner as rn
+        rn.run(rn.parse_conf(text), "box")
+    else:
+        r = subprocess.run([os.path.join(BIN, "FCFC_2PT_BOX_GPU"), "-c", conf],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+    assert open(tmp_path / "mp.txt").read() == \
+        open(os.path.join(case.dir, "mp.txt")).read()
