@@ -638,6 +638,11 @@ int main(int argc, char **argv) {
   for (int i = 0; i < ncat; i++) {
     const char *l = conf_str(&C, "CATALOG_LABEL", i);
     label[i] = (conf_len(&C, "CATALOG_LABEL") && l) ? l[0] : (char) ('A' + i);
+    /* capital letters, each once (load_conf.c:675-705) */
+    if (label[i] < 'A' || label[i] > 'Z')
+      die("invalid CATALOG_LABEL: %c", label[i]);
+    for (int j = 0; j < i; j++)
+      if (label[j] == label[i]) die("duplicate CATALOG_LABEL: %c", label[i]);
   }
   for (int i = 0; i < ncat; i++) {
     const char *t = conf_str(&C, "CATALOG_TYPE", i);
@@ -702,7 +707,8 @@ int main(int argc, char **argv) {
   int weighted[MAXCAT];
   for (int i = 0; i < ncat; i++) {
     const char *w = conf_str(&C, "WEIGHT", i);
-    weighted[i] = (conf_len(&C, "WEIGHT") && w && *w);
+    /* an empty weight or "1" means no weights (load_conf.c:780-789) */
+    weighted[i] = (conf_len(&C, "WEIGHT") && w && *w && strcmp(w, "1"));
   }
   if (npair > 64) die("too many pairs");
   /* pairs with an existing file (OVERWRITE <= 1) are read back */

@@ -220,6 +220,13 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
     files = _arr(conf, "CATALOG")
     ncat = len(files)
     labels = _arr(conf, "CATALOG_LABEL") or [chr(ord("A") + i) for i in range(ncat)]
+    # capital letters, each once (load_conf.c:675-705)
+    labels = [l[:1] for l in labels]
+    for i, l in enumerate(labels):
+        if not ("A" <= l <= "Z"):
+            raise FCFCGError(capi.ERR_CFG, "invalid CATALOG_LABEL: %r" % l)
+        if l in labels[:i]:
+            raise FCFCGError(capi.ERR_CFG, "duplicate CATALOG_LABEL: %s" % l)
     fmtr = _arr(conf, "ASCII_FORMATTER", ncat)
     pos = _arr(conf, "POSITION")
     wts = _arr(conf, "WEIGHT", ncat)
@@ -296,7 +303,8 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
 
     def load_cat(i, slot):
         p3 = pos[3 * i: 3 * i + 3]
-        w = wts[i] if wts and wts[i] not in (None, "", "''", '""') else None
+        w = wts[i] if wts and wts[i] not in (None, "", "''", '""', "1") \
+            else None
         x, ww = read_catalog(files[i], fmtr[i] if fmtr else None, p3, w,
                              skip[i], cmt[i] if cmt else None,
                              sel[i] if sel and sel[i] not in ("", "''", '""')
@@ -306,10 +314,11 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
         else:
             pc.load(slot, x, ww)
 
+    # an empty weight or "1" means no weights (load_conf.c:780-789)
     weighted_cat = {}
     for i, lab in enumerate(labels):
         w = wts[i] if wts else None
-        weighted_cat[lab] = w not in (None, "", "''", '""')
+        weighted_cat[lab] = w not in (None, "", "''", '""', "1")
 
     done, todo = {}, []
     for k, pair in enumerate(pairs):

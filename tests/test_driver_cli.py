@@ -203,3 +203,20 @@ def test_runner_check_output(tmp_path):
                             ask=lambda _: "?")
     with pytest.raises(FCFCGError, match="directory"):
         runner.check_output(str(tmp_path / "no" / "x"), "CF_OUTPUT_FILE", 2, 1)
+
+
+def test_labels_and_unit_weights(drivers, tmp_path):
+    """CATALOG_LABEL: capital letters, each once; WEIGHT = 1 counts without
+    weights (FCFC's load_conf.c:675-705, 780-789)."""
+    conf = tmp_path / "c.conf"
+    for lab, word in (("[d]", "invalid CATALOG_LABEL"),
+                      ("[D, D]", "duplicate CATALOG_LABEL")):
+        conf.write_text("CATALOG = [a.txt, b.txt]\nCATALOG_LABEL = %s\n" % lab)
+        r = subprocess.run([drivers[0], "-c", str(conf)], capture_output=True,
+                           text=True)
+        assert r.returncode != 0 and word in r.stderr, (lab, r.stderr)
+    from fcfc_gb300 import runner
+    from fcfc_gb300.capi import FCFCGError
+    with pytest.raises(FCFCGError, match="duplicate CATALOG_LABEL"):
+        runner.run(runner.parse_conf("CATALOG = [a, b]\nCATALOG_LABEL = [D, D]\n"
+                                     "POSITION = [$1,$2,$3,$1,$2,$3]\n"), "box")

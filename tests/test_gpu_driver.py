@@ -150,3 +150,25 @@ def test_multipoles_sorted_without_duplicates(runner, tmp_path):
         assert r.returncode == 0, r.stderr
     assert open(tmp_path / "mp.txt").read() == \
         open(os.path.join(case.dir, "mp.txt")).read()
+
+
+@pytest.mark.parametrize("runner", [False, True], ids=["driver", "runner"])
+def test_unit_weight_counts_without_weights(runner, tmp_path):
+    """WEIGHT = 1 is FCFC's way of saying no weights: the integer pair-count
+    file of the unweighted golden case, byte for byte."""
+    case = Case("box_smu_auto")
+    conf = _write_conf(case, str(tmp_path))
+    text = open(conf).read()
+    assert "WEIGHT" not in text
+    text += "WEIGHT = [1]\n"
+    open(conf, "w").write(text)
+    if runner:
+        from fcfc_gb300 import runner as rn
+        rn.run(rn.parse_conf(text), "box")
+    else:
+        r = subprocess.run([os.path.join(BIN, "FCFC_2PT_BOX_GPU"), "-c", conf],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+    for pair in case.meta["pairs"]:
+        assert open(tmp_path / (pair + ".bin"), "rb").read() == \
+            open(os.path.join(case.dir, pair + ".bin"), "rb").read(), pair
