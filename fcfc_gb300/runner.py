@@ -241,6 +241,10 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
     bintype = int(conf.get("BINNING_SCHEME", 0))
     pairs = _arr(conf, "PAIR_COUNT")
     pcout = _arr(conf, "PAIR_COUNT_FILE")
+    if not pairs:
+        raise FCFCGError(capi.ERR_CFG, "PAIR_COUNT is not set")
+    if not pcout or len(pcout) < len(pairs):
+        raise FCFCGError(capi.ERR_CFG, "PAIR_COUNT_FILE needs one file per pair")
     est = _arr(conf, "CF_ESTIMATOR") or []
     cfout = _arr(conf, "CF_OUTPUT_FILE") or []
     # sorted, without duplicates, 0 to 6 (load_conf.c:915-941)
@@ -429,24 +433,78 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
     return out
 
 
+# FCFC's command line options and the keys they set (short, long, key,
+# Boolean), src/fcfc/2pt_box/load_conf.c:477-515, src/fcfc/2pt/load_conf.c:
+# 512-553; box-only and survey-only entries are marked
+OPTIONS = [
+    ("i", "input", "CATALOG", 0), ("l", "label", "CATALOG_LABEL", 0),
+    ("T", "type", "CATALOG_TYPE", 0), (None, "skip", "ASCII_SKIP", 0),
+    (None, "comment", "ASCII_COMMENT", 0), ("f", "formatter", "ASCII_FORMATTER", 0),
+    ("x", "position", "POSITION", 0), ("w", "weight", "WEIGHT", 0),
+    ("s", "select", "SELECTION", 0), ("b", "box", "BOX_SIZE", "box-opt"),
+    (None, "convert", "COORD_CONVERT", "survey-bool"),
+    ("d", "omega-m", "OMEGA_M", "survey"), (None, "omega-l", "OMEGA_LAMBDA", "survey"),
+    (None, "eos-w", "DE_EOS_W", "survey"), (None, "cmvdst-err", "CMVDST_ERR", "survey"),
+    (None, "cmvdst-file", "Z_CMVDST_FILE", "survey"),
+    ("S", "data-struct", "DATA_STRUCT", 0), ("B", "bin", "BINNING_SCHEME", 0),
+    ("p", "pair", "PAIR_COUNT", 0), ("P", "pair-output", "PAIR_COUNT_FILE", 0),
+    ("e", "cf", "CF_ESTIMATOR", 0), ("E", "cf-output", "CF_OUTPUT_FILE", 0),
+    ("m", "multipole", "MULTIPOLE", 0), ("M", "mp-output", "MULTIPOLE_FILE", 0),
+    ("u", "wp", "PROJECTED_CF", "bool"), ("U", "wp-output", "PROJECTED_FILE", 0),
+    (None, "s-file", "SEP_BIN_FILE", 0), (None, "s-min", "SEP_BIN_MIN", 0),
+    (None, "s-max", "SEP_BIN_MAX", 0), (None, "s-step", "SEP_BIN_SIZE", 0),
+    (None, "mu-num", "MU_BIN_NUM", 0), (None, "pi-file", "PI_BIN_FILE", 0),
+    (None, "pi-min", "PI_BIN_MIN", 0), (None, "pi-max", "PI_BIN_MAX", 0),
+    (None, "pi-step", "PI_BIN_SIZE", 0), ("F", "out-format", "OUTPUT_FORMAT", 0),
+    ("O", "overwrite", "OVERWRITE", 0),
+]
+
+
 def main(argv=None):
+    """FCFC's command line: every option sets its key over the configuration
+    file's value; the file defaults to FCFC's name for the geometry, and a
+    missing one leaves the command line's keys alone."""
     ap = argparse.ArgumentParser(description="FCFC run flow on the GB300 engine")
-    g = ap.add_mutually_exclusive_group()
-    g.add_argument("--box", action="store_true", help="FCFC_2PT_BOX keys")
-    g.add_argument("--survey", action="store_true", help="FCFC_2PT keys")
-    ap.add_argument("-c", "--conf", required=True)
+    # --survey: FCFC_2PT's flow; FCFC_2PT_BOX's otherwise.  --box alone
+    # selects the box flow too, --box VALUE (or -b) is FCFC's BOX_SIZE.
+    ap.add_argument("--survey", action="store_true", help="FCFC_2PT keys")
+    ap.add_argument("-c", "--conf", default=None)
     ap.add_argument("--fp64", action="store_true", help="all-FP64 GPU path")
     ap.add_argument("--with-mu-one", action="store_true",
                     help="mu = 1 in the last mu bin, as FCFC built with "
                          "-DWITH_MU_ONE")
     ap.add_argument("--no-graph", action="store_true",
                     help="one count per pair instead of one CUDA graph")
-    ap.add_argument("-v", "--verbose", action="store_true")
+    ap.add_argument("-v", "--verbose", nargs="?", const="T", default=None)
+    survey = argv is not None and "--survey" in argv or \
+        argv is None and "--survey" in sys.argv[1:]
+    for short, long_, key, kind in OPTIONS:
+        if kind in ("survey", "survey-bool") and not survey:
+            continue
+        names = (["-" + short] if short else []) + ["--" + long_]
+        if kind == "box-opt":
+            ap.add_argument(*names, dest=key, nargs="?", const="", default=None)
+        elif kind in ("bool", "survey-bool"):
+            ap.add_argument(*names, dest=key, nargs="?", const="T", default=None)
+        else:
+            ap.add_argument(*names, dest=key, default=None)
     a = ap.parse_args(argv)
-    conf = parse_conf(open(a.conf).read())
+    path = a.conf or ("fcfc_2pt.conf" if a.survey else "fcfc_2pt_box.conf")
+    if os.access(path, os.R_OK):
+        conf = parse_conf(open(path).read())
+    else:
+        print("Warning: cannot access the configuration file: `%s'" % path,
+              file=sys.stderr)
+        conf = {}
+    for _, _, key, _ in OPTIONS:
+        v = getattr(a, key, None)
+        if v:
+            conf.update(parse_conf("%s = %s" % (key, v)))
+    verbose = a.verbose if a.verbose is not None else conf.get("VERBOSE", "T")
     run(conf, "survey" if a.survey else "box",
         precision=capi.PREC_FP64 if a.fp64 else capi.PREC_FP32_RECHECK,
-        verbose=a.verbose, with_mu_one=a.with_mu_one, graph=not a.no_graph)
+        verbose=_bool(verbose), with_mu_one=a.with_mu_one,
+        graph=not a.no_graph)
     return 0
 
 

@@ -220,3 +220,20 @@ def test_labels_and_unit_weights(drivers, tmp_path):
     with pytest.raises(FCFCGError, match="duplicate CATALOG_LABEL"):
         runner.run(runner.parse_conf("CATALOG = [a, b]\nCATALOG_LABEL = [D, D]\n"
                                      "POSITION = [$1,$2,$3,$1,$2,$3]\n"), "box")
+
+
+def test_runner_command_line(tmp_path, monkeypatch):
+    """python -m fcfc_gb300.runner takes FCFC's options too, over the file's
+    values, and FCFC's default file name."""
+    from fcfc_gb300 import runner
+    from fcfc_gb300.capi import FCFCGError
+    conf = tmp_path / "c.conf"
+    conf.write_text(_base_conf("DATA_STRUCT = 2\n"))
+    with pytest.raises(FCFCGError, match="DATA_STRUCT"):
+        runner.main(["--box", "-c", str(conf)])
+    with pytest.raises(FCFCGError, match="PAIR_COUNT is not set"):
+        runner.main(["-c", str(conf), "-S", "0"])
+    monkeypatch.chdir(tmp_path)
+    with pytest.raises(FCFCGError, match="PAIR_COUNT is not set"):
+        runner.main(["-b", "100", "-i", "a.txt", "-x", "[$1, $2, $3]",
+                     "-B", "0", "--s-min", "0", "--s-max=10", "--s-step", "1"])
