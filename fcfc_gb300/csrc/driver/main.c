@@ -648,6 +648,12 @@ int main(int argc, char **argv) {
     const char *t = conf_str(&C, "CATALOG_TYPE", i);
     if (t && strtol(t, NULL, 10) != 0)
       die("only ASCII catalogues (CATALOG_TYPE = 0) are supported");
+    /* load_conf.c:738-773 */
+    if (conf_long(&C, "ASCII_SKIP", i, 0) < 0)
+      die("ASCII_SKIP cannot be negative");
+    const char *cm = conf_str(&C, "ASCII_COMMENT", i);
+    if (cm && cm[0] && !isgraph((unsigned char) cm[0]))
+      die("invalid ASCII_COMMENT: '%c' (ASCII code: %d)", cm[0], cm[0]);
   }
   if (conf_len(&C, "POSITION") != 3 * ncat)
     die("POSITION needs 3 entries per catalogue");

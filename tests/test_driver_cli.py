@@ -31,6 +31,10 @@ def test_config_errors(drivers, tmp_path):
          "ASCII"),
         ("CATALOG = [a.txt]\nPOSITION = [$1, $2, $3]\nDATA_STRUCT = 2\n",
          "DATA_STRUCT"),
+        ("CATALOG = [a.txt]\nASCII_SKIP = [-1]\nPOSITION = [$1, $2, $3]\n",
+         "ASCII_SKIP"),
+        ("CATALOG = [a.txt]\nASCII_COMMENT = [' ']\nPOSITION = [$1, $2, $3]\n",
+         "ASCII_COMMENT"),
     ]
     for text, word in cases:
         conf.write_text(text)
