@@ -747,9 +747,20 @@ int main(int argc, char **argv) {
   const int dowp = (b.bintype == FCFCG_BIN_SPI) &&
                    is_true(conf_str(&C, "PROJECTED_CF", 0));
   if (nest > 0) {
+    /* each estimator parses and names only counted pairs (setup_cf.c:
+     * 128-200): evaluated once on zero counts before any device work */
+    double zero[64] = {0}, dummy;
+#ifdef FCFCG_SURVEY
+    const double *rr0 = NULL;       /* no analytic RR for surveys */
+#else
+    const double rr_zero = 0, *rr0 = &rr_zero;
+#endif
     for (int e = 0; e < nest; e++) {
       const char *ex = conf_str(&C, "CF_ESTIMATOR", e);
       if (!ex || !*ex) die("unexpected empty CF_ESTIMATOR");
+      if (fcfcg_cf_eval(ex, npair, labels, zero, rr0, 1, &dummy))
+        die("invalid CF_ESTIMATOR `%s' (a syntax error, or a pair not in "
+            "PAIR_COUNT)", ex);
     }
     const char *outk[3] = {"CF_OUTPUT_FILE", NULL, NULL};
     if (b.bintype == FCFCG_BIN_SMU && conf_len(&C, "MULTIPOLE") > 0) {

@@ -285,6 +285,20 @@ def run(conf: dict, geometry: str = "box", device: int = -1,
                 raise FCFCGError(capi.ERR_CFG, "too few elements of %s" % key)
             for k in range(len(est)):
                 check_output(files_[k], key, ovw, 1)
+    # each estimator parses and names only counted pairs (setup_cf.c:
+    # 128-200): evaluated once on zero counts before any device work
+    if est:
+        lib = capi.load_library()
+        z = np.zeros(len(pairs))
+        zrr = np.zeros(1)
+        one = np.zeros(1)
+        for e in est:
+            if lib.fcfcg_cf_eval(e.encode(), len(pairs), "".join(pairs).encode(),
+                                 capi.ptr(z), capi.ptr(zrr) if box else None,
+                                 1, capi.ptr(one)):
+                raise FCFCGError(capi.ERR_CFG, "invalid CF_ESTIMATOR %r (a "
+                                 "syntax error, or a pair not in PAIR_COUNT)"
+                                 % e)
     kw = dict(geometry=geometry, bintype=bintype, device=device)
     if box:
         b = [float(v) for v in _arr(conf, "BOX_SIZE")]

@@ -241,3 +241,24 @@ def test_runner_command_line(tmp_path, monkeypatch):
     with pytest.raises(FCFCGError, match="PAIR_COUNT is not set"):
         runner.main(["-b", "100", "-i", "a.txt", "-x", "[$1, $2, $3]",
                      "-B", "0", "--s-min", "0", "--s-max=10", "--s-step", "1"])
+
+
+def test_estimators_checked_before_device_work(drivers, tmp_path):
+    """An estimator naming a pair that is not counted, or one that does not
+    parse, stops the run before any device work (FCFC's setup_cf.c:128-200)."""
+    conf = tmp_path / "c.conf"
+    for est in ("DR / @@ - 1", "DD / (@@ - 1"):
+        conf.write_text(_pc_conf(tmp_path, 'CF_ESTIMATOR = ["%s"]\n'
+                                 'CF_OUTPUT_FILE = [%s]\nOVERWRITE = 2\n'
+                                 % (est, tmp_path / "xi.txt")))
+        r = subprocess.run([drivers[0], "-c", str(conf)], capture_output=True,
+                           text=True)
+        assert r.returncode != 0 and "invalid CF_ESTIMATOR" in r.stderr, \
+            (est, r.stderr)
+    from fcfc_gb300 import runner
+    from fcfc_gb300.capi import FCFCGError
+    conf.write_text(_pc_conf(tmp_path, 'CF_ESTIMATOR = ["DR / @@ - 1"]\n'
+                             'CF_OUTPUT_FILE = [%s]\nOVERWRITE = 2\n'
+                             % (tmp_path / "xi.txt")))
+    with pytest.raises(FCFCGError, match="invalid CF_ESTIMATOR"):
+        runner.run(runner.parse_conf(conf.read_text()), "box")
