@@ -89,7 +89,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
-DRIVER_SOURCES = ["main.c", "catalog.c", "expr.c"]
+DRIVER_SOURCES = ["main.c", "conf.c", "catalog.c", "expr.c"]
 DRIVERS = {"FCFC_2PT_BOX_GPU": [], "FCFC_2PT_GPU": ["-DFCFCG_SURVEY"]}
 BINDIR = os.path.join(HERE, "bin")
 
