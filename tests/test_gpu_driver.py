@@ -172,3 +172,26 @@ def test_unit_weight_counts_without_weights(runner, tmp_path):
     for pair in case.meta["pairs"]:
         assert open(tmp_path / (pair + ".bin"), "rb").read() == \
             open(os.path.join(case.dir, pair + ".bin"), "rb").read(), pair
+
+
+def test_catalogue_errors_from_the_reading_thread(tmp_path):
+    """A catalogue that cannot be read, or a line that does not parse, is
+    reported (the catalogues are read on a helper thread while the device is
+    set up) and the run ends with an error and no pair-count file."""
+    good = tmp_path / "d.txt"
+    np.savetxt(good, np.random.default_rng(1).random((100, 3)) * 50.0)
+    bad = tmp_path / "bad.txt"
+    bad.write_text("1 2 3\n4 five 6\n")
+    for cat, word in ((tmp_path / "missing.txt", "cannot read"),
+                      (bad, "failed to read line 2")):
+        conf = tmp_path / "c.conf"
+        conf.write_text(
+            "CATALOG = [%s]\nCATALOG_LABEL = [D]\nASCII_FORMATTER = "
+            "[\"%%lf %%lf %%lf\"]\nPOSITION = [$1, $2, $3]\nBOX_SIZE = 100\n"
+            "BINNING_SCHEME = 0\nSEP_BIN_MIN = 0\nSEP_BIN_MAX = 10\n"
+            "SEP_BIN_SIZE = 1\nPAIR_COUNT = [DD]\nPAIR_COUNT_FILE = [%s]\n"
+            "OVERWRITE = 2\n" % (cat, tmp_path / "dd.bin"))
+        r = subprocess.run([os.path.join(BIN, "FCFC_2PT_BOX_GPU"), "-c",
+                            str(conf)], capture_output=True, text=True)
+        assert r.returncode != 0 and word in r.stderr, r.stderr
+        assert not (tmp_path / "dd.bin").exists()
