@@ -168,3 +168,45 @@ def test_adjoint_random_matches_oracle(case):
                                    atol=1e-12 * max(1.0, np.abs(want_b).max()))
     finally:
         pc.close()
+
+
+@pytest.mark.parametrize("case", range(8))
+def test_survey_spi_wide_low_redshift(case):
+    """(s_perp, pi) over the whole sky at low redshift (objects a few outer
+    radii from the observer, lines of sight in every direction, some within
+    the radius where the line-of-sight prefilter is off): the FP32 path
+    gives the FP64 path's counts exactly, and the oracle's on every other
+    case."""
+    import fcfc_gb300 as fg
+    from fcfc_gb300 import synth
+    rng = np.random.default_rng(zlib.crc32(b"wide%d" % case))
+    zlo = float(rng.uniform(0.003, 0.02))
+    sk = dict(ra=(0.0, 360.0), dec=(-90.0, 90.0), zmu=2 * zlo, zsig=zlo,
+              zr=(zlo, 4 * zlo))
+    a = synth.radecz_to_xyz(synth.survey_radecz(
+        int(rng.integers(1500, 4000)), seed=int(rng.integers(1 << 30)), **sk))
+    b = synth.radecz_to_xyz(synth.survey_radecz(
+        int(rng.integers(1500, 4000)), seed=int(rng.integers(1 << 30)), **sk))
+    weighted = bool(case % 2)
+    wa = rng.uniform(0.5, 1.5, len(a)) if weighted else None
+    pmax = float(rng.choice([5.0, 10.0, 20.0]))
+    kw = dict(smin=0.0, smax=float(rng.choice([10.0, 20.0, 30.0])), ds=1.0,
+              pmin=0.0, pmax=pmax, dpi=1.0)
+    pc = fg.PairCounter("survey", 2, **kw)
+    pc.load(0, a, wa)
+    pc.load(1, b, None)
+    try:
+        for pair in ((0, None), (0, 1)):
+            c32 = pc.count_pairs(*pair, weighted=weighted, precision=0)
+            assert pc.stats()["precision_used"] == 0
+            c64 = pc.count_pairs(*pair, weighted=weighted, precision=1)
+            if weighted:
+                np.testing.assert_allclose(c32, c64, rtol=1e-10, atol=1e-12)
+            else:
+                np.testing.assert_array_equal(c32, c64)
+            if case % 2 == 0:
+                ob = fo.Bins(True, 2, **_oracle_kw(kw))
+                ref = (ob.count(a) if pair[1] is None else ob.count(a, b))
+                np.testing.assert_array_equal(c32, ref)
+    finally:
+        pc.close()
