@@ -170,13 +170,14 @@ def test_adjoint_random_matches_oracle(case):
         pc.close()
 
 
-@pytest.mark.parametrize("case", range(8))
-def test_survey_spi_wide_low_redshift(case):
-    """(s_perp, pi) over the whole sky at low redshift (objects a few outer
-    radii from the observer, lines of sight in every direction, some within
-    the radius where the line-of-sight prefilter is off): the FP32 path
-    gives the FP64 path's counts exactly, and the oracle's on every other
-    case."""
+@pytest.mark.parametrize("case", range(12))
+def test_survey_wide_low_redshift(case):
+    """Surveys over the whole sky at low redshift (objects a few outer radii
+    from the observer, lines of sight in every direction; for (s_perp, pi)
+    some within the radius where the line-of-sight prefilter is off): the
+    FP32 path gives the FP64 path's counts exactly, and the oracle's on
+    every other case.  Cases 0-7 bin in (s_perp, pi), 8-9 in (s, mu),
+    10-11 in s."""
     import fcfc_gb300 as fg
     from fcfc_gb300 import synth
     rng = np.random.default_rng(zlib.crc32(b"wide%d" % case))
@@ -189,10 +190,14 @@ def test_survey_spi_wide_low_redshift(case):
         int(rng.integers(1500, 4000)), seed=int(rng.integers(1 << 30)), **sk))
     weighted = bool(case % 2)
     wa = rng.uniform(0.5, 1.5, len(a)) if weighted else None
-    pmax = float(rng.choice([5.0, 10.0, 20.0]))
-    kw = dict(smin=0.0, smax=float(rng.choice([10.0, 20.0, 30.0])), ds=1.0,
-              pmin=0.0, pmax=pmax, dpi=1.0)
-    pc = fg.PairCounter("survey", 2, **kw)
+    bt = 2 if case < 8 else (1 if case < 10 else 0)
+    kw = dict(smin=0.0, smax=float(rng.choice([10.0, 20.0, 30.0])), ds=1.0)
+    if bt == 2:
+        kw.update(pmin=0.0, pmax=float(rng.choice([5.0, 10.0, 20.0])),
+                  dpi=1.0)
+    if bt == 1:
+        kw["nmu"] = int(rng.integers(5, 40))
+    pc = fg.PairCounter("survey", bt, **kw)
     pc.load(0, a, wa)
     pc.load(1, b, None)
     try:
@@ -205,7 +210,7 @@ def test_survey_spi_wide_low_redshift(case):
             else:
                 np.testing.assert_array_equal(c32, c64)
             if case % 2 == 0:
-                ob = fo.Bins(True, 2, **_oracle_kw(kw))
+                ob = fo.Bins(True, bt, **_oracle_kw(kw))
                 ref = (ob.count(a) if pair[1] is None else ob.count(a, b))
                 np.testing.assert_array_equal(c32, ref)
     finally:
