@@ -474,6 +474,18 @@ OPTIONS = [
 ]
 
 
+class _FirstValue(argparse.Action):
+    """Keep an option's first value, as libcfg does (a repeated option is
+    reported and dropped, src/lib/libcfg.c:1106-1112)."""
+
+    def __call__(self, parser, namespace, values, option_string=None):
+        if getattr(namespace, self.dest, None) is not None:
+            print("Warning: omitting duplicate entry of parameter `%s'"
+                  % self.dest, file=sys.stderr)
+            return
+        setattr(namespace, self.dest, values)
+
+
 def main(argv=None):
     """FCFC's command line: every option sets its key over the configuration
     file's value; the file defaults to FCFC's name for the geometry, and a
@@ -497,11 +509,13 @@ def main(argv=None):
             continue
         names = (["-" + short] if short else []) + ["--" + long_]
         if kind == "box-opt":
-            ap.add_argument(*names, dest=key, nargs="?", const="", default=None)
+            ap.add_argument(*names, dest=key, nargs="?", const="", default=None,
+                            action=_FirstValue)
         elif kind in ("bool", "survey-bool"):
-            ap.add_argument(*names, dest=key, nargs="?", const="T", default=None)
+            ap.add_argument(*names, dest=key, nargs="?", const="T", default=None,
+                            action=_FirstValue)
         else:
-            ap.add_argument(*names, dest=key, default=None)
+            ap.add_argument(*names, dest=key, default=None, action=_FirstValue)
     a = ap.parse_args(argv)
     path = a.conf or ("fcfc_2pt.conf" if a.survey else "fcfc_2pt_box.conf")
     if os.access(path, os.R_OK):

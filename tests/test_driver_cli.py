@@ -237,6 +237,9 @@ def test_runner_command_line(tmp_path, monkeypatch):
         runner.main(["--box", "-c", str(conf)])
     with pytest.raises(FCFCGError, match="PAIR_COUNT is not set"):
         runner.main(["-c", str(conf), "-S", "0"])
+    # the first value of a repeated option is kept
+    with pytest.raises(FCFCGError, match="DATA_STRUCT"):
+        runner.main(["-c", str(conf), "-S", "3", "-S", "0"])
     monkeypatch.chdir(tmp_path)
     with pytest.raises(FCFCGError, match="PAIR_COUNT is not set"):
         runner.main(["-b", "100", "-i", "a.txt", "-x", "[$1, $2, $3]",
