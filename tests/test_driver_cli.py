@@ -265,3 +265,18 @@ def test_estimators_checked_before_device_work(drivers, tmp_path):
                              % (tmp_path / "xi.txt")))
     with pytest.raises(FCFCGError, match="invalid CF_ESTIMATOR"):
         runner.run(runner.parse_conf(conf.read_text()), "box")
+
+
+def test_option_terminator_and_boolean_forms(drivers, tmp_path):
+    """`--' ends the options (what follows is ignored, as in libcfg); a
+    Boolean option takes T/F or stands alone for T."""
+    conf = tmp_path / "c.conf"
+    conf.write_text(_base_conf("DATA_STRUCT = 2\n"))
+    r = subprocess.run([drivers[0], "-c", str(conf), "--", "-S", "0"],
+                       capture_output=True, text=True)
+    assert "DATA_STRUCT" in r.stderr, r.stderr
+    for opt in (["-v", "F"], ["--verbose=T"], ["-v"], ["-u"], ["--wp", "F"]):
+        r = subprocess.run([drivers[0], "-c", str(conf), "-S", "0"] + opt,
+                           capture_output=True, text=True)
+        assert "PAIR_COUNT" in r.stderr and "argument not found" not in \
+            r.stderr, (opt, r.stderr)
