@@ -580,7 +580,11 @@ def run_adjoint(args, rank, world, local, dist):
         ms1 = pc.stats()["ms_total"]
         a2, _ = pc.adjoint(0, 1, gdr)
         ms2 = pc.stats()["ms_total"]
-        return a1 + a2, ms1 + ms2
+        # the normalisations W (W - 1) and W Wr depend on every data weight
+        gr = np.where(ok, g / np.where(ok, rrn, 1), 0.0)
+        dW = (-(gr * 2 * dd).sum() * (2 * W - 1) / nDD ** 2 +
+              (gr * 2 * dr).sum() * Wr / nDR ** 2)
+        return a1 + a2 + dW, ms1 + ms2
 
     un = [int(pc.count_pairs(0).sum()), int(pc.count_pairs(0, 1).sum())]
     pairs_grad = sum(un)

@@ -432,12 +432,15 @@ __device__ __forceinline__ void hist_add(const fcfcg_launch &L,
   }
 }
 
-/* Queue a pair for the FP64 recheck; when the queue is full, bin it here. */
+/* Queue a pair for the FP64 recheck; when the queue is full, bin it here.
+ * Every ambiguous pair takes a ticket from the fill counter, queued or not,
+ * so one launch can take more than 2^32 of them: the counter is 64-bit, or
+ * it would wrap and hand out slots of pairs still waiting in the queue. */
 template <int WT, int BATCH>
 __device__ __forceinline__ void enqueue(const fcfcg_launch &L,
     const MockSh *ms, uint32_t a, uint32_t b, uint32_t code, uint32_t *h,
     unsigned long long &n_inline) {
-  uint32_t slot = atomicAdd(L.qcount, 1u);
+  const unsigned long long slot = atomicAdd(L.qcount, 1ull);
   if (slot < L.qcap) {
     *((uint4 *) L.queue + slot) = make_uint4(a, b, code, BATCH ? ms->id : 0u);
     return;
@@ -498,7 +501,7 @@ __device__ __forceinline__ void adj_pair(const fcfcg_launch &L, uint32_t a,
  * when the queue is full. */
 __device__ __forceinline__ void enqueue_adj(const fcfcg_launch &L,
     uint32_t a, uint32_t b, uint32_t code, unsigned long long &n_inline) {
-  uint32_t slot = atomicAdd(L.qcount, 1u);
+  const unsigned long long slot = atomicAdd(L.qcount, 1ull);
   if (slot < L.qcap) {
     *((uint4 *) L.queue + slot) = make_uint4(a, b, code, 0u);
     return;
@@ -1227,8 +1230,8 @@ k_count64(const fcfcg_launch L) {
 
 /* Queued pairs to recheck: the queue's fill, at most its capacity. */
 __device__ __forceinline__ uint32_t queue_len(const fcfcg_launch &L) {
-  const uint32_t n = *(volatile const uint32_t *) L.qcount;
-  return n < L.qcap ? n : L.qcap;
+  const unsigned long long n = *(volatile const unsigned long long *) L.qcount;
+  return n < L.qcap ? (uint32_t) n : L.qcap;
 }
 
 /* Adjoint: FP64 recheck of queued pairs. */

@@ -56,8 +56,9 @@ struct fcfcg_ctx {
   unsigned long long *d_cnt, *d_wt, *d_stats, *d_bbox;
   double *d_wd;
   double *d_gfix;                /* adjoint: the scaled cotangent */
-  uint32_t *d_head, *d_qcount, *d_queue;
-  size_t qcap;
+  uint32_t *d_head, *d_queue;      /* d_head: chunk counter, pad, fill */
+  unsigned long long *d_qcount;    /* queue fill (64-bit), in d_head */
+  size_t qcap, qcap_alloc;
   void *h_pinned;
   size_t h_pinned_cap;
   fcfcg_stats stats;
@@ -279,8 +280,8 @@ int fcfcg_create(const fcfcg_binning *cfg, int device, fcfcg_ctx **out) {
                 sizeof(double) * (fcfcg_prep_partials() + 1)));
   CK(cudaMalloc((void **) &c->d_bbox, sizeof(unsigned long long) * 6));
   CK(cudaMalloc((void **) &c->d_head, sizeof(uint32_t) * 4));
-  c->d_qcount = c->d_head + 1;
-  c->qcap = (size_t) 1 << 25;   /* 32M pairs, 512 MiB */
+  c->d_qcount = (unsigned long long *) (c->d_head + 2);
+  c->qcap = c->qcap_alloc = (size_t) 1 << 25;   /* 32M pairs, 512 MiB */
   CK(cudaMalloc((void **) &c->d_queue, sizeof(uint32_t) * 4 * c->qcap));
   CK(cudaStreamSynchronize(c->stream));
   return FCFCG_OK;
@@ -328,6 +329,12 @@ int fcfcg_set_cells_per_smax(fcfcg_ctx *c, int k) {
   if (!c || k < 0 || k > 8) return FCFCG_ERR_ARG;
   c->kcell = k;
   for (int i = 0; i <= FCFCG_MAX_SLOT; i++) c->slot[i].grid_valid = 0;
+  return FCFCG_OK;
+}
+
+int fcfcg_set_queue_capacity(fcfcg_ctx *c, size_t cap) {
+  if (!c || c->host_only) return FCFCG_ERR_ARG;
+  c->qcap = cap < c->qcap_alloc ? cap : c->qcap_alloc;
   return FCFCG_OK;
 }
 
@@ -1228,7 +1235,7 @@ static int count_launch(fcfcg_ctx *c, const count_plan *P, int sort_a,
     CK(cudaMemsetAsync(c->d_wd, 0, sizeof(double) * b->ntot, c->stream));
   CK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * 4,
                      c->stream));
-  CK(cudaMemsetAsync(c->d_head, 0, sizeof(uint32_t) * 2, c->stream));
+  CK(cudaMemsetAsync(c->d_head, 0, sizeof(uint32_t) * 4, c->stream));
   if (timed) CK(cudaEventRecord(c->ev[2], c->stream));
   size_t smem = 0;
   CKK(fcfcg_k_count(c->stream, L, P->prec, c->nsm, &smem));
@@ -2233,18 +2240,18 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
   L.chunk_head = c->d_head;
   BCK(cudaMemsetAsync(c->d_stats, 0, sizeof(unsigned long long) * 4,
                       c->stream));
-  BCK(cudaMemsetAsync(c->d_head, 0, sizeof(uint32_t) * 2, c->stream));
+  BCK(cudaMemsetAsync(c->d_head, 0, sizeof(uint32_t) * 4, c->stream));
   BCK(cudaEventRecord(c->ev[2], c->stream));
   size_t smem = 0;
   BCKK(fcfcg_k_count(c->stream, &L, prec, c->nsm, &smem));
   c->launches += 1;
   BCK(cudaEventRecord(c->ev[3], c->stream));
-  uint32_t nq = 0;
+  unsigned long long nq = 0;
   BCK(cudaMemcpyAsync(&nq, c->d_qcount, sizeof nq, cudaMemcpyDeviceToHost,
                       c->stream));
   BCK(cudaStreamSynchronize(c->stream));
-  if (nq > c->qcap) nq = (uint32_t) c->qcap;
-  BCKK(fcfcg_k_recheck(c->stream, &L, nq));
+  if (nq > c->qcap) nq = c->qcap;
+  BCKK(fcfcg_k_recheck(c->stream, &L, (uint32_t) nq));
   c->launches += nq ? 1 : 0;
   BCK(cudaEventRecord(c->ev[4], c->stream));
   /* 9. results */

@@ -157,7 +157,7 @@ typedef struct {
   double *gwd;                 /* ntot FP64 sums (FP64 path) */
   /* recheck queue: uint4 (a, b, code, 0) */
   uint32_t *queue;
-  uint32_t *qcount;
+  unsigned long long *qcount;  /* fill: 64 bits, so it cannot wrap */
   uint32_t qcap;
   unsigned long long *stats;   /* [0] candidates [1] in-range [2] recheck
                                   [3] inline rechecks */

@@ -192,6 +192,11 @@ class PairCounter:
     def set_cells_per_smax(self, k: int):
         self._check(self.lib.fcfcg_set_cells_per_smax(self.h, int(k)))
 
+    def set_queue_capacity(self, cap: int):
+        """Limit the FP64 recheck queue (pairs beyond are binned inside the
+        counting kernel; the counts do not change)."""
+        self._check(self.lib.fcfcg_set_queue_capacity(self.h, int(cap)))
+
     def autotune(self, a: int, b: int | None = None, weighted=False):
         """Time the FP32 count at 1..8 cells per maximum separation and keep
         the fastest for catalogues of this density; returns (k, ms)."""

@@ -352,6 +352,13 @@ int fcfcg_stats_get(const fcfcg_ctx *ctx, fcfcg_stats *out);
  * box). */
 int fcfcg_set_cells_per_smax(fcfcg_ctx *ctx, int k);
 
+/* Capacity of the FP64 recheck queue in pairs (default and maximum: the
+ * 2^25 pairs allocated with the context; larger values are clamped).
+ * Ambiguous pairs beyond it are binned by the FP64 formula inside the
+ * counting kernel instead of after it: the counts are the same, only
+ * slower.  Meant for tests of that overflow path. */
+int fcfcg_set_queue_capacity(fcfcg_ctx *ctx, size_t cap);
+
 /*
  * Autotune the grid refinement for this binning and catalogue pair: times
  * the FP32 count at 1..8 cells per maximum separation (stopping two past
@@ -419,10 +426,11 @@ int fcfcg_write_wp(const fcfcg_ctx *ctx, const char *fname, const double *wp);
 #define FCFCG_NOALLOC_SCRATCH_BYTES (4u << 20)
 
 /*
- * Unweighted pair counts for callers that cannot allocate device memory
- * (code running inside another framework's memory pool, a CUDA graph being
- * built, or an embedding that forbids cudaMalloc).  No counterpart in the
- * reference; it is a variant of the FP64 counting kernel.
+ * Unweighted pair counts for callers that cannot allocate device memory:
+ * code that runs inside another framework's memory pool (whose allocator
+ * owns the device and must not be bypassed), or a host program embedded
+ * under a policy that forbids cudaMalloc after start-up.  No counterpart in
+ * the reference; it is a variant of the FP64 counting kernel.
  *
  * bins_ctx: a host-only context (fcfcg_create_host) describing the bins; it
  * is only read.  xa/ya/za (na objects) and xb/yb/zb (nb, ignored when

@@ -52,3 +52,46 @@ def test_non_finite_inputs_rejected():
         assert e.value.code == fg.capi.ERR_DATA
     pc.load(0, x)
     assert pc.count_pairs(0).sum() > 0
+
+
+def test_recheck_queue_overflow():
+    """Ambiguous pairs that find the FP64 recheck queue full are binned in
+    the counting kernel itself (plain, weighted, batched and adjoint
+    kernels): the results must not change with the queue's capacity."""
+    import fcfc_gb300 as fg
+    from fcfc_gb300 import synth
+    kws = dict(ra=(150.0, 158.0), dec=(10.0, 17.0), zmu=0.5, zsig=0.04,
+               zr=(0.46, 0.54))
+    d = synth.radecz_to_xyz(synth.survey_radecz(3000, seed=81, **kws))
+    r = synth.radecz_to_xyz(synth.survey_radecz(4000, seed=82, **kws))
+    wd = synth.lognormal_weights(len(d), 0.3, seed=83)
+    pc = fg.PairCounter("survey", fg.BIN_SMU, smin=0, smax=40, ds=0.5, nmu=60)
+    ob = fo.Bins(True, 1, ns=80, smin=0, ds=0.5, nmu=60)
+    pc.load(0, d, wd)
+    pc.load(1, r)
+    want = ob.count(d, r, mode=1)
+    want_w = ob.count(d, r, wa=wd, mode=1)
+    g = np.random.default_rng(84).normal(size=pc.ntot)
+    pc.set_queue_capacity(1 << 30)          # clamped to the allocation
+    ref_dw, ref_dr = pc.adjoint(0, 1, g)
+    for cap in (0, 5):
+        pc.set_queue_capacity(cap)
+        np.testing.assert_array_equal(pc.count_pairs(0, 1), want)
+        st = pc.stats()
+        assert st["precision_used"] == fg.PREC_FP32_RECHECK
+        assert st["rechecked"] > cap and st["recheck_inline"] == st["rechecked"] - cap
+        np.testing.assert_allclose(pc.count_pairs(0, 1, weighted=True), want_w,
+                                   rtol=1e-10, atol=1e-300)
+        dw, dr = pc.adjoint(0, 1, g)
+        np.testing.assert_allclose(dw, ref_dw, rtol=1e-11, atol=1e-11 * np.abs(ref_dw).max())
+        np.testing.assert_allclose(dr, ref_dr, rtol=1e-11, atol=1e-11 * np.abs(ref_dr).max())
+    # batched boxes share the queue
+    bx = fg.PairCounter("box", fg.BIN_SMU, box=300.0, smin=0, smax=40, ds=0.5,
+                        nmu=60)
+    cats = [synth.neyman_scott(30, 300.0, 40, 3.0, seed=85 + k) for k in range(3)]
+    bx.set_queue_capacity(3)
+    cnt, status, _ = bx.count_batch(cats, [300.0] * 3)
+    assert not any(status)
+    for k in range(3):
+        obk = fo.Bins(False, 1, ns=80, smin=0, ds=0.5, nmu=60, box=300.0)
+        np.testing.assert_array_equal(cnt[k], obk.count(cats[k], mode=1))

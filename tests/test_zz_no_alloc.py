@@ -1,6 +1,7 @@
 """fcfcg_count_noalloc: unweighted counts for callers that cannot allocate
-device memory (code inside another framework's memory pool or a graph being
-built).  Its results must equal those of the ordinary entry point,
+device memory (code inside another framework's memory pool, whose allocator
+owns the device, or a program whose policy forbids cudaMalloc after
+start-up).  Its results must equal those of the ordinary entry point,
 fcfcg_count, call after call: the scratch it reuses between calls must not
 leak one call's counts into the next.
 
