@@ -227,20 +227,12 @@ def run_reference(args, rank, world):
     return 0
 
 
-def mocks_workload(nmock=256, seed=7, density=2.5e-4, nmin=1e4, nmax=1e6):
+def mocks_workload(nmock=256, seed=7):
     """Neyman-Scott boxes (the generator of the clustered-box workload:
-    Poisson(100) children, sigma = 5 Mpc/h), N log-uniform in [nmin, nmax],
-    box side (N / density)^(1/3)."""
+    Poisson(100) children, sigma = 5 Mpc/h), N log-uniform in [1e4, 1e6],
+    box side (N / 2.5e-4)^(1/3)."""
     from fcfc_gb300 import synth
-    rng = np.random.default_rng(seed)
-    cats, boxes = [], []
-    for j in range(nmock):
-        n = float(np.exp(rng.uniform(np.log(nmin), np.log(nmax))))
-        L = (n / density) ** (1.0 / 3.0)
-        cats.append(synth.neyman_scott(max(1, int(round(n / 100))), L, 100.0,
-                                       5.0, seed=seed * 100003 + j))
-        boxes.append(L)
-    return cats, boxes
+    return synth.mock_boxes(nmock, seed=seed)
 
 
 def run_mocks(args, rank, world, local, dist):
@@ -383,17 +375,7 @@ def survey_workload(nd, nr, seed=11):
     r = synth.survey_radecz(nr, seed=seed + 1)
     wd = synth.fkp_weights(d)
     # the randoms carry the data's n(z) at their redshifts
-    z = d[:, 2]
-    edges = np.arange(z.min(), z.max() + 0.01, 0.01)
-    nz_w = synth.fkp_weights(d)
-    idx = np.clip(np.searchsorted(edges, r[:, 2], side="right") - 1, 0,
-                  len(edges) - 2)
-    per = np.zeros(len(edges) - 1)
-    cnt = np.zeros(len(edges) - 1)
-    di = np.clip(np.searchsorted(edges, z, side="right") - 1, 0, len(edges) - 2)
-    np.add.at(per, di, nz_w)
-    np.add.at(cnt, di, 1)
-    wr = (per / np.maximum(cnt, 1))[idx]
+    wr = synth.fkp_weights(d, at=r)
     return d, r, wd, wr
 
 

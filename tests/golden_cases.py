@@ -124,3 +124,78 @@ class Case:
     def xyzw(self, label):
         a = self.cats[label]
         return a[:, :3], (a[:, 3] if a.shape[1] > 3 else None)
+
+
+# --------------------------------------------------------------------------
+# Full-size fixtures (tests/golden/full, written by make_golden_full.py):
+# FCFC's pair-count files for the benchmark workloads at their stated sizes.
+# The catalogues are regenerated from their specs and checked by sha256.
+
+FULL = os.path.join(GOLDEN, "full")
+
+
+def full_case_names():
+    if not os.path.isdir(FULL):
+        return []
+    return sorted(d for d in os.listdir(FULL)
+                  if os.path.isfile(os.path.join(FULL, d, "meta.json")))
+
+
+class FullCase:
+    _cache: dict = {}
+
+    def __init__(self, name):
+        self.name = name
+        self.dir = os.path.join(FULL, name)
+        with open(os.path.join(self.dir, "meta.json")) as f:
+            self.meta = json.load(f)
+        self.box = self.meta["geometry"] == "box"
+
+    def catalogue(self, label):
+        """(N x 3 or 4 array, sha256 as generated, sha256 recorded)."""
+        from fcfc_gb300 import synth
+        c = self.meta["cats"][label]
+        key = json.dumps(c["spec"], sort_keys=True)
+        if key not in FullCase._cache:
+            a = synth.catalogue(c["spec"])
+            FullCase._cache.clear()          # hold one catalogue set at most
+            FullCase._cache[key] = (a, synth.catalogue_sha256(a))
+        a, h = FullCase._cache[key]
+        return a, h, c["sha256"]
+
+    def runs(self):
+        return self.meta["runs"]
+
+    def pcfile(self, run, pair):
+        return pcfile.read_binary(os.path.join(self.dir, "%s_%s.bin" % (
+            run["name"], pair)))
+
+    def sedges(self, run):
+        if not run.get("sfile"):
+            return None
+        t = np.loadtxt(os.path.join(self.dir, run["sfile"]), ndmin=2)
+        e = np.empty(len(t) + 1)
+        e[0] = t[0, 0]
+        for i in range(1, len(t)):
+            e[i] = t[i, 0] if t[i, 0] == t[i - 1, 1] else 0.5 * (t[i, 0] + t[i - 1, 1])
+        e[-1] = t[-1, 1]
+        return e
+
+    def engine_kwargs(self, run):
+        """PairCounter keyword arguments of a run's binning."""
+        kw = dict(geometry="box" if self.box else "survey",
+                  bintype=run["bintype"])
+        se = self.sedges(run)
+        if se is not None:
+            kw["sedges"] = se
+        else:
+            s = run["sbin"]
+            kw.update(smin=s["smin"], smax=s["smax"], ds=s["ds"])
+        if run["bintype"] == 1:
+            kw["nmu"] = run["nmu"]
+        if run["bintype"] == 2:
+            p = run["pbin"]
+            kw.update(pmin=p["pmin"], pmax=p["pmax"], dpi=p["dpi"])
+        if self.box:
+            kw["box"] = run["box"][0]
+        return kw
