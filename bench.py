@@ -1,29 +1,33 @@
 #!/usr/bin/env python3
-"""Throughput of the GB300 pair-counting engine on FCFC's clustered-box
-workload, one JSON line on stdout.
+"""Throughput of the GB300 pair-counting engine, one JSON line on stdout.
 
-Workload ("ns_box_2e6"): Neyman-Scott catalogue, 2e4 uniform parents in a
-periodic box of side 2000 Mpc/h, Poisson(100) children per parent with
-isotropic Gaussian offsets (sigma = 5 Mpc/h), about 2e6 points with
-lognormal(0, 0.3) weights, FP64 coordinates.  One step counts the weighted
-DD pairs twice, as two FCFC runs would:
-  (s, mu)       s in [0, 200) Mpc/h, 40 linear bins, 100 mu bins;
-  (s_perp, pi)  40 logarithmic s_perp bins in [0.1, 100), pi in [0, 40) in
-                40 linear bins.
-The metric is unique in-range pairs per second (pairs that land in a bin,
-i < j), summed over both counts.
+Default workload ("mocks256"): 256 periodic Neyman-Scott boxes (Poisson(100)
+children per parent, Gaussian offsets sigma = 5 Mpc/h) with N log-uniform in
+[1e4, 1e6] and box side (N / 2.5e-4)^(1/3); FCFC refuses the boxes with
+s_max >= L / 2 (26 of them), the other 230 (5.5e7 points) are counted in
+one persistent launch per step: unweighted DD in (s, mu), s in [0, 200)
+Mpc/h in 40 bins, 100 mu bins.  The metric is unique in-range pairs per
+second (pairs that land in a bin, i < j).
 
-  value   -- FP32 + FP64-recheck path, catalogue already in HBM; a step is
-             catalogue preparation (rescale, cell sort) plus both counts,
-             timed whole with CUDA events (the device idle on both sides,
-             host round trips included); L2 is flushed between steps.
-  e2e     -- the same step through the C ABI from pinned host buffers: the
-             host-to-device copy of the catalogue and the read-back of the
-             counts are inside the timed region.
-  fp64    -- the all-FP64 GPU path on the same step (one step).
---impl reference times the CPU restatement of FCFC's counter (oracle/, the
-reference's FP64 per-pair formula, OpenMP on every host core) on a bounded
-sample of the workload (same density, smaller box).
+  value   -- FP32 + FP64-recheck path, catalogues already in HBM; a step is
+             the batched count (rescale, cell sort, count, recheck), timed
+             with CUDA events, the device idle on both sides; L2 is flushed
+             between steps.
+  e2e     -- the same step from pinned host arrays through the C ABI: the
+             catalogues' transfer and the counts' read-back are inside.
+  fp64    -- the all-FP64 GPU path on every accepted mock (one pass), with
+             a check that its counts equal the FP32 path's.
+  cpu_baseline -- the CPU restatement of FCFC's counter (oracle/: FCFC's FP64
+             per-pair formula on a cell grid, OpenMP on every host core) on
+             every 64th accepted mock; cpu_sample_on_gpu is the GPU on the
+             same mocks.
+--impl reference times that CPU restatement on the same sample mocks, each
+step one pass over them.
+
+Other workloads (--workload): ns_box_2e6 (one weighted 2e6-point box in
+(s, mu) and (s_perp, pi)), survey (DD/DR/RR of 1e6 data and 1e7 randoms),
+adjoint (dL/dw of a Landy-Szalay loss), cli (the command line drivers end
+to end on an ASCII catalogue).
 """
 from __future__ import annotations
 
@@ -180,10 +184,40 @@ def max_over_ranks(value, dist):
     return float(t[0])
 
 
+def run_reference_mocks(args, rank, world):
+    """CPU restatement of FCFC's counter on the sample mocks of the batched
+    workload (every 64th accepted mock), every host core."""
+    from fcfc_gb300 import synth
+    _, boxes = synth.mock_boxes(256, seed=7, sizes_only=True)
+    acc = [j for j, L in enumerate(boxes) if 2 * MOCK_SMAX < L]
+    subset = acc[::MOCK_CPU_STRIDE]
+    cats = {j: synth.mock_boxes(j + 1, seed=7, first=j)[0][0] for j in subset}
+    val, pairs, ms, desc = mocks_cpu_sample(cats, boxes, subset,
+                                            steps=args.steps,
+                                            warmup=args.warmup)
+    out = {
+        "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": mocks_config(256, boxes),
+        "impl": "reference",
+        "cpu_baseline": {"value": val, "unit": UNIT,
+                         "cores": os.cpu_count() or 1, "kind": "port",
+                         "sample": desc},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_reference(args, rank, world):
     """CPU restatement of FCFC's counter on a bounded sample of the workload."""
     if rank != 0:
         return 0
+    if args.workload == "mocks256":
+        return run_reference_mocks(args, rank, world)
     from oracle import fcfc_oracle as fo
     box = 1200.0   # same density: 2e4 * (1200/2000)^3 parents
     x, w = workload(box=box, nparent=int(round(20000 * (box / BOX) ** 3)), seed=1)
@@ -235,6 +269,76 @@ def mocks_workload(nmock=256, seed=7):
     return synth.mock_boxes(nmock, seed=seed)
 
 
+MOCK_SMAX = 200.0
+MOCK_CPU_STRIDE = 64     # the CPU sample: every 64th accepted mock
+
+
+def mocks_config(nmock, boxes):
+    """The workload's configuration, the same dict in both arms."""
+    acc = [j for j, L in enumerate(boxes) if 2 * MOCK_SMAX < L]
+    return {"workload": "mocks%d" % nmock, "n_catalogues": nmock,
+            "accepted": len(acc),
+            "rejected_smax_ge_half_box": nmock - len(acc),
+            "bins": "(s,mu) 40x100 s<200", "weighted": False,
+            "density": 2.5e-4, "n_range": [1e4, 1e6], "seed": 7,
+            "cpu_sample": "accepted mocks %s (one in %d)" % (
+                acc[::MOCK_CPU_STRIDE], MOCK_CPU_STRIDE),
+            "l2": "flushed between GPU steps (256 MiB write)"}
+
+
+def mocks_cpu_sample(cats, boxes, subset, steps=1, warmup=0):
+    """The CPU restatement of FCFC's counter (oracle/, cell grid, OpenMP on
+    every host core) on the sample mocks: (pairs/s, in-range pairs, s per
+    step, description)."""
+    from oracle import fcfc_oracle as fo
+    bins = [fo.Bins(False, 1, ns=40, smin=0, ds=5, nmu=100, box=boxes[j])
+            for j in subset]
+    pairs = 0
+    tt = 0.0
+    for it in range(warmup + steps):
+        t0 = time.perf_counter()
+        tot = 0
+        for b, j in zip(bins, subset):
+            tot += int(b.count(cats[j], mode=3).sum())
+        dt = time.perf_counter() - t0
+        pairs = tot
+        if it >= warmup:
+            tt += dt
+    ms = tt / steps
+    desc = ("mocks %s of the 256 (%d catalogues, %d points, %d in-range "
+            "pairs per step), unweighted DD (s,mu) 40x100, %.2f s per step" % (
+                list(subset), len(subset), sum(len(cats[j]) for j in subset),
+                pairs, ms))
+    return pairs / ms, pairs, ms, desc
+
+
+def profile_info(name):
+    """Figures of a committed ncu summary (``key: value`` lines) and whether
+    it was captured on the current count kernel source (its recorded
+    sha256 of count.cu against the file's)."""
+    import hashlib
+    info = {}
+    try:
+        for line in open(os.path.join(ROOT, "profiles", name)):
+            if ":" in line and not line.startswith((" ", "#")):
+                k, v = line.split(":", 1)
+                info[k.strip()] = v.strip()
+    except OSError:
+        return None
+    src = open(os.path.join(ROOT, "fcfc_gb300", "csrc", "count.cu"), "rb").read()
+    info["source_matches"] = (info.get("count_cu_sha256") ==
+                              hashlib.sha256(src).hexdigest())
+    return info
+
+
+def smem_atomic_peak(local):
+    import ctypes as C
+    import fcfc_gb300 as fg
+    v = C.c_double()
+    rc = fg.capi.load_library().fcfcg_probe_smem_atomics(int(local), C.byref(v))
+    return v.value if rc == 0 else None
+
+
 def run_mocks(args, rank, world, local, dist):
     """256 mock boxes, unweighted DD (s, mu) 40 x 100, one persistent launch
     per step (fcfcg_count_batch)."""
@@ -254,12 +358,28 @@ def run_mocks(args, rank, world, local, dist):
         dcats.append((cols[0].data_ptr(), cols[1].data_ptr(),
                       cols[2].data_ptr(), len(x)))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    pc = fg.PairCounter("box", fg.BIN_SMU, box=max(boxes), smin=0, smax=200,
-                        ds=5, nmu=100, device=local)
+    pc = fg.PairCounter("box", fg.BIN_SMU, box=max(boxes), smin=0,
+                        smax=MOCK_SMAX, ds=5, nmu=100, device=local)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
 
-    def step(on_device=True, cat=None):
-        return pc.count_batch(cat if cat is not None else dcats, boxes,
-                              on_device=on_device)
+    def timed(fn, *a, **kw):
+        """CUDA events on the current stream around a call that returns when
+        its device work is done, the device idle on both sides."""
+        torch.cuda.synchronize()
+        e0.record()
+        r = fn(*a, **kw)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), r
+
+    def step(on_device=True, cat=None, sel=None, precision=fg.PREC_FP32_RECHECK):
+        c = cat if cat is not None else dcats
+        b = boxes
+        if sel is not None:
+            c = [c[j] for j in sel]
+            b = [boxes[j] for j in sel]
+        return pc.count_batch(c, b, on_device=on_device, precision=precision)
 
     counts, status, _ = step()
     accepted = [j for j in range(nmock) if status[j] == 0]
@@ -267,9 +387,7 @@ def run_mocks(args, rank, world, local, dist):
     # fixed s_max / 3 cells against the autotuned refinement
     pc.set_cells_per_smax(3)
     step()
-    t0 = time.perf_counter()
-    step()
-    ms_fixed3 = (time.perf_counter() - t0) * 1e3
+    ms_fixed3, _ = timed(step)
     pc.set_cells_per_smax(0)
     k_tuned, _ = pc.autotune_batch(dcats, boxes, on_device=True)
     for _ in range(max(args.warmup, 0)):
@@ -283,81 +401,104 @@ def run_mocks(args, rank, world, local, dist):
     tt, tk = 0.0, 0.0
     for _ in range(args.steps):
         flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        step()
-        tt += time.perf_counter() - t0
+        ms, _ = timed(step)
+        tt += ms
         tk += pc.stats()["ms_count"]
     clocks = clk.stop()
     st = pc.stats()
     launches = pc.stats()["launches"] - launches0
-    ms_step = max_over_ranks(tt / args.steps * 1e3, dist)
+    ms_step = max_over_ranks(tt / args.steps, dist)
     value = pairs * world / (ms_step * 1e-3)
     k_ms = tk / args.steps
-    # all-FP64 path on every 8th accepted catalogue (the same catalogues)
-    sub = accepted[::8]
-    sub_cats = [dcats[j] for j in sub]
-    sub_boxes = [boxes[j] for j in sub]
-    c64, _, _ = pc.count_batch(sub_cats, sub_boxes, on_device=True,
-                               precision=fg.PREC_FP64)
-    t0 = time.perf_counter()
-    c64, _, _ = pc.count_batch(sub_cats, sub_boxes, on_device=True,
-                               precision=fg.PREC_FP64)
-    ms64 = (time.perf_counter() - t0) * 1e3
-    pairs64 = int(sum(int(c.sum()) for c in c64))
-    t0 = time.perf_counter()
-    c32, _, _ = pc.count_batch(sub_cats, sub_boxes, on_device=True)
-    ms32_sub = (time.perf_counter() - t0) * 1e3
-    exact = all(np.array_equal(a, b) for a, b in zip(c64, c32))
-    # end to end from host arrays (x, y, z columns per catalogue, pageable
-    # memory; the copies to the device are inside the timed region)
-    cols = [tuple(np.ascontiguousarray(x[:, k]) for k in range(3)) for x in cats]
-    step(on_device=False, cat=cols)
+    # the all-FP64 path on every accepted catalogue: same counts?
+    ms64, (c64, _, _) = timed(step, precision=fg.PREC_FP64)
+    exact = all(np.array_equal(c64[j], counts[j]) for j in accepted)
+    # the CPU sample mocks on the GPU (one launch of just those catalogues)
+    subset = accepted[::MOCK_CPU_STRIDE]
+    step(sel=subset)
+    ms_sub = min(timed(step, sel=subset)[0] for _ in range(3))
+    pairs_sub = int(sum(int(counts[j].sum()) for j in subset))
+    # end to end from pinned host arrays (x, y, z columns per catalogue; the
+    # copies to the device are inside the timed region)
+    cols = [tuple(torch.from_numpy(np.ascontiguousarray(x[:, k])).pin_memory()
+                  for k in range(3)) for x in cats]
+    hcols = [tuple(t.numpy() for t in c) for c in cols]
+    step(on_device=False, cat=hcols)
     te = 0.0
     for _ in range(args.steps):
         flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        step(on_device=False, cat=cols)
-        te += time.perf_counter() - t0
-    e2e_ms = te / args.steps * 1e3
+        ms, _ = timed(step, on_device=False, cat=hcols)
+        te += ms
+    e2e_ms = te / args.steps
     peak = fp32_peak_tflops(dev)
+    apeak = smem_atomic_peak(local)
     achieved = pairs * FLOPS_PER_PAIR["smu"] / (k_ms * 1e-3) / 1e12
+    prof = profile_info("k_count32_batch_mocks32.txt") or {}
+    traffic = None
+    if prof.get("traffic_bytes_per_launch_full_workload"):
+        traffic = float(prof["traffic_bytes_per_launch_full_workload"])
+    ipp = float(prof["warp_instructions_per_in_range_pair"]) \
+        if prof.get("warp_instructions_per_in_range_pair") else None
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    cfg = mocks_config(nmock, boxes)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64-recheck", "data": "synthetic",
-        "config": {"workload": "mocks%d" % nmock, "n_catalogues": nmock,
-                   "n_points": ntot_pts, "accepted": len(accepted),
-                   "rejected_smax_ge_half_box": nmock - len(accepted),
-                   "bins": "(s,mu) 40x100 s<200", "weighted": False,
-                   "pairs_per_step": pairs,
-                   "density": 2.5e-4, "n_range": [1e4, 1e6],
-                   "l2": "flushed between steps (256 MiB write)",
-                   "cells_per_smax_autotuned": k_tuned,
-                   "ms_per_step_fixed_smax_over_3": ms_fixed3,
-                   "parallelism": "replicas" if world > 1 else "1 GPU"},
-        "fp64": {"value": pairs64 / (ms64 * 1e-3), "unit": UNIT,
-                 "catalogues": len(sub), "pairs": pairs64, "ms": ms64,
-                 "fp32_recheck_ms_same_catalogues": ms32_sub,
-                 "speedup_fp32_recheck_over_fp64": ms64 / ms32_sub,
+        "config": cfg,
+        "workload_detail": {
+            "n_points": ntot_pts, "pairs_per_step": pairs,
+            "timing": "CUDA events on the current stream around each "
+                      "batched count, device idle on both sides",
+            "cells_per_smax_autotuned": k_tuned,
+            "ms_per_step_fixed_smax_over_3": ms_fixed3,
+            "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "fp64": {"value": pairs / (ms64 * 1e-3), "unit": UNIT,
+                 "catalogues": len(accepted), "pairs": pairs, "ms": ms64,
+                 "speedup_fp32_recheck_over_fp64": ms64 / ms_step,
                  "counts_identical": exact},
+        "cpu_sample_on_gpu": {"value": pairs_sub / (ms_sub * 1e-3),
+                              "unit": UNIT, "catalogues": subset,
+                              "pairs": pairs_sub, "ms": ms_sub},
         "e2e": {"value": pairs / (e2e_ms * 1e-3), "unit": UNIT,
                 "ms_per_step": e2e_ms, "h2d_bytes_per_step": ntot_pts * 24,
                 "d2h_bytes_per_step": len(accepted) * pc.ntot * 8},
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "issue", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "k_count32<box,smu,unweighted,batch>",
+                     "traffic": traffic,
+                     "kernel": "k_count32<box,smu,unweighted,batch>",
                      "kernel_ms": k_ms,
                      "peak_source": "measured cuBLAS SGEMM (TF32 off) on this GPU",
-                     "flops_per_pair": FLOPS_PER_PAIR["smu"]},
+                     "flops_per_pair": FLOPS_PER_PAIR["smu"],
+                     "smem_atomics": None if not apeak else {
+                         "achieved": pairs / (k_ms * 1e-3), "peak": apeak,
+                         "unit": "shared 32-bit atomic adds/s",
+                         "frac": pairs / (k_ms * 1e-3) / apeak,
+                         "per_pair": 1,
+                         "peak_source": "fcfcg_probe_smem_atomics on this GPU "
+                                        "(lane-distinct banks, every SM)"},
+                     "issue": None if ipp is None else {
+                         "achieved": pairs / (k_ms * 1e-3) * ipp,
+                         "peak": 152 * 4 * mhz * 1e6,
+                         "unit": "warp instructions/s",
+                         "frac": pairs / (k_ms * 1e-3) * ipp / (152 * 4 * mhz * 1e6),
+                         "warp_instructions_per_pair": ipp},
+                     "from_profile": {
+                         "file": "profiles/k_count32_batch_mocks32.txt",
+                         "keys": ["traffic", "issue.warp_instructions_per_pair"],
+                         "captured_on_current_source": prof.get("source_matches")}},
         "counters": {"candidates": st["candidates"], "rechecked": st["rechecked"],
                      "nchunks": st["nchunks"], "ms_grid": st["ms_grid"],
                      "ms_recheck": st["ms_recheck"]},
         "clocks": clocks,
         "gpu_launches": int(launches),
     }
+    if rank == 0 and not args.no_cpu and not args.small:
+        v, p_, ms_c, desc = mocks_cpu_sample(cats, boxes, subset)
+        out["cpu_baseline"] = {"value": v, "unit": UNIT,
+                               "cores": os.cpu_count() or 1, "kind": "port",
+                               "sample": desc, "pairs_match_gpu": p_ == pairs_sub}
     if dist:
         dist.barrier()
     if rank == 0:
@@ -734,7 +875,7 @@ def main():
     ap.add_argument("--small", action="store_true",
                     help="quarter-size box (for profiler captures)")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="ns_box_2e6",
+    ap.add_argument("--workload", default="mocks256",
                     choices=["ns_box_2e6", "mocks256", "survey", "adjoint",
                              "cli"],
                     help="mocks256: 256 mock boxes in one persistent launch; "

@@ -18,7 +18,7 @@ LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libfcfcg.so")
 
-CU_SOURCES = ["prep.cu", "count.cu", "cnvt.cu"]
+CU_SOURCES = ["prep.cu", "count.cu", "cnvt.cu", "probe.cu"]
 C_SOURCES = ["bins.c", "ctx.c", "epilogue.c", "cnvt.c"]
 HEADERS = ["fcfcg_internal.h", "legauss_tab.h",
            os.path.join("..", "..", "include", "fcfcg.h")]

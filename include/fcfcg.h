@@ -420,6 +420,18 @@ int fcfcg_write_multipoles(const fcfcg_ctx *ctx, const char *fname,
     int npole, const int *poles, const double *mp);
 int fcfcg_write_wp(const fcfcg_ctx *ctx, const char *fname, const double *wp);
 
+/* ---------------- measurement ------------------------------------------- */
+
+/*
+ * Measured rate of 32-bit shared-memory atomic adds on CUDA device `device`
+ * (-1: the current one), all SMs busy, every lane of a warp on its own bank:
+ * the peak the histogram updates of the counting kernels (one per in-range
+ * pair, two for weighted sums) are measured against.  Takes a few
+ * milliseconds; allocates 4 bytes of device memory for the check.  No
+ * counterpart in the reference.
+ */
+int fcfcg_probe_smem_atomics(int device, double *adds_per_s);
+
 /* ---------------- allocation-free counting ------------------------------ */
 
 /* Bytes of the fixed device scratch fcfcg_count_noalloc works in. */
