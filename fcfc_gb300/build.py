@@ -18,9 +18,10 @@ LIBDIR = os.path.join(HERE, "lib")
 OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libfcfcg.so")
 
-CU_SOURCES = ["prep.cu", "count.cu", "cnvt.cu", "probe.cu"]
+CU_SOURCES = ["prep.cu", "count.cu", "count32_box.cu", "count32_survey.cu",
+              "count32_batch.cu", "count32_adj.cu", "cnvt.cu", "probe.cu"]
 C_SOURCES = ["bins.c", "ctx.c", "epilogue.c", "cnvt.c"]
-HEADERS = ["fcfcg_internal.h", "legauss_tab.h",
+HEADERS = ["fcfcg_internal.h", "legauss_tab.h", "count_common.cuh", "count32.cuh",
            os.path.join("..", "..", "include", "fcfcg.h")]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

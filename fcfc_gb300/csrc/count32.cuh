@@ -1,0 +1,704 @@
+/*
+ * count32.cuh -- the FP32 pair-counting kernel (instantiated by count32_*.cu).
+ *
+ * Work decomposition (replaces FCFC's dual k-d tree, src/fcfc/2pt_box/
+ * dual_tree.c:245-373, and its OpenMP/MPI node-pair scheduler,
+ * count_func.c:7431-7722):
+ *   - points are sorted into a uniform cell grid; a cell is cut into chunks
+ *     of at most 32 points;
+ *   - a persistent warp takes the next chunk from a global counter, holds one
+ *     chunk point per lane (lanes are replicated over the neighbour's points
+ *     when the chunk is short) and walks the cell-offset stencil, streaming
+ *     the neighbour cell's points from L1/L2;
+ *   - auto counts use half of the stencil and i<j inside a cell.
+ *
+ * Per pair (FP32 path): separations on coordinates relative to the cell
+ * centres, bin lookup in shared-memory tables, and a rounding bound: a pair
+ * whose s^2, mu, s_perp^2 or pi lies within the bound of a bin edge is queued
+ * and re-binned by the FP64 formula of the reference (metric_common.c of
+ * src/fcfc/2pt_box and src/fcfc/2pt), so integer counts equal the FP64 build.
+ *
+ * Histograms live in shared memory (u32 counts, or int64 fixed-point weight
+ * products) and are merged into global 64/128-bit integer accumulators, so
+ * the results do not depend on the order of the additions.
+ */#ifndef FCFCG_COUNT32_CUH
+#define FCFCG_COUNT32_CUH
+#include "count_common.cuh"
+
+/* Image code of the neighbour cell of a stencil offset (box). */
+__device__ __forceinline__ uint32_t nb_code(const int *ncell, int cx,
+    int cy, int cz, int4 o) {
+  int q[3] = {cx + o.x, cy + o.y, cz + o.z};
+  uint32_t code = 0;
+  for (int k = 0; k < 3; k++) {
+    const int n = ncell[k];
+    int w = 0;
+    while (q[k] < 0) { q[k] += n; w--; }
+    while (q[k] >= n) { q[k] -= n; w++; }
+    code |= (uint32_t) (w + 1) << (2 * k);
+  }
+  return code;
+}
+
+/*
+ * Bin one queued pair per lane.  FP32 windows decide; ambiguous pairs go to
+ * the FP64 recheck queue.  c2 = twice the chunk cell's centre (survey).
+ */
+template <int GEOM, int BIN, int WT, int BATCH, int ADJ>
+__device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
+    const MockSh *ms, const Stage &S, uint32_t ent, uint32_t first, int cx,
+    int cy, int cz,
+    float c2x, float c2y, float c2z, const uint16_t *fs, const uint16_t *fp,
+    const float *fse, const float *fpe, uint32_t *h, uint32_t &n_in,
+    uint32_t &n_q, unsigned long long &n_inline, long long &gbv) {
+  const int i = (int) (ent & 63u), src = (int) (ent >> 6);
+  const float4 pa = S.a[i];
+  const float4 pb = S.b[src];
+  const float dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
+  bool amb = false;
+  int bin = -1;
+  if (IS_SPI(BIN) && GEOM == FCFCG_GEOM_BOX) {
+    const float sp2 = fmaf(dy, dy, dx * dx);
+    const float pi = fabsf(dz);
+    amb = !(sp2 >= L.tiny);
+    /* with a bit-pattern table (log bins, narrow near zero) the window of
+     * s_perp^2 follows s_perp; otherwise its value at s_perp max (tiny sp2
+     * is ambiguous anyway) */
+    const float Es = LOGTAB(BIN)
+        ? fmaf(L.K2, sp2, fmaf(L.K1, sp2 * rsqrtf(sp2), L.K0)) : L.Emax;
+    unsigned sb = ftab_bin<false, LOGTAB(BIN)>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb, sp2, Es, amb, L.fslog, L.fsamb);
+    unsigned pbn = ftab_bin<false, false>(fp, L.fpoff, L.nfp, L.fpinv, fpe, L.npb, pi, L.P0, amb, L.fplog, L.fpamb);
+    if (!amb) {
+      if (sb == FCFCG_FTAB_BIN_MASK || pbn == FCFCG_FTAB_BIN_MASK) return;
+      bin = (int) sb + (int) pbn * L.ns;
+    }
+  } else {
+    const float s2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    amb = !(s2 >= L.tiny);
+    if (IS_ISO(BIN) && LINS(BIN)) {
+      const int k = lin_bin(L, s2 * rsqrtf(s2), amb);
+      if (!amb) {
+        if ((unsigned) k >= (unsigned) L.ns) return;
+        bin = k;
+      }
+    } else if (IS_ISO(BIN)) {
+      /* with a bit-pattern table the window follows s (log bins near zero
+       * are narrower than its value at s max) */
+      const float Es = LOGTAB(BIN)
+          ? fmaf(L.K2, s2, fmaf(L.K1, s2 * rsqrtf(s2), L.K0)) : L.Emax;
+      unsigned sb = ftab_bin<false, LOGTAB(BIN)>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb, s2, Es, amb, L.fslog, L.fsamb);
+      if (!amb) {
+        if (sb == FCFCG_FTAB_BIN_MASK) return;
+        bin = (int) sb;
+      }
+    } else {
+      const float rs = rsqrtf(s2);
+      const float s = s2 * rs;
+      const float E = LINS(BIN) ? 0.f : fmaf(L.K2, s2, fmaf(L.K1, s, L.K0));
+      float mx = 0.f, my = 0.f, mz = 0.f;
+      if (GEOM == FCFCG_GEOM_SURVEY) {
+        /* line of sight m = x_a + x_b = 2 (l_b - D) + 2 c_A + d */
+        mx = fmaf(2.f, pb.x, c2x) + dx;
+        my = fmaf(2.f, pb.y, c2y) + dy;
+        mz = fmaf(2.f, pb.z, c2z) + dz;
+      }
+      if (IS_SMU(BIN)) {
+        float q;
+        if (GEOM == FCFCG_GEOM_BOX) {
+          q = L.fnmu * fabsf(dz) * rs;
+        } else {
+          const float dm = fmaf(dz, mz, fmaf(dy, my, dx * mx));
+          const float mm = fmaf(mz, mz, fmaf(my, my, mx * mx));
+          q = L.fnmu * fabsf(dm) * rsqrtf(mm * s2);
+        }
+        const float Eq = fmaf(L.Q1, rs, fmaf(L.Q2, q, L.Q0));
+        int qi = mu_bin(q, Eq, amb);
+        if (LINS(BIN)) {
+          const int k = lin_bin(L, s, amb);
+          if (!amb) {
+            if (qi >= L.nmu) {
+              if (!L.mu_one) return;
+              qi = L.nmu - 1;
+            }
+            if ((unsigned) k >= (unsigned) L.ns) return;
+            bin = k + qi * L.ns;
+          }
+        } else {
+          unsigned sb = ftab_bin<GEOM == FCFCG_GEOM_SURVEY, LOGTAB(BIN)>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb,
+                                                              s2, E, amb, L.fslog, L.fsamb);
+          if (!amb) {
+            if (qi >= L.nmu) {
+              if (!L.mu_one) return;
+              qi = L.nmu - 1;
+            }
+            if (sb == FCFCG_FTAB_BIN_MASK) return;
+            bin = (int) sb + qi * L.ns;
+          }
+        }
+      } else {
+        /* survey (s_perp, pi): pi^2 = (d.m)^2 / |m|^2 */
+        const float dm = fmaf(dz, mz, fmaf(dy, my, dx * mx));
+        const float mm = fmaf(mz, mz, fmaf(my, my, mx * mx));
+        const float pi2 = __fdividef(dm * dm, mm);
+        const float sp2 = s2 - pi2;
+        const float Ep = fmaf(L.P2, s2, fmaf(L.P1, s, L.P0));
+        unsigned pbn = ftab_bin<true, false>(fp, L.fpoff, L.nfp, L.fpinv, fpe, L.npb, pi2, Ep, amb, L.fplog, L.fpamb);
+        unsigned sb = ftab_bin<true, LOGTAB(BIN)>(fs, L.fsoff, L.nfs, L.fsinv, fse, L.nsb,
+                                     sp2 < 0.f ? 0.f : sp2, E + Ep, amb, L.fslog, L.fsamb);
+        if (!amb) {
+          if (sb == FCFCG_FTAB_BIN_MASK || pbn == FCFCG_FTAB_BIN_MASK) return;
+          bin = (int) sb + (int) pbn * L.ns;
+        }
+      }
+    }
+  }
+  const uint32_t ai = first + (uint32_t) i;
+  const uint32_t bj = __float_as_uint(pb.w);
+  if (amb) {
+    n_q++;
+    uint32_t code = 0;
+    if (GEOM == FCFCG_GEOM_BOX)
+      code = nb_code(BATCH ? ms->nc : L.ncell, cx, cy, cz,
+                     __ldg((const int4 *) L.sten + S.bt[src]));
+    if (ADJ) enqueue_adj(L, ai, bj, code, n_inline, n_in);
+    else enqueue<WT, BATCH>(L, ms, ai, bj, code, h, n_inline, n_in);
+    return;
+  }
+  n_in++;
+  if (ADJ) {
+    /* d/dw_a of w_a w_b g[bin] is w_b g[bin], and the other way round; the
+     * neighbour side is summed across the warp by the caller */
+    const double g = L.hist_smem ? ((const double *) h)[bin] : __ldg(L.gfix + bin);
+    adj_acc((uint32_t *) S.ga + i, (int *) S.ga + FCHUNK + i,
+            adj_term(S.wb[src], g), L.dA + ai, L.gunit);
+    gbv = adj_term(S.wa[i], g);
+    return;
+  }
+  long long w = 0;
+  if (WT) {
+    const int2 wa = S.aw[i];
+    const float4 bw = S.bw[src];
+    w = fix_prod(wa.x, __int_as_float(wa.y), pa.w, __float_as_int(bw.y), bw.z,
+                 bw.x);
+  }
+  hist_add<WT, BATCH>(L, ms, h, bin, w);
+}
+
+/* Is chunk point pa a candidate for the lane's neighbour (bx, by, bz):
+ * inside the outer range (and, for survey (s_perp, pi) counts, not beyond
+ * pi_max for sure by the line-of-sight prefilter (u, lh, lP))? */
+template <int GEOM, int BIN>
+__device__ __forceinline__ bool candidate(const fcfcg_launch &L, float4 pa,
+    float bx, float by, float bz, float ux, float uy, float uz, float lh,
+    float lP) {
+  const float dx = pa.x - bx, dy = pa.y - by, dz = pa.z - bz;
+  if (IS_SPI(BIN) && GEOM == FCFCG_GEOM_BOX) {
+    const float v = fmaf(dy, dy, dx * dx);
+    return (fabsf(dz) < L.p_lim) & (v < L.s_lim);
+  } else if (LOSCUT(GEOM, BIN)) {
+    const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    const float t = fmaf(dz, uz, fmaf(dy, uy, dx * ux));
+    return (v < L.s_lim) & (fabsf(t) < fmaf(v, lh, lP));
+  }
+  const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+  return v < L.s_lim;
+}
+
+/* Compare a neighbour point (one per lane) with chunk points [i0, i1):
+ * bit i - i0 of the result marks a candidate inside the outer range.  For
+ * survey (s_perp, pi) counts (u, lh, lP) is the lane's line-of-sight
+ * prefilter: a pair is dropped when |d.u| >= lP + lh s^2, where its pi
+ * exceeds pi_max for sure. */
+template <int GEOM, int BIN, bool LIMIT>
+__device__ __forceinline__ uint32_t scan_chunk_(const fcfcg_launch &L,
+    const float4 *a, int i0, int i1, int ilim, float bx, float by,
+    float bz, float ux, float uy, float uz, float lh, float lP) {
+  uint32_t msk = 0;
+  const float s_lim = L.s_lim, p_lim = L.p_lim;
+#pragma unroll 4
+  for (int i = i0; i < i1; i++) {
+    const float4 pa = a[i];
+    const float dx = pa.x - bx, dy = pa.y - by, dz = pa.z - bz;
+    bool inr;
+    if (IS_SPI(BIN) && GEOM == FCFCG_GEOM_BOX) {
+      const float v = fmaf(dy, dy, dx * dx);
+      inr = (fabsf(dz) < p_lim) & (v < s_lim);
+    } else if (LOSCUT(GEOM, BIN)) {
+      const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+      const float t = fmaf(dz, uz, fmaf(dy, uy, dx * ux));
+      inr = (v < s_lim) & (fabsf(t) < fmaf(v, lh, lP));
+    } else {
+      const float v = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+      inr = v < s_lim;
+    }
+    if (LIMIT) inr &= (i < ilim);
+    msk |= (uint32_t) inr << (i - i0);
+  }
+  return msk;
+}
+
+/* The i < ilim test only matters in the chunk's own cell (auto counts). */
+template <int GEOM, int BIN>
+__device__ __forceinline__ uint32_t scan_chunk(const fcfcg_launch &L,
+    const float4 *a, int i0, int i1, int ilim, float bx, float by,
+    float bz, float ux, float uy, float uz, float lh, float lP) {
+  if (__all_sync(FULLMASK, ilim >= i1))
+    return scan_chunk_<GEOM, BIN, false>(L, a, i0, i1, ilim, bx, by, bz, ux,
+                                         uy, uz, lh, lP);
+  return scan_chunk_<GEOM, BIN, true>(L, a, i0, i1, ilim, bx, by, bz, ux, uy,
+                                      uz, lh, lP);
+}
+
+/*
+ * FP32 counting kernel.  GEOM: box / survey; BIN: iso / smu / spi;
+ * WT: weighted.  Shared memory: FP32 tables, the histogram, the CTA's chunk
+ * and neighbour list, and per warp a block of neighbour points and a queue.
+ *
+ * A CTA holds one chunk (<= 64 points of a cell).  The non-empty neighbour
+ * cells of the stencil are laid end to end (a prefix sum per chunk); the
+ * warps take blocks of 32 consecutive neighbour points from a shared
+ * counter, and each lane compares its point with every chunk point
+ * (broadcast from shared
+ * memory), recording those inside the outer range as mask bits.  A block's
+ * in-range pairs are then compacted into the warp queue and binned 32 at a
+ * time, every lane busy.
+ */
+/* (s, mu) binning keeps more values live: 3 CTAs per SM (85 registers)
+ * measure faster there, 4 CTAs (64 registers) for the other binnings. */
+template <int GEOM, int BIN, int WT, int BATCH, int ADJ>
+__global__ void __launch_bounds__(CT32_THREADS, IS_SMU(BIN) ? 3 : 4)
+k_count32(const fcfcg_launch L) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint32_t sh_chunk;
+  __shared__ uint32_t sh_blk;   /* next neighbour block of the chunk */
+  __shared__ MockSh sh_mock;   /* batched launch: the current catalogue */
+  int cur = -1;
+  uint16_t *fs = (uint16_t *) smem;
+  uint16_t *fp = fs + L.nfs;
+  float *fse = (float *) (smem + (((size_t) (L.nfs + L.nfp) * 2 + 3) & ~(size_t) 3));
+  float *fpe = fse + L.nsb + 1;
+  size_t hoff = (size_t) ((unsigned char *) (fpe + (L.npb ? L.npb + 1 : 0)) - smem);
+  hoff = (hoff + 15) & ~(size_t) 15;
+  uint32_t *h = (uint32_t *) (smem + hoff);
+  size_t soff = hoff + (L.hist_smem ? (size_t) L.ntot * (WT ? 8 : 4) : 0);
+  soff = (soff + 15) & ~(size_t) 15;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Stage S;
+  {
+    unsigned char *b = smem + soff;
+    S.a = (float4 *) b;
+    b += (size_t) FCHUNK * 16;
+    S.aw = (int2 *) b;
+    b += WT ? (size_t) FCHUNK * 8 : 0;
+    S.pre = (uint32_t *) b;
+    b += (((size_t) L.nsten + 1) * 4 + 15) & ~(size_t) 15;
+    S.bst = (uint32_t *) b;
+    b += (((size_t) L.nsten) * 4 + 15) & ~(size_t) 15;
+    if (ADJ) {
+      S.ga = (unsigned long long *) b;
+      b += (size_t) FCHUNK * 8;
+      S.wa = (double *) b;
+      b += (size_t) FCHUNK * 8;
+    }
+    b += (size_t) warp * stage_warp_bytes(WT + ADJ);
+    S.b = (float4 *) b;
+    b += 32 * 16;
+    S.bw = (float4 *) b;
+    b += WT ? 32 * 16 : 0;
+    S.bt = (uint16_t *) b;
+    b += 32 * 2;
+    S.q = (uint16_t *) b;
+    if (ADJ) {
+      b += QCAP * 2;
+      S.gb = (long long *) b;
+      b += 32 * 8;
+      S.wb = (double *) b;
+    }
+  }
+  for (int i = threadIdx.x; i < L.nfs; i += blockDim.x) fs[i] = L.fs[i];
+  for (int i = threadIdx.x; i < L.nfp; i += blockDim.x) fp[i] = L.fp[i];
+  for (int i = threadIdx.x; i <= L.nsb; i += blockDim.x) fse[i] = L.fse[i];
+  if (L.npb)
+    for (int i = threadIdx.x; i <= L.npb; i += blockDim.x) fpe[i] = L.fpe[i];
+  if (ADJ) {
+    /* the cotangent of the counts takes the histogram's place */
+    if (L.hist_smem)
+      for (long i = threadIdx.x; i < L.ntot; i += blockDim.x)
+        ((double *) h)[i] = L.gfix[i];
+    for (int i = threadIdx.x; i < FCHUNK; i += blockDim.x) S.ga[i] = 0;
+    if (lane < 32) S.gb[lane] = 0;
+  } else if (L.hist_smem) {
+    for (long i = threadIdx.x; i < L.ntot * (WT ? 2 : 1); i += blockDim.x) h[i] = 0;
+  }
+
+  const float4 *__restrict__ Bl4 = (const float4 *) L.B.l4;
+  const int2 *__restrict__ Bwq = (const int2 *) L.B.wq;
+  const int4 *__restrict__ sten = (const int4 *) L.sten;
+  const float4 *__restrict__ stD = (const float4 *) L.stenD;
+  unsigned long long n_cand = 0, n_in64 = 0, n_q64 = 0, n_inline = 0;
+  const uint32_t nchunk = L.nchunk_dev ? __ldg(L.nchunk_dev) : L.nchunk;
+
+  for (;;) {
+    __syncthreads();    /* the previous chunk is done with a / pre / bst */
+    if (threadIdx.x == 0) {
+      sh_chunk = atomicAdd(L.chunk_head, 1u);
+      sh_blk = 0;
+    }
+    __syncthreads();
+    const uint32_t c = sh_chunk;
+    if (c >= nchunk) break;
+    const uint4 ch = __ldg(((const uint4 *) L.chunks) + c);
+    int ncl[3] = {L.ncell[0], L.ncell[1], L.ncell[2]};
+    uint32_t cbase = 0;
+    if (BATCH) {
+      /* chunks come in catalogue order: on a change of catalogue, hand the
+       * shared histogram to the previous one's global histogram */
+      const int mk = (int) ch.w;
+      if (mk != cur) {
+        if (cur >= 0 && L.hist_smem) hist_flush<WT>(L, h, sh_mock.g);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          const fcfcg_mock *M = L.mocks + mk;
+          for (int k = 0; k < 3; k++) {
+            sh_mock.nc[k] = M->ncell[k];
+            const float f = (float) M->cw[k];
+            sh_mock.cwf[k] = f;
+            sh_mock.cwl[k] = (float) (M->cw[k] - (double) f);
+            sh_mock.box[k] = M->box[k];
+          }
+          sh_mock.base = M->cell_base;
+          sh_mock.g = WT ? M->gwt : M->gcnt;
+          sh_mock.id = (uint32_t) mk;
+        }
+        __syncthreads();
+        cur = mk;
+      }
+      ncl[0] = sh_mock.nc[0];
+      ncl[1] = sh_mock.nc[1];
+      ncl[2] = sh_mock.nc[2];
+      cbase = sh_mock.base;
+    }
+    const uint32_t cell = ch.x, first = ch.y;
+    const uint32_t lcell = cell - cbase;
+    const int m = (int) ch.z;
+    const int cx = (int) (lcell % (uint32_t) ncl[0]);
+    const int cy = (int) ((lcell / (uint32_t) ncl[0]) % (uint32_t) ncl[1]);
+    const int cz = (int) (lcell / ((uint32_t) ncl[0] * (uint32_t) ncl[1]));
+    const int aoff = (int) (first - __ldg(L.A.cstart + cell));
+    float c2x = 0.f, c2y = 0.f, c2z = 0.f;
+    if (GEOM == FCFCG_GEOM_SURVEY) {
+      c2x = 2.f * fmaf((float) cx + 0.5f, L.cwf[0], L.lof[0]);
+      c2y = 2.f * fmaf((float) cy + 0.5f, L.cwf[1], L.lof[1]);
+      c2z = 2.f * fmaf((float) cz + 0.5f, L.cwf[2], L.lof[2]);
+    }
+    if (warp == 1) {
+      for (int k = lane; k < m; k += 32) {
+        S.a[k] = ((const float4 *) L.A.l4)[first + k];
+        if (WT) S.aw[k] = ((const int2 *) L.A.wq)[first + k];
+        if (ADJ) S.wa[k] = L.A.w[first + k];
+      }
+    } else if (warp == 0) {
+      /* neighbour cells of this chunk, laid end to end */
+      uint32_t run = 0;
+      for (int t0 = 0; t0 < L.nsten; t0 += 32) {
+        const int t = t0 + lane;
+        uint32_t nb = 0, bs = 0;
+        if (t < L.nsten) {
+          const int4 o = __ldg(sten + t);
+          int q[3] = {cx + o.x, cy + o.y, cz + o.z};
+          bool ok = true;
+          for (int k = 0; k < 3; k++) {
+            const int n = ncl[k];
+            if (GEOM == FCFCG_GEOM_SURVEY) {
+              ok &= (q[k] >= 0) & (q[k] < n);
+            } else {
+              while (q[k] < 0) q[k] += n;
+              while (q[k] >= n) q[k] -= n;
+            }
+          }
+          if (ok) {
+            const uint32_t cb = cbase +
+                ((uint32_t) q[2] * ncl[1] + q[1]) * ncl[0] + q[0];
+            bs = __ldg(L.B.cstart + cb);
+            nb = __ldg(L.B.cstart + cb + 1) - bs;
+          }
+        }
+        uint32_t inc = nb;
+        for (int s = 1; s < 32; s <<= 1) {
+          uint32_t u = __shfl_up_sync(FULLMASK, inc, s);
+          if (lane >= s) inc += u;
+        }
+        if (t < L.nsten) {
+          S.pre[t] = run + inc - nb;
+          S.bst[t] = bs;
+        }
+        run += __shfl_sync(FULLMASK, inc, 31);
+      }
+      if (lane == 0) S.pre[L.nsten] = run;
+    }
+    __syncthreads();
+    const uint32_t total = S.pre[L.nsten];
+    /* neighbour positions [0, pin): cells whose pairs with the chunk's cell
+     * all lie within the outer range (their stencil entries come first) */
+    const uint32_t pin = S.pre[L.nin];
+    if (warp == 0 && lane == 0) n_cand += (unsigned long long) m * total;
+    uint32_t n_in = 0, n_q = 0;
+
+    /* the warps take the chunk's blocks of 32 neighbour points as they
+     * become free (their work varies), so they reach the next chunk's
+     * barrier together */
+    for (;;) {
+      uint32_t blk = 0;
+      if (lane == 0) blk = atomicAdd(&sh_blk, 1u);
+      const uint32_t base = __shfl_sync(FULLMASK, blk, 0) * 32u;
+      if (base >= total) break;
+      const uint32_t p = base + (uint32_t) lane;
+      float bx = 0.f, by = 0.f, bz = 0.f;
+      float ux = 0.f, uy = 0.f, uz = 0.f, lh = 0.f, lP = 0.f;
+      int ilim = 0;
+      uint32_t bjl = 0;
+      if (p < total) {
+        /* neighbour cell of position p: last t with pre[t] <= p */
+        int lo = 0, hi = L.nsten;
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (S.pre[mid] <= p) lo = mid;
+          else hi = mid;
+        }
+        const int t = lo;
+        const uint32_t jc = p - S.pre[t];
+        const uint32_t bj = S.bst[t] + jc;
+        const float4 pb = Bl4[bj];
+        float4 D;
+        if (BATCH) {
+          /* -offset * cell width of this catalogue, rounded once: the width
+           * is held as a float plus its float residual, and the fused
+           * multiply-add rounds (-o) (cwf + cwl) a single time, as the
+           * single-catalogue stencil table is rounded (no FP64 needed) */
+          const int4 o = __ldg(sten + t);
+          const float ox = (float) (-o.x), oy = (float) (-o.y),
+                      oz = (float) (-o.z);
+          D = make_float4(
+              __fmaf_rn(ox, sh_mock.cwf[0], __fmul_rn(ox, sh_mock.cwl[0])),
+              __fmaf_rn(oy, sh_mock.cwf[1], __fmul_rn(oy, sh_mock.cwl[1])),
+              __fmaf_rn(oz, sh_mock.cwf[2], __fmul_rn(oz, sh_mock.cwl[2])),
+              0.f);
+        } else {
+          D = __ldg(stD + t);
+        }
+        bx = pb.x - D.x;
+        by = pb.y - D.y;
+        bz = pb.z - D.z;
+        if (LOSCUT(GEOM, BIN)) {
+          /* x_b = (bx, by, bz) + c_A: its direction and 1 / |x_b| */
+          const float xx = fmaf(0.5f, c2x, bx), xy = fmaf(0.5f, c2y, by),
+                      xz = fmaf(0.5f, c2z, bz);
+          const float r2 = fmaf(xz, xz, fmaf(xy, xy, xx * xx));
+          if (r2 > L.los_r2min) {
+            const float ir = rsqrtf(r2);
+            ux = xx * ir;
+            uy = xy * ir;
+            uz = xz * ir;
+            lh = L.los_h * ir;
+            lP = fmaf(L.los_pr, ir, L.los_p);
+          } else {
+            lP = FLT_MAX;   /* near the observer: no prefilter */
+          }
+        }
+        ilim = m;
+        if (L.isauto && t == L.tzero) ilim = min(m, (int) jc - aoff);
+        S.b[lane] = make_float4(bx, by, bz, __uint_as_float(bj));
+        S.bt[lane] = (uint16_t) t;
+        bjl = bj;
+        if (ADJ) S.wb[lane] = L.B.w[bj];
+        if (WT) {
+          const int2 wq = Bwq[bj];
+          S.bw[lane] = make_float4(pb.w, __int_as_float(wq.x),
+                                   __int_as_float(wq.y), 0.f);
+        }
+      }
+      if (!ADJ) {
+        /*
+         * The block's candidates go to the warp's queue chunk point by chunk
+         * point (entry i | lane << 6), compacted by one ballot per chunk
+         * point, and are binned 32 at a time with every lane busy: when the
+         * next chunk point could overflow the queue, and at the end of the
+         * block.  A block wholly in cells within range of the chunk's cell
+         * (every pair a candidate) skips the test and the queue: pass k bins
+         * chunk point k against every lane's neighbour.
+         */
+        const bool all_lim = __all_sync(FULLMASK, ilim >= m);
+        const bool direct = !LOSCUT(GEOM, BIN) && all_lim && base + 32u <= pin;
+        const uint32_t lt = (1u << lane) - 1u;
+        uint32_t nq = direct ? (uint32_t) m * 32u : 0u;
+        int i = direct ? m : 0;
+        for (;;) {
+          /* scan from chunk point i until the next one could overflow the
+           * queue (the binning below is the only copy of that code) */
+          if (all_lim) {
+#pragma unroll 2
+            for (; i < m && nq <= QCAP - 32u; i++) {
+              const bool inr = candidate<GEOM, BIN>(L, S.a[i], bx, by, bz, ux,
+                                                    uy, uz, lh, lP);
+              const uint32_t bal = __ballot_sync(FULLMASK, inr);
+              if (inr) S.q[nq + __popc(bal & lt)] = (uint16_t) (i | (lane << 6));
+              nq += __popc(bal);
+            }
+          } else {
+            /* the chunk's own cell in an auto count (j > i only), or lanes
+             * past the end of the neighbour list (ilim 0) */
+            for (; i < m && nq <= QCAP - 32u; i++) {
+              const bool inr = (i < ilim) &&
+                  candidate<GEOM, BIN>(L, S.a[i], bx, by, bz, ux, uy, uz, lh,
+                                       lP);
+              const uint32_t bal = __ballot_sync(FULLMASK, inr);
+              if (inr) S.q[nq + __popc(bal & lt)] = (uint16_t) (i | (lane << 6));
+              nq += __popc(bal);
+            }
+          }
+          __syncwarp();
+          const uint32_t np = (nq + 31) >> 5;
+          for (uint32_t k = 0; k < np; k++) {
+            const uint32_t e = k * 32u + (uint32_t) lane;
+            long long gbv = 0;
+            if (e < nq) {
+              const uint32_t ent = direct ? (k | ((uint32_t) lane << 6))
+                                          : (uint32_t) S.q[e];
+              bin_pair<GEOM, BIN, WT, BATCH, ADJ>(L, &sh_mock, S, ent, first,
+                                                  cx, cy, cz, c2x, c2y, c2z,
+                                                  fs, fp, fse, fpe, h, n_in,
+                                                  n_q, n_inline, gbv);
+            }
+          }
+          __syncwarp();
+          nq = 0;
+          if (i >= m) break;
+        }
+        continue;
+      }
+      /* compare with every chunk point (two 32-point halves); in weighted
+       * counts a block wholly in cells within range takes every chunk point
+       * (below ilim) without a test -- the binning checks each pair anyway
+       * (measured: 1-2 % faster weighted; the unweighted kernel's code runs
+       * 6 % slower with the branch, so it keeps the test) */
+      uint32_t m0, m1;
+      if (WT && !LOSCUT(GEOM, BIN) && base + 32u <= pin) {
+        const int lim = min(ilim, m);
+        m0 = (lim <= 0) ? 0u : (lim >= 32 ? ~0u : (1u << lim) - 1u);
+        m1 = (lim <= 32) ? 0u
+                         : (lim >= 64 ? ~0u : (1u << (lim - 32)) - 1u);
+      } else {
+        m0 = scan_chunk<GEOM, BIN>(L, S.a, 0, min(m, 32), ilim, bx, by, bz,
+                                   ux, uy, uz, lh, lP);
+        m1 = (m > 32) ? scan_chunk<GEOM, BIN>(L, S.a, 32, m, ilim, bx, by,
+                                              bz, ux, uy, uz, lh, lP)
+                      : 0u;
+      }
+      /* compact the block's in-range pairs into the queue, QCAP per round */
+      const uint32_t cnt = __popc(m0) + __popc(m1);
+      uint32_t inc = cnt;
+      for (int s = 1; s < 32; s <<= 1) {
+        uint32_t u = __shfl_up_sync(FULLMASK, inc, s);
+        if (lane >= s) inc += u;
+      }
+      const uint32_t tot = __shfl_sync(FULLMASK, inc, 31);
+      const uint32_t excl = inc - cnt;
+      for (uint32_t r0 = 0; r0 < tot; r0 += QCAP) {
+        /* this lane's entries with positions in [r0, r0 + QCAP) */
+        uint32_t lo = excl > r0 ? excl : r0;
+        uint32_t hi = excl + cnt < r0 + QCAP ? excl + cnt : r0 + QCAP;
+        if (lo < hi) {
+          uint32_t b0 = m0, b1 = m1;
+          for (uint32_t sk = lo - excl; sk > 0; sk--) {
+            if (b0) b0 &= b0 - 1;
+            else b1 &= b1 - 1;
+          }
+          for (uint32_t pos = lo; pos < hi; pos++) {
+            uint32_t i;
+            if (b0) {
+              i = (uint32_t) (__ffs(b0) - 1);
+              b0 &= b0 - 1;
+            } else {
+              i = 32u + (uint32_t) (__ffs(b1) - 1);
+              b1 &= b1 - 1;
+            }
+            S.q[pos - r0] = (uint16_t) (i | ((uint32_t) lane << 6));
+          }
+        }
+        __syncwarp();
+        const uint32_t nr = (tot - r0 < QCAP) ? tot - r0 : QCAP;
+        /* pass k: lane l takes entry 32 k + l */
+        const uint32_t np = (nr + 31) >> 5;
+        for (uint32_t k = 0; k < np; k++) {
+          const uint32_t e = k * 32u + (uint32_t) lane;
+          long long gbv = 0;
+          int key = -1;
+          if (e < nr) {
+            const uint32_t ent = S.q[e];
+            key = (int) (ent >> 6);
+            bin_pair<GEOM, BIN, WT, BATCH, ADJ>(L, &sh_mock, S, ent, first,
+                                                cx, cy, cz, c2x, c2y, c2z, fs,
+                                                fp, fse, fpe, h, n_in, n_q,
+                                                n_inline, gbv);
+          }
+          if (ADJ) {
+            /* the pass's entries run in neighbour order: sum each run of
+             * equal neighbours across the lanes (suffix sums within a run)
+             * and let the run's first lane add it -- the neighbour block is
+             * this warp's own, so no atomic is needed */
+            for (int o = 1; o < 32; o <<= 1) {
+              const long long t = __shfl_down_sync(FULLMASK, gbv, o);
+              const int k2 = __shfl_down_sync(FULLMASK, key, o);
+              if (lane + o < 32 && k2 == key) gbv += t;
+            }
+            const int kp = __shfl_up_sync(FULLMASK, key, 1);
+            if (key >= 0 && (lane == 0 || kp != key)) S.gb[key] += gbv;
+            __syncwarp();
+          }
+        }
+        __syncwarp();
+      }
+      if (ADJ) {
+        /* the block's neighbour points are done: their gradients out */
+        if (p < total) {
+          const long long v = S.gb[lane];
+          if (v != 0) atomicAdd(L.dB + bjl, (double) v * L.gunit);
+          S.gb[lane] = 0;
+        }
+        __syncwarp();
+      }
+    }
+    if (ADJ) {
+      /* the chunk is done: its points' gradients out */
+      __syncthreads();
+      uint32_t *glo = (uint32_t *) S.ga;
+      int *ghi = (int *) S.ga + FCHUNK;
+      for (int k = threadIdx.x; k < m; k += blockDim.x) {
+        const long long v = (long long) ghi[k] * 4294967296ll + glo[k];
+        if (v != 0) atomicAdd(L.dA + first + k, (double) v * L.gunit);
+        glo[k] = 0;
+        ghi[k] = 0;
+      }
+    }
+    n_in64 += n_in;
+    n_q64 += n_q;
+  }
+
+  /* statistics */
+  for (int o = 16; o > 0; o >>= 1) {
+    n_in64 += __shfl_xor_sync(FULLMASK, n_in64, o);
+    n_q64 += __shfl_xor_sync(FULLMASK, n_q64, o);
+    n_inline += __shfl_xor_sync(FULLMASK, n_inline, o);
+  }
+  if (lane == 0) {
+    if (warp == 0) atomicAdd(L.stats + 0, n_cand);
+    atomicAdd(L.stats + 1, n_in64);
+    atomicAdd(L.stats + 2, n_q64);
+    atomicAdd(L.stats + 3, n_inline);
+  }
+  __syncthreads();
+  if (!ADJ && L.hist_smem && (!BATCH || cur >= 0))
+    hist_flush<WT>(L, h, BATCH ? sh_mock.g : (WT ? L.gwt : L.gcnt));
+}
+
+#endif

@@ -59,6 +59,7 @@ struct fcfcg_ctx {
   uint32_t *d_head, *d_queue;      /* d_head: chunk counter, pad, fill */
   unsigned long long *d_qcount;    /* queue fill (64-bit), in d_head */
   size_t qcap, qcap_alloc;
+  int qcap_user;                  /* capacity set by fcfcg_set_queue_capacity */
   void *h_pinned;
   size_t h_pinned_cap;
   fcfcg_stats stats;
@@ -335,7 +336,29 @@ int fcfcg_set_cells_per_smax(fcfcg_ctx *c, int k) {
 int fcfcg_set_queue_capacity(fcfcg_ctx *c, size_t cap) {
   if (!c || c->host_only) return FCFCG_ERR_ARG;
   c->qcap = cap < c->qcap_alloc ? cap : c->qcap_alloc;
+  c->qcap_user = 1;
   return FCFCG_OK;
+}
+
+/* After a count whose ambiguous pairs overflowed the recheck queue (the
+ * overflow is binned inside the counting kernel, one lane at a time): grow
+ * the queue for the next counts to a power of two above `need`, at most
+ * 2^28 pairs (4 GiB).  Not once a capacity was set explicitly.  Called with
+ * the stream idle. */
+static void queue_grow(fcfcg_ctx *c, unsigned long long need) {
+  if (c->qcap_user || need <= c->qcap_alloc) return;
+  size_t cap = c->qcap_alloc;
+  while (cap < need && cap < ((size_t) 1 << 28)) cap <<= 1;
+  if (cap == c->qcap_alloc) return;
+  uint32_t *q = NULL;
+  if (cudaMalloc((void **) &q, sizeof(uint32_t) * 4 * cap) != cudaSuccess) {
+    cudaGetLastError();         /* keep the present queue */
+    return;
+  }
+  cudaFree(c->d_queue);
+  c->d_queue = q;
+  c->qcap = c->qcap_alloc = cap;
+  c->bufgen++;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -909,6 +932,55 @@ static int fp32_bounds(const fcfcg_ctx *c, const grid_t *g, double dmax,
   double tiny = 1e6 * L->K0 * (nmu > 1 ? nmu : 1);
   if (tiny < 1e-20) tiny = 1e-20;
   L->tiny = (float) tiny;
+  /*
+   * Linear s bins as FCFC's integer table sees them: rescaled edges
+   * e_k = a + k d with integers a >= 0, d >= 1, so that the table's edges
+   * e_k^2 are integers and FCFC's bin is the k with e_k <= sqrt(s2_ref) <
+   * e_k+1.  The kernel then bins s itself: k = floor(t), t = (s - a) / d.
+   * Window of t, for a pair with s^2 >= tiny (smaller ones are rechecked):
+   *   |s_32 - sqrt(s2_ref)| <= eta s_32 (1 + 2 eta) + E(s) / sqrt(s2_32),
+   *   with eta = 2^-22 + 2^-24 (s_32 = fl(s2 rsqrtf(s2)): rsqrtf within 2
+   *   ulp, CUDA's documented bound, then the product's rounding), E(s) =
+   *   K2 s^2 + K1 s + K0 the bound on |s2_32 - s2_ref| above, and
+   *   sqrt(s2_32) >= s_32 / (1 + eta), K0 / s <= K0 / sqrt(tiny);
+   *   t = fl(fma(s, fl(1 / d), fl(-a / d))) adds u (s + a) / d + u |t|,
+   *   |t| <= ns + 1 where the window matters; fr = t - floor(t) adds u
+   *   (t < 0), and the tests fr < W and fr + W > 1 another u each.  The
+   *   factor 1.01 covers W's own FP32 evaluation.
+   */
+  L->slin = 0;
+  if (b->bintype != FCFCG_BIN_SPI && b->s.tabtype == FCFCG_TAB_INT &&
+      b->s.nbin >= 1) {
+    int ok = 1;
+    double a = 0, d = 0;
+    for (int k = 0; k <= b->s.nbin && ok; k++) {
+      const double e = sqrt(b->s.edge[k]);
+      if (!(e == floor(e) && e * e == b->s.edge[k] && e < 1e6)) ok = 0;
+      else if (k == 0) a = e;
+      else if (k == 1) d = e - a;
+      else if (e != a + k * d) ok = 0;
+    }
+    if (ok && d >= 1) {
+      const double eta = ldexp(1.0, -22) + ldexp(1.0, -24);
+      const double uu = ldexp(1.0, -24);
+      const double A = 1.01 * (eta * (1 + 2 * eta) + (double) L->K2 * (1 + eta)
+                               + uu) / d;
+      const double Bw = 1.01 * (((double) L->K1 + (double) L->K0 /
+                                 sqrt((double) L->tiny)) * (1 + eta) / d +
+                                uu * a / d + uu * (b->s.nbin + 1) + 3 * uu);
+      const double smax = a + d * b->s.nbin;
+      if (A * (smax + d) + Bw < 0.45) {
+        L->slin = 1;
+        L->lin_inv = (float) (1.0 / d);
+        L->lin_off = (float) (-a / d);
+        L->lin_A = (float) A;
+        if ((double) L->lin_A < A) L->lin_A = nextafterf(L->lin_A, INFINITY);
+        L->lin_B = (float) Bw;
+        if ((double) L->lin_B < Bw) L->lin_B = nextafterf(L->lin_B, INFINITY);
+        L->lin_k0 = b->s.min0 ? 0 : -1;
+      }
+    }
+  }
   /* worst windows at the top of the ranges */
   double smax2 = b->s.vmax;
   double Es = L->K2 * smax2 + L->K1 * sqrt(smax2) + L->K0;
@@ -1436,6 +1508,7 @@ static int count_impl(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
   } else {
     count_finish(c, &P, hres, hstats, icnt, wcnt);
   }
+  if (hstats[3]) queue_grow(c, hstats[2] + hstats[2] / 4);
   fcfcg_stats *o = &c->stats;
   float ms = 0;
   cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
@@ -2308,6 +2381,7 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
     o->nchunks = nchunk;
     o->precision_used = prec;
     o->launches = c->launches;
+    if (hstats[3]) queue_grow(c, hstats[2] + hstats[2] / 4);
   }
   free(wexp);
 out:

@@ -135,6 +135,11 @@ typedef struct {
    * is skipped for |x_b|^2 <= los_r2min */
   float los_p, los_pr, los_h, los_r2min;
   float K0, K1, K2;            /* E(s^2) = K2 s^2 + K1 s + K0 */
+  /* linear s bins (slin): t = s lin_inv + lin_off, bin floor(t), window
+   * lin_A s + lin_B in units of t; lin_k0: bins above it have a lower edge
+   * that is a boundary */
+  int slin, lin_k0;
+  float lin_inv, lin_off, lin_A, lin_B;
   float P0, P1, P2;            /* E(pi) (box) or E(pi^2) (survey) */
   float Q0, Q1, Q2;            /* E(q), q = nmu mu: Q1 / s + Q2 q + Q0 */
   float tiny;                  /* s^2 below: always recheck */
