@@ -109,6 +109,7 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
         } else {
           const float dm = fmaf(dz, mz, fmaf(dy, my, dx * mx));
           const float mm = fmaf(mz, mz, fmaf(my, my, mx * mx));
+          amb |= !(mm >= L.m2min);
           q = L.fnmu * fabsf(dm) * rsqrtf(mm * s2);
         }
         const float Eq = fmaf(L.Q1, rs, fmaf(L.Q2, q, L.Q0));
@@ -139,6 +140,7 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
         /* survey (s_perp, pi): pi^2 = (d.m)^2 / |m|^2 */
         const float dm = fmaf(dz, mz, fmaf(dy, my, dx * mx));
         const float mm = fmaf(mz, mz, fmaf(my, my, mx * mx));
+        amb |= !(mm >= L.m2min);
         const float pi2 = __fdividef(dm * dm, mm);
         const float sp2 = s2 - pi2;
         const float Ep = fmaf(L.P2, s2, fmaf(L.P1, s, L.P0));
@@ -387,9 +389,11 @@ k_count32(const fcfcg_launch L) {
     const int aoff = (int) (first - __ldg(L.A.cstart + cell));
     float c2x = 0.f, c2y = 0.f, c2z = 0.f;
     if (GEOM == FCFCG_GEOM_SURVEY) {
-      c2x = 2.f * fmaf((float) cx + 0.5f, L.cwf[0], L.lof[0]);
-      c2y = 2.f * fmaf((float) cy + 0.5f, L.cwf[1], L.lof[1]);
-      c2z = 2.f * fmaf((float) cz + 0.5f, L.cwf[2], L.lof[2]);
+      /* twice the chunk cell's centre: the FP64 centre the local
+       * coordinates are relative to, rounded once */
+      c2x = (float) (2.0 * (L.lo[0] + ((double) cx + 0.5) * L.cw[0]));
+      c2y = (float) (2.0 * (L.lo[1] + ((double) cy + 0.5) * L.cw[1]));
+      c2z = (float) (2.0 * (L.lo[2] + ((double) cz + 0.5) * L.cw[2]));
     }
     if (warp == 1) {
       for (int k = lane; k < m; k += 32) {

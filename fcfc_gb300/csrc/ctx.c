@@ -896,40 +896,119 @@ static double ftab_cell_value(long c, int sh) {
 
 /* Rounding bounds of the FP32 path; returns 0 when the FP32 windows stay
  * below half a table unit, i.e. the FP32 path applies. */
+/*
+ * Error windows of the FP32 kernels (every constant below is derived here;
+ * the kernels' arithmetic is in count32.cuh bin_pair / lin_bin / mu_bin /
+ * ftab_bin).  u = 2^-24, v = 2^-53; CUDA's documented maximum errors:
+ * rsqrtf 2 ulp (relative <= 2^-22), __fdividef 2 ulp for divisors in
+ * [2^-126, 2^126]; every other FP32 operation is correctly rounded.
+ *
+ * 1. One separation component.  The reference forms dx_ref = fl(X_a (+
+ *    shift) - X_b) from FP64 rescaled coordinates X.  The kernel forms
+ *    dx = fl32(l_a - fl32(l_b - D)): l = fl32(fl64(X - c)) is a point's
+ *    offset from its FP64 cell centre c (|X - c| <= hw), D = fl32(-o cw)
+ *    the cell displacement (|D| <= dmax).  Roundings: l_a, l_b (u hw each),
+ *    D (u dmax), l_b - D (u (hw + dmax)), the difference (u |dx| <= u R);
+ *    FP64 terms: the centres (3 v |c| each), the box side against n cw
+ *    (v L), the reference's own two roundings (v (xabs + L + R)).  So
+ *      |dx - dx_ref| <= dc = 1.25 [u (3 hw + 2 dmax + R) + 10 v (xabs + R)].
+ * 2. s^2 (and s_perp^2).  The kernel's fma chain is within 3u (2u) of the
+ *    exact sum of its squared components; the reference's within 3v of its
+ *    own; the components differ by <= dc each, so the exact sums differ by
+ *    <= 2 sqrt(3) dc s + 3 dc^2 (Cauchy-Schwarz).  Survey pairs add the
+ *    reference's S - t rounding: s_i (3v |x|^2), S (2v sabs), t (6v sabs),
+ *    S - t exact (Sterbenz) or v s^2: <= 14 v sabs, carried as refs2 =
+ *    64 v sabs.  Hence |s2 - s2_ref| <= E = K2' s^2 + K1 s + K0' with
+ *      K2' = 3.0002 u + 3.0001 v   (taken as 4 u),
+ *      K1  = 1.1 * 2 sqrt(3) dc    (2 sqrt(2) for s_perp^2; the 1.1 covers
+ *            E's own FP32 evaluation and s = s2 rsqrtf(s2) against the
+ *            exact root),
+ *      K0' = 4 dc^2 + refs2.
+ *    The kernel's table lookup of an FP32 value adds the rounding of its
+ *    cell position, fl(v / w) (u v), and of 1 - fr against the window
+ *    (u w / 2): the table windows use K2 = K2' + u, K0 = K0' + u w.
+ * 3. mu in a box: FCFC's bin is floor(sqrt(Q)), Q = fl(fl(dz^2 / s^2)
+ *    nmu^2) (the (int) cut and the mu table reduce to that); sqrt(Q) is
+ *    within 1.5 v of nmu |dz_ref| / sqrt(s2_ref).  The kernel's q =
+ *    fl(fl(nmu |dz|) rsqrtf(s2)) is within 3 2^-23 q (rsqrtf and two
+ *    products) of nmu |dz| / sqrt(s2); |dz - dz_ref| <= dc contributes
+ *    nmu dc / s, the root of s2 against s2_ref contributes q E / (2 s^2) =
+ *    q (K2'/2 + K1 / (2 s) + K0' / (2 s^2)), q <= nmu.  So
+ *      Eq = Q1 / s + Q2 q + Q0, Q1 = 1.25 nmu (dc + K1 / 2),
+ *      Q2 = 1.25 (K2' / 2 + 2^-21 + 2 v), Q0 = 1e-6,
+ *    the last covering nmu K0' / (2 s^2) <= 5e-7 (pairs with s^2 < tiny =
+ *    1e6 K0' nmu are rechecked whatever their value) and the rounding of
+ *    1 - Eq.
+ * 4. Survey mu and pi^2 use the line of sight m = x_a + x_b.  The kernel
+ *    forms m = fl(fl(2 b + c2) + d) with b the neighbour's offset from the
+ *    chunk cell's centre c and c2 = fl32(2 c) (the centre in FP64, rounded
+ *    once): per component |dm| <= 3 dc + 2u |c| + u (|m| + s) + u |m|,
+ *    and with |x_a| <= (|m| + s) / 2, |c| <= |x_a| + hw:
+ *      |dm| / |m| <= dmr = sqrt(3) (3 dc + 2 u (hw + R)) / |m| +
+ *                         3.0001 sqrt(3) u,
+ *    bounded by requiring |m| >= 2 R (pairs with |m|^2 < m2min = (2.01
+ *    R)^2, i.e. next to the observer, are rechecked).  The direction m/|m|
+ *    moves by <= 2 dmr.  The reference's dd = s1 - s2 = d.m carries
+ *    6 v sabs, its S + t = |m|^2 carries 8 v sabs.
+ *    mu: q = nmu |d.m| / (|m| s): d contributes nmu sqrt(3) dc / s (the
+ *    length of d is E's business), m 2 nmu dmr, the kernel's roundings
+ *    (dm 3u absolute, mm, the product, rsqrtf, two products: 8u relative)
+ *    and the reference's (6 v nmu sabs / (2 R s), 4 v sabs / |m|^2):
+ *      Q1 = 1.25 nmu (sqrt(3) dc + K1 / 2 + 3 v sabs / R),
+ *      Q2 = 1.25 (K2' / 2 + 8 u + v sabs / R^2 + 2 v),
+ *      Q0 = 1.25 nmu (3 u + 2 dmr) + 1e-6.
+ *    pi^2 = (d.m)^2 / |m|^2: |d pi| <= sqrt(3) dc + s (2 dmr + 3u), so
+ *      Ep = P2 s^2 + P1 s + P0, P1 = 1.25 (2 sqrt(3) dc + 6 v sabs / R),
+ *      P2 = 1.25 (4 dmr + 14 u + 2 v sabs / R^2 + 2 v + u) (dm^2, mm and
+ *      __fdividef: 8u relative; the table position: u),
+ *      P0 = 1.25 (6 dc^2 + u w_pi) + 1e-12.
+ *    s_perp^2 = s^2 - pi^2 takes E + Ep.
+ * 5. pi in a box is |dz|: P0 = 1.25 (dc + u w_pi).
+ * Every constant carries a factor >= 1.1 over its derived value; the
+ * near-edge tests place pairs on every bin edge and check that each one is
+ * rechecked.
+ */
 static int fp32_bounds(const fcfcg_ctx *c, const grid_t *g, double dmax,
     const slot_t *A, const slot_t *B, fcfcg_launch *L) {
   const fcfcg_bins *b = &c->bins;
   const int box = (b->geometry == FCFCG_GEOM_BOX);
-  const double u = ldexp(1.0, -24);
+  const double u = ldexp(1.0, -24), v = ldexp(1.0, -53);
   double hw = 0;
   for (int d = 0; d < 3; d++) hw = fmax(hw, 0.5 * g->cw[d] * (1 + 1e-6));
   const double R = g->reach3 * 1.01;
   double xabs = fmax(A->xabs, B->xabs);
   double sabs = fmax(A->s2abs, B->s2abs);
   if (box) xabs = fmax(xabs, fmax(b->box[0], fmax(b->box[1], b->box[2])));
-  /* per-component error of an FP32 separation against the reference's FP64
-   * separation: rounding of both local coordinates, of D, of l_a + D, of the
-   * difference, and the reference's own FP64 rounding */
-  const double dc = 1.25 * u * (2 * hw + 2 * dmax + hw + R) +
-                    4 * ldexp(1.0, -53) * (2 * xabs + R) + 1e-12;
-  const double refs2 = box ? 0 : ldexp(1.0, -47) * sabs;
+  const double dc = 1.25 * (u * (3 * hw + 2 * dmax + R) + 10 * v * (xabs + R)) +
+                    1e-300;
+  const double refs2 = box ? 0 : 64 * v * sabs;
   const double s3 = sqrt(3.0);
-  L->K2 = (float) ldexp(1.0, -20);
-  L->K1 = (float) (1.1 * 2 * s3 * dc);
-  if (b->bintype == FCFCG_BIN_SPI && box) L->K1 = (float) (1.1 * 2 * sqrt(2.0) * dc);
-  L->K0 = (float) (4 * dc * dc + refs2 + 1e-30);
+  /* cell widths of the FP32 tables (uniform ones; 0 for bit patterns) */
+  const double ws = b->s.ftab && !b->s.flog ? ldexp(1.0, b->s.fshift) : 0;
+  const double wp = (b->bintype == FCFCG_BIN_SPI && b->p.ftab && !b->p.flog)
+                        ? ldexp(1.0, b->p.fshift) : 0;
+  const double K2a = 4 * u, K0a = 4 * dc * dc + refs2;   /* arithmetic */
+  const double K1 = 1.1 * 2 * ((b->bintype == FCFCG_BIN_SPI && box)
+                                   ? sqrt(2.0) : s3) * dc;
+  L->K2 = (float) (K2a + u);
+  L->K1 = (float) K1;
+  L->K0 = (float) (K0a + u * ws + 1e-30);
   double nmu = b->nmu;
   L->fnmu = (float) nmu;
+  /* survey: relative error of the line of sight for |m| >= 2 R */
+  const double dmr = s3 * (3 * dc + 2 * u * (hw + R)) / (2 * R) +
+                     3.0001 * s3 * u;
+  L->m2min = box ? 0.f : (float) (2.01 * R * 2.01 * R);
   if (box) {
-    L->Q1 = (float) (1.25 * nmu * (dc + 0.5 * L->K1));
-    L->Q2 = (float) (1.25 * (0.5 * L->K2 + ldexp(1.0, -21)));
+    L->Q1 = (float) (1.25 * nmu * (dc + 0.5 * K1));
+    L->Q2 = (float) (1.25 * (0.5 * K2a + ldexp(1.0, -21) + 2 * v));
     L->Q0 = 1e-6f;
   } else {
-    L->Q1 = (float) (1.25 * nmu * (s3 * dc + 0.5 * L->K1));
-    L->Q2 = (float) (1.25 * (0.5 * L->K2 + ldexp(1.0, -20)));
-    L->Q0 = (float) (1.25 * nmu * ldexp(1.0, -20) + 1e-6);
+    L->Q1 = (float) (1.25 * nmu * (s3 * dc + 0.5 * K1 + 3 * v * sabs / R));
+    L->Q2 = (float) (1.25 * (0.5 * K2a + 8 * u + v * sabs / (R * R) + 2 * v));
+    L->Q0 = (float) (1.25 * nmu * (3 * u + 2 * dmr) + 1e-6);
   }
-  double tiny = 1e6 * L->K0 * (nmu > 1 ? nmu : 1);
+  double tiny = 1e6 * K0a * (nmu > 1 ? nmu : 1);
   if (tiny < 1e-20) tiny = 1e-20;
   L->tiny = (float) tiny;
   /*
@@ -987,16 +1066,17 @@ static int fp32_bounds(const fcfcg_ctx *c, const grid_t *g, double dmax,
   double Ep = 0;
   if (b->bintype == FCFCG_BIN_SPI) {
     if (box) {
-      L->P0 = (float) (1.25 * dc);
+      L->P0 = (float) (1.25 * (dc + u * wp));
       L->P1 = L->P2 = 0;
       Ep = L->P0;
       L->p_lim = (float) (b->p.vmax + Ep + 1e-6 * (1 + b->p.vmax));
       L->s_lim = (float) (smax2 + Es + 1e-6 * (1 + smax2));
     } else {
       double r2 = b->s.vmax + b->p.vmax;
-      L->P0 = (float) (refs2 + 1e-12);
-      L->P1 = (float) (1.25 * 2 * s3 * dc);
-      L->P2 = (float) (1.25 * (ldexp(1.0, -19) + ldexp(1.0, -21)));
+      L->P0 = (float) (1.25 * (6 * dc * dc + u * wp) + 1e-12);
+      L->P1 = (float) (1.25 * (2 * s3 * dc + 6 * v * sabs / R));
+      L->P2 = (float) (1.25 * (4 * dmr + 15 * u + 2 * v * sabs / (R * R) +
+                               2 * v));
       Ep = L->P2 * r2 + L->P1 * sqrt(r2) + L->P0;
       Es = L->K2 * r2 + L->K1 * sqrt(r2) + L->K0 + Ep;
       L->s_lim = (float) (r2 + Es + 1e-6 * (1 + r2));

@@ -142,6 +142,8 @@ typedef struct {
   float lin_inv, lin_off, lin_A, lin_B;
   float P0, P1, P2;            /* E(pi) (box) or E(pi^2) (survey) */
   float Q0, Q1, Q2;            /* E(q), q = nmu mu: Q1 / s + Q2 q + Q0 */
+  float m2min;                 /* survey: |m|^2 below (next to the observer):
+                                  mu and pi^2 are rechecked */
   float tiny;                  /* s^2 below: always recheck */
   float Emax;                  /* E at the top of the s axis (iso, spi) */
   int tzero;                   /* stencil index of the zero offset */
