@@ -52,6 +52,17 @@ LOGBINS = np.geomspace(0.1, 100.0, 41)
 FLOPS_PER_PAIR = {"smu": 10, "spi": 8}   # algorithmic FP32 flops per pair
 
 
+def nvtx(name):
+    """An NVTX range (profilers can restrict a capture to it: the timed
+    steps are "timed", the all-FP64 passes "fp64")."""
+    import contextlib
+    try:
+        import torch
+        return torch.cuda.nvtx.range(name)
+    except Exception:
+        return contextlib.nullcontext()
+
+
 def env_rank():
     return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
             int(os.environ.get("LOCAL_RANK", 0)))
@@ -312,11 +323,21 @@ def mocks_cpu_sample(cats, boxes, subset, steps=1, warmup=0):
     return pairs / ms, pairs, ms, desc
 
 
+def kernel_source_sha256():
+    """sha256 over the FP32 count kernel's sources (count32.cuh, then
+    count_common.cuh): a committed ncu summary records the value it was
+    captured on."""
+    import hashlib
+    h = hashlib.sha256()
+    for f in ("count32.cuh", "count_common.cuh"):
+        h.update(open(os.path.join(ROOT, "fcfc_gb300", "csrc", f), "rb").read())
+    return h.hexdigest()
+
+
 def profile_info(name):
     """Figures of a committed ncu summary (``key: value`` lines) and whether
     it was captured on the current count kernel source (its recorded
-    sha256 of count.cu against the file's)."""
-    import hashlib
+    kernel_source_sha256 against the files')."""
     info = {}
     try:
         for line in open(os.path.join(ROOT, "profiles", name)):
@@ -325,9 +346,8 @@ def profile_info(name):
                 info[k.strip()] = v.strip()
     except OSError:
         return None
-    src = open(os.path.join(ROOT, "fcfc_gb300", "csrc", "count.cu"), "rb").read()
-    info["source_matches"] = (info.get("count_cu_sha256") ==
-                              hashlib.sha256(src).hexdigest())
+    info["source_matches"] = (info.get("kernel_source_sha256") ==
+                              kernel_source_sha256())
     return info
 
 
@@ -401,7 +421,8 @@ def run_mocks(args, rank, world, local, dist):
     tt, tk = 0.0, 0.0
     for _ in range(args.steps):
         flush.zero_()
-        ms, _ = timed(step)
+        with nvtx("timed"):
+            ms, _ = timed(step)
         tt += ms
         tk += pc.stats()["ms_count"]
     clocks = clk.stop()
@@ -411,7 +432,8 @@ def run_mocks(args, rank, world, local, dist):
     value = pairs * world / (ms_step * 1e-3)
     k_ms = tk / args.steps
     # the all-FP64 path on every accepted catalogue: same counts?
-    ms64, (c64, _, _) = timed(step, precision=fg.PREC_FP64)
+    with nvtx("fp64"):
+        ms64, (c64, _, _) = timed(step, precision=fg.PREC_FP64)
     exact = all(np.array_equal(c64[j], counts[j]) for j in accepted)
     # the CPU sample mocks on the GPU (one launch of just those catalogues)
     subset = accepted[::MOCK_CPU_STRIDE]
@@ -961,9 +983,10 @@ def main():
     for _ in range(args.steps):
         flush.zero_()
         torch.cuda.synchronize()
-        e0.record()
-        ms, res = step()
-        e1.record()
+        with nvtx("timed"):
+            e0.record()
+            ms, res = step()
+            e1.record()
         torch.cuda.synchronize()
         ms_tot += e0.elapsed_time(e1)
         ms_dev += ms
@@ -981,9 +1004,10 @@ def main():
 
     # all-FP64 GPU path, one step, timed the same way
     torch.cuda.synchronize()
-    e0.record()
-    step(prec=fg.PREC_FP64)
-    e1.record()
+    with nvtx("fp64"):
+        e0.record()
+        step(prec=fg.PREC_FP64)
+        e1.record()
     torch.cuda.synchronize()
     ms64 = e0.elapsed_time(e1)
     fp64_value = pairs_per_step / (ms64 * 1e-3)
