@@ -1075,7 +1075,13 @@ def main():
                      "kernel_ms": k1_ms,
                      "peak_source": "measured cuBLAS SGEMM (TF32 off) on this GPU",
                      "flops_per_pair": FLOPS_PER_PAIR["smu"],
-                     "issue": issue_bound(n_in[0] / (k1_ms * 1e-3), clocks)},
+                     "issue": issue_bound(n_in[0] / (k1_ms * 1e-3), clocks),
+                     "from_profile": {
+                         "file": "profiles/k_count32_box_smu_wt_ns_box.txt",
+                         "keys": ["traffic", "issue.warp_instructions_per_pair"],
+                         "captured_on_current_source": (profile_info(
+                             "k_count32_box_smu_wt_ns_box.txt") or {}).get(
+                                 "source_matches")}},
         "counters": {"candidates_smu": st1["candidates"],
                      "rechecked_smu": st1["rechecked"],
                      "candidates_spi": st2["candidates"],
