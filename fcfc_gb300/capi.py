@@ -95,7 +95,8 @@ class Stats(C.Structure):
                 ("ms_recheck", C.c_double), ("ms_total", C.c_double),
                 ("cells_per_smax", C.c_int), ("ncell", C.c_int * 3),
                 ("nstencil", C.c_int), ("nchunks", C.c_uint64),
-                ("precision_used", C.c_int), ("launches", C.c_uint64)]
+                ("precision_used", C.c_int), ("launches", C.c_uint64),
+                ("warp_queue", C.c_int)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_}
@@ -149,6 +150,7 @@ PROTOTYPES = {
     "fcfcg_graph_destroy": (None, [P]),
     "fcfcg_set_cells_per_smax": (C.c_int, [P, C.c_int]),
     "fcfcg_set_queue_capacity": (C.c_int, [P, C.c_size_t]),
+    "fcfcg_set_warp_queue": (C.c_int, [P, C.c_int]),
     "fcfcg_probe_smem_atomics": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     "fcfcg_autotune": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int,
                                  C.POINTER(C.c_int), C.POINTER(C.c_double)]),

@@ -145,15 +145,24 @@ static kfun_t pick64(int geom, int wt, int adj) {
 }
 
 extern "C" int fcfcg_k_count(void *stream, const fcfcg_launch *L,
-    int precision, int nsm, size_t *smem_used) {
+    int precision, int nsm, size_t *smem_used, uint32_t *qwarp_used) {
   kfun_t f;
   size_t smem;
   int threads;
+  fcfcg_launch Lq = *L;
+  cudaError_t e;
+  int per_sm = 0;
   if (precision == FCFCG_PREC_FP64) {
     f = pick64(L->geometry, L->withwt, L->adjoint);
     smem = (L->hist_smem && !L->adjoint)
                ? (size_t) L->ntot * (L->withwt ? 8 : 4) : 0;
     threads = CT_THREADS;
+    if (!f) return (int) cudaErrorInvalidValue;
+    if ((e = cudaFuncSetAttribute((const void *) f,
+             cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)) ||
+        (e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+             &per_sm, (const void *) f, threads, smem)))
+      return (int) e;
   } else {
     /* a bit-pattern s table selects the kernel's log variant */
     int bin = !L->fslog ? L->bintype
@@ -163,23 +172,45 @@ extern "C" int fcfcg_k_count(void *stream, const fcfcg_launch *L,
     if (L->slin && L->bintype == FCFCG_BIN_ISO) bin = BIN_ISOLIN;
     if (L->slin && L->bintype == FCFCG_BIN_SMU) bin = BIN_SMULIN;
     f = pick32(L->geometry, bin, L->withwt, L->mocks != NULL, L->adjoint);
+    if (!f) return (int) cudaErrorInvalidValue;
     size_t tab = fcfcg_k_count32_tab_bytes(L->nfs, L->nfp, L->nsb, L->npb);
-    smem = tab + (L->hist_smem ? (size_t) L->ntot * (L->withwt ? 8 : 4) : 0);
-    smem = ((smem + 15) & ~(size_t) 15) +
-           stage_bytes(L->nsten, L->withwt + L->adjoint);
+    size_t fixed = tab + (L->hist_smem ? (size_t) L->ntot * (L->withwt ? 8 : 4)
+                                        : 0);
+    fixed = (fixed + 15) & ~(size_t) 15;
     threads = CT32_THREADS;
+    /* the warp queue: as given, or the largest of 1024 / 512 / 256 entries
+     * that reaches the most CTAs per SM the kernel can hold (a smaller
+     * queue can free shared memory for another CTA) */
+    const uint32_t cand[3] = {QWARP_MAX, 512u, QWARP_MIN};
+    uint32_t q = 0;
+    int best = 0, occ[3] = {0, 0, 0};
+    for (int k = 0; k < 3; k++) {
+      if (L->qwarp && cand[k] != L->qwarp) continue;
+      const size_t sm = fixed + stage_bytes(L->nsten, L->withwt + L->adjoint,
+                                            cand[k]);
+      if ((e = cudaFuncSetAttribute((const void *) f,
+               cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm)))
+        return (int) e;
+      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+               &occ[k], (const void *) f, threads, sm)))
+        return (int) e;
+      if (occ[k] > best) best = occ[k];
+    }
+    for (int k = 0; k < 3 && !q; k++)
+      if ((!L->qwarp || cand[k] == L->qwarp) && occ[k] == best && best > 0)
+        q = cand[k];
+    if (!q) return (int) cudaErrorInvalidConfiguration;
+    smem = fixed + stage_bytes(L->nsten, L->withwt + L->adjoint, q);
+    Lq.qwarp = q;
+    if ((e = cudaFuncSetAttribute((const void *) f,
+             cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem)))
+      return (int) e;
+    per_sm = best;
+    if (qwarp_used) *qwarp_used = q;
   }
-  if (!f) return (int) cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute((const void *) f,
-      cudaFuncAttributeMaxDynamicSharedMemorySize, (int) smem);
-  if (e) return (int) e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *) f,
-                                                    threads, smem);
-  if (e) return (int) e;
   if (per_sm < 1) return (int) cudaErrorInvalidConfiguration;
   if (smem_used) *smem_used = smem;
-  f<<<nsm * per_sm, threads, smem, (cudaStream_t) stream>>>(*L);
+  f<<<nsm * per_sm, threads, smem, (cudaStream_t) stream>>>(Lq);
   return (int) cudaGetLastError();
 }
 
@@ -191,9 +222,10 @@ extern "C" size_t fcfcg_k_count32_tab_bytes(int nfs, int nfp, int nsb,
   return (n + 15) & ~(size_t) 15;
 }
 
-/* Shared memory the FP32 kernel needs beyond its histogram. */
+/* Shared memory the FP32 kernel needs beyond its histogram, with the
+ * smallest warp queue (whether the kernel fits at all). */
 extern "C" size_t fcfcg_k_count32_stage(int nsten, int withwt) {
-  return stage_bytes(nsten, withwt);
+  return stage_bytes(nsten, withwt, QWARP_MIN);
 }
 
 extern "C" int fcfcg_k_recheck(void *stream, const fcfcg_launch *L,

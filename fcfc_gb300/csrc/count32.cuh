@@ -302,7 +302,7 @@ k_count32(const fcfcg_launch L) {
       S.wa = (double *) b;
       b += (size_t) FCHUNK * 8;
     }
-    b += (size_t) warp * stage_warp_bytes(WT + ADJ);
+    b += (size_t) warp * stage_warp_bytes(WT + ADJ, L.qwarp);
     S.b = (float4 *) b;
     b += 32 * 16;
     S.bw = (float4 *) b;
@@ -311,7 +311,7 @@ k_count32(const fcfcg_launch L) {
     b += 32 * 2;
     S.q = (uint16_t *) b;
     if (ADJ) {
-      b += QCAP * 2;
+      b += (size_t) L.qwarp * 2;
       S.gb = (long long *) b;
       b += 32 * 8;
       S.wb = (double *) b;
@@ -541,7 +541,7 @@ k_count32(const fcfcg_launch L) {
            * queue (the binning below is the only copy of that code) */
           if (all_lim) {
 #pragma unroll 2
-            for (; i < m && nq <= QCAP - 32u; i++) {
+            for (; i < m && nq <= L.qwarp - 32u; i++) {
               const bool inr = candidate<GEOM, BIN>(L, S.a[i], bx, by, bz, ux,
                                                     uy, uz, lh, lP);
               const uint32_t bal = __ballot_sync(FULLMASK, inr);
@@ -551,7 +551,7 @@ k_count32(const fcfcg_launch L) {
           } else {
             /* the chunk's own cell in an auto count (j > i only), or lanes
              * past the end of the neighbour list (ilim 0) */
-            for (; i < m && nq <= QCAP - 32u; i++) {
+            for (; i < m && nq <= L.qwarp - 32u; i++) {
               const bool inr = (i < ilim) &&
                   candidate<GEOM, BIN>(L, S.a[i], bx, by, bz, ux, uy, uz, lh,
                                        lP);
@@ -598,7 +598,7 @@ k_count32(const fcfcg_launch L) {
                                               bz, ux, uy, uz, lh, lP)
                       : 0u;
       }
-      /* compact the block's in-range pairs into the queue, QCAP per round */
+      /* compact the block's in-range pairs into the queue, qwarp per round */
       const uint32_t cnt = __popc(m0) + __popc(m1);
       uint32_t inc = cnt;
       for (int s = 1; s < 32; s <<= 1) {
@@ -607,10 +607,10 @@ k_count32(const fcfcg_launch L) {
       }
       const uint32_t tot = __shfl_sync(FULLMASK, inc, 31);
       const uint32_t excl = inc - cnt;
-      for (uint32_t r0 = 0; r0 < tot; r0 += QCAP) {
-        /* this lane's entries with positions in [r0, r0 + QCAP) */
+      for (uint32_t r0 = 0; r0 < tot; r0 += L.qwarp) {
+        /* this lane's entries with positions in [r0, r0 + qwarp) */
         uint32_t lo = excl > r0 ? excl : r0;
-        uint32_t hi = excl + cnt < r0 + QCAP ? excl + cnt : r0 + QCAP;
+        uint32_t hi = excl + cnt < r0 + L.qwarp ? excl + cnt : r0 + L.qwarp;
         if (lo < hi) {
           uint32_t b0 = m0, b1 = m1;
           for (uint32_t sk = lo - excl; sk > 0; sk--) {
@@ -630,7 +630,7 @@ k_count32(const fcfcg_launch L) {
           }
         }
         __syncwarp();
-        const uint32_t nr = (tot - r0 < QCAP) ? tot - r0 : QCAP;
+        const uint32_t nr = (tot - r0 < L.qwarp) ? tot - r0 : L.qwarp;
         /* pass k: lane l takes entry 32 k + l */
         const uint32_t np = (nr + 31) >> 5;
         for (uint32_t k = 0; k < np; k++) {

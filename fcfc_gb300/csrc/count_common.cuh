@@ -543,7 +543,11 @@ __device__ __forceinline__ void hist_flush(const fcfcg_launch &L,
 
 #define CT32_THREADS 256
 #define FCHUNK 64                 /* chunk points a CTA holds (FP32 path) */
-#define QCAP 1024                 /* queued pairs per round */
+/* A warp's queue of candidates holds qwarp entries (a launch parameter:
+ * 256, 512 or 1024); a smaller queue frees shared memory for another CTA
+ * per SM or for L1. */
+#define QWARP_MAX 1024
+#define QWARP_MIN 256
 
 /* Shared memory of the FP32 kernel after the tables and the histogram.
  * Per CTA: the chunk points (and weights) and the neighbour list of the
@@ -557,7 +561,7 @@ struct Stage {
   float4 *b;        /* per warp, 32: neighbour (l_b - D) x y z, index */
   float4 *bw;       /* per warp, 32: weight, integer weight, remainder */
   uint16_t *bt;     /* per warp, 32: stencil entry */
-  uint16_t *q;      /* per warp, QCAP: queued pairs */
+  uint16_t *q;      /* per warp, qwarp: queued pairs */
   /* adjoint only: gradient sums in units of 2^-S, FP64 weights */
   unsigned long long *ga;   /* FCHUNK x 8 bytes: the 32-bit lo words of
                                the chunk points, then their hi words */
@@ -575,14 +579,16 @@ __host__ __device__ __forceinline__ size_t stage_cta_bytes(int nsten, int wt) {
   return n;
 }
 
-__host__ __device__ __forceinline__ size_t stage_warp_bytes(int wt) {
-  return 32 * 16 + (wt ? 32 * 16 : 0) + 32 * 2 + QCAP * 2 +
+__host__ __device__ __forceinline__ size_t stage_warp_bytes(int wt,
+    uint32_t qwarp) {
+  return 32 * 16 + (wt ? 32 * 16 : 0) + 32 * 2 + (size_t) qwarp * 2 +
          (wt == 2 ? 32 * 16 : 0);
 }
 
-__host__ __device__ __forceinline__ size_t stage_bytes(int nsten, int wt) {
+__host__ __device__ __forceinline__ size_t stage_bytes(int nsten, int wt,
+    uint32_t qwarp) {
   return stage_cta_bytes(nsten, wt) +
-         (size_t) (CT32_THREADS / 32) * stage_warp_bytes(wt);
+         (size_t) (CT32_THREADS / 32) * stage_warp_bytes(wt, qwarp);
 }
 
 typedef void (*kfun_t)(const fcfcg_launch);

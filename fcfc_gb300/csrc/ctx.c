@@ -70,6 +70,10 @@ struct fcfcg_ctx {
   /* autotuned grid refinement, keyed on the expected neighbours per object */
   int tuned_k;
   int tuned_key;
+  /* FP32 kernel's warp queue: forced (fcfcg_set_warp_queue), or autotuned
+   * for a key and weighting, else the launcher's choice; the last used */
+  uint32_t qwarp_force, tuned_q, last_qwarp;
+  int tuned_q_key, tuned_q_wt;
   /* RA/Dec/z conversion scratch */
   void *d_cnvt;
   size_t cnvt_cap;
@@ -330,6 +334,14 @@ int fcfcg_set_cells_per_smax(fcfcg_ctx *c, int k) {
   if (!c || k < 0 || k > 8) return FCFCG_ERR_ARG;
   c->kcell = k;
   for (int i = 0; i <= FCFCG_MAX_SLOT; i++) c->slot[i].grid_valid = 0;
+  return FCFCG_OK;
+}
+
+int fcfcg_set_warp_queue(fcfcg_ctx *c, int entries) {
+  if (!c || !(entries == 0 || entries == 256 || entries == 512 ||
+              entries == 1024))
+    return FCFCG_ERR_ARG;
+  c->qwarp_force = (uint32_t) entries;
   return FCFCG_OK;
 }
 
@@ -1355,6 +1367,9 @@ static int count_plan_make(fcfcg_ctx *c, slot_t *A, slot_t *B, int isauto,
     stage = 0;
   }
   L->hist_smem = (tabbytes + stage + hbytes <= 200 * 1024);
+  L->qwarp = c->qwarp_force ? c->qwarp_force
+      : ((c->tuned_q && c->tuned_q_key == g->key && c->tuned_q_wt == withwt)
+             ? c->tuned_q : 0);
   P->prec = prec;
   return FCFCG_OK;
 }
@@ -1390,7 +1405,7 @@ static int count_launch(fcfcg_ctx *c, const count_plan *P, int sort_a,
   CK(cudaMemsetAsync(c->d_head, 0, sizeof(uint32_t) * 4, c->stream));
   if (timed) CK(cudaEventRecord(c->ev[2], c->stream));
   size_t smem = 0;
-  CKK(fcfcg_k_count(c->stream, L, P->prec, c->nsm, &smem));
+  CKK(fcfcg_k_count(c->stream, L, P->prec, c->nsm, &smem, &c->last_qwarp));
   c->launches += 1;
   if (timed) CK(cudaEventRecord(c->ev[3], c->stream));
   if (P->prec == FCFCG_PREC_FP32_RECHECK) {
@@ -1450,6 +1465,7 @@ static void count_finish(fcfcg_ctx *c, const count_plan *P, const void *res,
   o->nstencil = P->nsten;
   o->nchunks = (uint32_t) stats[4];
   o->precision_used = P->prec;
+  o->warp_queue = P->prec == FCFCG_PREC_FP32_RECHECK ? (int) c->last_qwarp : 0;
   o->launches = c->launches;
 }
 
@@ -1584,6 +1600,7 @@ static int count_impl(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
     o->cells_per_smax = P.g.k;
     o->nchunks = (uint32_t) hstats[4];
     o->precision_used = P.prec;
+    o->warp_queue = P.prec == FCFCG_PREC_FP32_RECHECK ? (int) c->last_qwarp : 0;
     o->launches = c->launches;
   } else {
     count_finish(c, &P, hres, hstats, icnt, wcnt);
@@ -1874,6 +1891,29 @@ int fcfcg_autotune(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
       bk = k;
     }
   }
+  /* then the warp queue at that refinement */
+  uint32_t bq = 0;
+  const uint32_t saved_q = c->qwarp_force;
+  if (rc == FCFCG_OK && bk) {
+    c->kcell = bk;
+    static const uint32_t qs[3] = {1024, 512, 256};
+    double qms = 1e300;
+    for (int i = 0; i < 3 && rc == FCFCG_OK; i++) {
+      c->qwarp_force = qs[i];
+      double ms = 0;
+      for (int rep = 0; rep < 2 && rc == FCFCG_OK; rep++) {
+        rc = fcfcg_count(c, sa, sb, isauto, withwt, FCFCG_PREC_FP32_RECHECK,
+                         ic, wc);
+        ms = c->stats.ms_count + c->stats.ms_recheck;
+      }
+      if (rc == FCFCG_OK && ms < qms) {
+        qms = ms;
+        bq = qs[i];
+      }
+    }
+    if (qms < bms) bms = qms;
+  }
+  c->qwarp_force = saved_q;
   c->kcell = saved;
   if (rc == FCFCG_OK && bk) {
     /* the key of this catalogue pair, as the grid set-up computes it */
@@ -1883,6 +1923,9 @@ int fcfcg_autotune(fcfcg_ctx *c, int sa, int sb, int isauto, int withwt,
     key = g.key;
     c->tuned_k = bk;
     c->tuned_key = key;
+    c->tuned_q = bq;
+    c->tuned_q_key = key;
+    c->tuned_q_wt = withwt;
   }
   free(ic);
   free(wc);
@@ -2396,7 +2439,10 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
   BCK(cudaMemsetAsync(c->d_head, 0, sizeof(uint32_t) * 4, c->stream));
   BCK(cudaEventRecord(c->ev[2], c->stream));
   size_t smem = 0;
-  BCKK(fcfcg_k_count(c->stream, &L, prec, c->nsm, &smem));
+  L.qwarp = c->qwarp_force ? c->qwarp_force
+      : ((c->tuned_q && c->tuned_q_key == key && c->tuned_q_wt == withwt)
+             ? c->tuned_q : 0);
+  BCKK(fcfcg_k_count(c->stream, &L, prec, c->nsm, &smem, &c->last_qwarp));
   c->launches += 1;
   BCK(cudaEventRecord(c->ev[3], c->stream));
   unsigned long long nq = 0;
@@ -2460,6 +2506,7 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
     o->nstencil = nsten;
     o->nchunks = nchunk;
     o->precision_used = prec;
+    o->warp_queue = prec == FCFCG_PREC_FP32_RECHECK ? (int) c->last_qwarp : 0;
     o->launches = c->launches;
     if (hstats[3]) queue_grow(c, hstats[2] + hstats[2] / 4);
   }
@@ -2498,6 +2545,29 @@ int fcfcg_autotune_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs,
       bk = k;
     }
   }
+  /* then the warp queue at that refinement */
+  uint32_t bq = 0;
+  const uint32_t saved_q = c->qwarp_force;
+  if (rc == FCFCG_OK && bk) {
+    c->kcell = bk;
+    static const uint32_t qs[3] = {1024, 512, 256};
+    double qms = 1e300;
+    for (int i = 0; i < 3 && rc == FCFCG_OK; i++) {
+      c->qwarp_force = qs[i];
+      double ms = 0;
+      for (int rep = 0; rep < 2 && rc == FCFCG_OK; rep++) {
+        rc = fcfcg_count_batch(c, jobs, njobs, withwt,
+                               FCFCG_PREC_FP32_RECHECK, on_device);
+        ms = c->stats.ms_count + c->stats.ms_recheck;
+      }
+      if (rc == FCFCG_OK && ms > 0 && ms < qms) {
+        qms = ms;
+        bq = qs[i];
+      }
+    }
+    if (qms < bms) bms = qms;
+  }
+  c->qwarp_force = saved_q;
   c->kcell = saved;
   if (rc == FCFCG_OK && bk) {
     /* the key fcfcg_count_batch computes for this batch */
@@ -2514,6 +2584,9 @@ int fcfcg_autotune_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs,
     }
     c->tuned_k = bk;
     c->tuned_key = tune_key(nsum / (vol > 0 ? vol : 1), gr.reach) + 1000;
+    c->tuned_q = bq;
+    c->tuned_q_key = c->tuned_key;
+    c->tuned_q_wt = withwt;
   }
   if (best_k) *best_k = bk;
   if (best_ms) *best_ms = bms;

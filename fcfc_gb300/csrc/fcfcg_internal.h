@@ -166,6 +166,8 @@ typedef struct {
   uint32_t *queue;
   unsigned long long *qcount;  /* fill: 64 bits, so it cannot wrap */
   uint32_t qcap;
+  uint32_t qwarp;              /* FP32 kernel: entries of a warp's candidate
+                                  queue (256..1024; 0: the launcher picks) */
   unsigned long long *stats;   /* [0] candidates [1] in-range [2] recheck
                                   [3] inline rechecks */
   int hist_smem;               /* histogram in shared memory */
@@ -225,8 +227,11 @@ size_t fcfcg_k_count32_stage(int nsten, int withwt);
 size_t fcfcg_k_count32_tab_bytes(int nfs, int nfp, int nsb, int npb);
 int fcfcg_k_bbox(void *stream, size_t n, const double *x, const double *y,
     const double *z, unsigned long long *bits6);
+/* The count kernel of a launch.  FP32: L->qwarp 0 lets the launcher pick
+ * the warp queue (the largest of 1024 / 512 / 256 entries at the most CTAs
+ * per SM); the one used goes to *qwarp_used. */
 int fcfcg_k_count(void *stream, const fcfcg_launch *L, int precision,
-    int nsm, size_t *smem_used);
+    int nsm, size_t *smem_used, uint32_t *qwarp_used);
 /* Bits of the coarse cells (dim, cells of 1 / inv_cell from lo) that hold
  * an object, and their number (count). */
 int fcfcg_k_occupancy(void *stream, size_t n, const double *x,

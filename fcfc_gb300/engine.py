@@ -192,14 +192,20 @@ class PairCounter:
     def set_cells_per_smax(self, k: int):
         self._check(self.lib.fcfcg_set_cells_per_smax(self.h, int(k)))
 
+    def set_warp_queue(self, entries: int):
+        """Entries of the FP32 kernel's per-warp candidate queue (256, 512,
+        1024; 0 automatic)."""
+        self._check(self.lib.fcfcg_set_warp_queue(self.h, int(entries)))
+
     def set_queue_capacity(self, cap: int):
         """Limit the FP64 recheck queue (pairs beyond are binned inside the
         counting kernel; the counts do not change)."""
         self._check(self.lib.fcfcg_set_queue_capacity(self.h, int(cap)))
 
     def autotune(self, a: int, b: int | None = None, weighted=False):
-        """Time the FP32 count at 1..8 cells per maximum separation and keep
-        the fastest for catalogues of this density; returns (k, ms)."""
+        """Time the FP32 count at 1..8 cells per maximum separation, then
+        the warp queue sizes at the fastest, and keep both for catalogues of
+        this density; returns (k, ms)."""
         isauto = b is None or b == a
         k = C.c_int()
         ms = C.c_double()

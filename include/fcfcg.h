@@ -123,6 +123,7 @@ typedef struct {
   uint64_t nchunks;
   int precision_used;    /* FCFCG_PREC_*: FP32 windows too wide fall to FP64 */
   uint64_t launches;     /* kernels launched by this context since creation */
+  int warp_queue;        /* FP32 kernel: entries of a warp's candidate queue */
 } fcfcg_stats;
 
 const char *fcfcg_strerror(int err);
@@ -352,20 +353,31 @@ int fcfcg_stats_get(const fcfcg_ctx *ctx, fcfcg_stats *out);
  * box). */
 int fcfcg_set_cells_per_smax(fcfcg_ctx *ctx, int k);
 
-/* Capacity of the FP64 recheck queue in pairs (default and maximum: the
- * 2^25 pairs allocated with the context; larger values are clamped).
- * Ambiguous pairs beyond it are binned by the FP64 formula inside the
- * counting kernel instead of after it: the counts are the same, only
- * slower.  Meant for tests of that overflow path. */
+/* Entries of a warp's candidate queue in the FP32 counting kernel: 256,
+ * 512 or 1024, or 0 (default) for automatic -- the value fcfcg_autotune
+ * found for this binning and density, else the largest queue that keeps
+ * the most CTAs per SM.  The counts do not depend on it. */
+int fcfcg_set_warp_queue(fcfcg_ctx *ctx, int entries);
+
+/* Capacity of the FP64 recheck queue in pairs.  By default the queue holds
+ * 2^25 pairs and grows, after a count that overflowed it, to hold that
+ * count's ambiguous pairs (at most 2^28).  A capacity set here (clamped to
+ * the allocation) stays, and the queue no longer grows.  Ambiguous pairs
+ * beyond it are binned by the FP64 formula inside the counting kernel
+ * instead of after it: the counts are the same, only slower.  Meant for
+ * tests of that overflow path. */
 int fcfcg_set_queue_capacity(fcfcg_ctx *ctx, size_t cap);
 
 /*
- * Autotune the grid refinement for this binning and catalogue pair: times
- * the FP32 count at 1..8 cells per maximum separation (stopping two past
- * the fastest) and keeps the fastest for catalogues of the same number
- * density (key: log2 of the mean number of objects of the first catalogue
- * within the maximum separation box).  Later automatic counts of matching
- * density use it.
+ * Autotune the grid refinement and the kernel's tile for this binning and
+ * catalogue pair: times the FP32 count at 1..8 cells per maximum
+ * separation (stopping two past the fastest), then at the fastest with a
+ * warp candidate queue of 1024, 512 and 256 entries (a smaller queue can
+ * free shared memory for another CTA per SM or for L1), and keeps both for
+ * catalogues of the same number density (key: log2 of the mean number of
+ * objects of the first catalogue within the maximum separation box) and
+ * weighting.  Later automatic counts of matching density use them;
+ * fcfcg_stats.warp_queue reports the queue a count used.
  */
 int fcfcg_autotune(fcfcg_ctx *ctx, int slot_a, int slot_b, int isauto,
     int withwt, int *best_k, double *best_ms);

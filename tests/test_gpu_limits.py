@@ -95,3 +95,39 @@ def test_recheck_queue_overflow():
     for k in range(3):
         obk = fo.Bins(False, 1, ns=80, smin=0, ds=0.5, nmu=60, box=300.0)
         np.testing.assert_array_equal(cnt[k], obk.count(cats[k], mode=1))
+
+
+@pytest.mark.parametrize("weighted", [False, True], ids=["unwt", "wt"])
+def test_warp_queue_sizes(weighted):
+    """The FP32 kernel's per-warp candidate queue (256, 512, 1024 entries or
+    automatic) changes when candidates are binned, never the counts; dense
+    clusters fill a small queue several times per neighbour block."""
+    import fcfc_gb300 as fg
+    from fcfc_gb300 import synth
+    x = synth.neyman_scott(40, 200.0, 300, 1.5, seed=91)
+    w = synth.lognormal_weights(len(x), 0.3, seed=92) if weighted else None
+    pc = fg.PairCounter("box", fg.BIN_SMU, box=200.0, smin=0, smax=30, ds=1,
+                        nmu=30)
+    pc.load(0, x, w)
+    ob = fo.Bins(False, 1, ns=30, smin=0, ds=1, nmu=30, box=200.0)
+    want = ob.count(x, wa=w, weighted=weighted)
+    seen = set()
+    for q in (256, 512, 1024, 0):
+        pc.set_warp_queue(q)
+        got = pc.count_pairs(0, weighted=weighted)
+        st = pc.stats()
+        assert st["precision_used"] == fg.PREC_FP32_RECHECK
+        if q:
+            assert st["warp_queue"] == q
+        seen.add(st["warp_queue"])
+        if weighted:
+            np.testing.assert_allclose(got, want, rtol=1e-10, atol=1e-300)
+        else:
+            np.testing.assert_array_equal(got, want)
+    with pytest.raises(fg.FCFCGError):
+        pc.set_warp_queue(300)
+    # the autotuner times the queue sizes and keeps one
+    pc.set_warp_queue(0)
+    pc.autotune(0, weighted=weighted)
+    pc.count_pairs(0, weighted=weighted)
+    assert pc.stats()["warp_queue"] in (256, 512, 1024)
