@@ -274,6 +274,7 @@ k_count32(const fcfcg_launch L) {
   __shared__ uint32_t sh_chunk;
   __shared__ uint32_t sh_blk;   /* next neighbour block of the chunk */
   __shared__ MockSh sh_mock;   /* batched launch: the current catalogue */
+  __shared__ float sh_box[6];  /* the chunk points' bounding box (lo, hi) */
   int cur = -1;
   uint16_t *fs = (uint16_t *) smem;
   uint16_t *fp = fs + L.nfs;
@@ -396,11 +397,30 @@ k_count32(const fcfcg_launch L) {
       c2z = (float) (2.0 * (L.lo[2] + ((double) cz + 0.5) * L.cw[2]));
     }
     if (warp == 1) {
+      float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
+      float hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
       for (int k = lane; k < m; k += 32) {
-        S.a[k] = ((const float4 *) L.A.l4)[first + k];
+        const float4 v = ((const float4 *) L.A.l4)[first + k];
+        S.a[k] = v;
+        lo[0] = fminf(lo[0], v.x);
+        lo[1] = fminf(lo[1], v.y);
+        lo[2] = fminf(lo[2], v.z);
+        hi[0] = fmaxf(hi[0], v.x);
+        hi[1] = fmaxf(hi[1], v.y);
+        hi[2] = fmaxf(hi[2], v.z);
         if (WT) S.aw[k] = ((const int2 *) L.A.wq)[first + k];
         if (ADJ) S.wa[k] = L.A.w[first + k];
       }
+      for (int o = 16; o > 0; o >>= 1)
+        for (int d = 0; d < 3; d++) {
+          lo[d] = fminf(lo[d], __shfl_xor_sync(FULLMASK, lo[d], o));
+          hi[d] = fmaxf(hi[d], __shfl_xor_sync(FULLMASK, hi[d], o));
+        }
+      if (lane == 0)
+        for (int d = 0; d < 3; d++) {
+          sh_box[d] = lo[d];
+          sh_box[3 + d] = hi[d];
+        }
     } else if (warp == 0) {
       /* neighbour cells of this chunk, laid end to end */
       uint32_t run = 0;
@@ -520,6 +540,24 @@ k_count32(const fcfcg_launch L) {
           S.bw[lane] = make_float4(pb.w, __int_as_float(wq.x),
                                    __int_as_float(wq.y), 0.f);
         }
+      }
+      /* a block none of whose points is within the outer range of the
+       * chunk points' bounding box holds no candidate: skip it.  The
+       * box distance is formed as the candidate test forms a pair's
+       * separation (the same roundings, each monotone), so it never
+       * exceeds that of any pair of the block */
+      if (base + 32u > pin) {
+        bool far = true;
+        if (p < total) {
+          const float ex = fmaxf(fmaxf(sh_box[0] - bx, bx - sh_box[3]), 0.f);
+          const float ey = fmaxf(fmaxf(sh_box[1] - by, by - sh_box[4]), 0.f);
+          const float ez = fmaxf(fmaxf(sh_box[2] - bz, bz - sh_box[5]), 0.f);
+          if (IS_SPI(BIN) && GEOM == FCFCG_GEOM_BOX)
+            far = (ez >= L.p_lim) | (fmaf(ey, ey, ex * ex) >= L.s_lim);
+          else
+            far = fmaf(ez, ez, fmaf(ey, ey, ex * ex)) >= L.s_lim;
+        }
+        if (__all_sync(FULLMASK, far)) continue;
       }
       if (!ADJ) {
         /*
