@@ -546,18 +546,32 @@ k_count32(const fcfcg_launch L) {
        * box distance is formed as the candidate test forms a pair's
        * separation (the same roundings, each monotone), so it never
        * exceeds that of any pair of the block */
-      if (base + 32u > pin) {
-        bool far = true;
+      /* and a block all of whose points are within the outer range of
+       * the whole box (its farthest corner, rounded the same way) is binned
+       * without the test, as a block of cells wholly in range */
+      bool near_all = base + 32u <= pin;
+      if (!near_all) {
+        bool far = true, near = false;
         if (p < total) {
-          const float ex = fmaxf(fmaxf(sh_box[0] - bx, bx - sh_box[3]), 0.f);
-          const float ey = fmaxf(fmaxf(sh_box[1] - by, by - sh_box[4]), 0.f);
-          const float ez = fmaxf(fmaxf(sh_box[2] - bz, bz - sh_box[5]), 0.f);
-          if (IS_SPI(BIN) && GEOM == FCFCG_GEOM_BOX)
+          const float lx = sh_box[0] - bx, hx = sh_box[3] - bx;
+          const float ly = sh_box[1] - by, hy = sh_box[4] - by;
+          const float lz = sh_box[2] - bz, hz = sh_box[5] - bz;
+          const float ex = fmaxf(fmaxf(lx, -hx), 0.f);
+          const float ey = fmaxf(fmaxf(ly, -hy), 0.f);
+          const float ez = fmaxf(fmaxf(lz, -hz), 0.f);
+          const float fx = fmaxf(fabsf(lx), fabsf(hx));
+          const float fy = fmaxf(fabsf(ly), fabsf(hy));
+          const float fz = fmaxf(fabsf(lz), fabsf(hz));
+          if (IS_SPI(BIN) && GEOM == FCFCG_GEOM_BOX) {
             far = (ez >= L.p_lim) | (fmaf(ey, ey, ex * ex) >= L.s_lim);
-          else
+            near = (fz < L.p_lim) & (fmaf(fy, fy, fx * fx) < L.s_lim);
+          } else {
             far = fmaf(ez, ez, fmaf(ey, ey, ex * ex)) >= L.s_lim;
+            near = fmaf(fz, fz, fmaf(fy, fy, fx * fx)) < L.s_lim;
+          }
         }
         if (__all_sync(FULLMASK, far)) continue;
+        near_all = __all_sync(FULLMASK, near);
       }
       if (!ADJ) {
         /*
@@ -570,7 +584,7 @@ k_count32(const fcfcg_launch L) {
          * chunk point k against every lane's neighbour.
          */
         const bool all_lim = __all_sync(FULLMASK, ilim >= m);
-        const bool direct = !LOSCUT(GEOM, BIN) && all_lim && base + 32u <= pin;
+        const bool direct = !LOSCUT(GEOM, BIN) && all_lim && near_all;
         const uint32_t lt = (1u << lane) - 1u;
         uint32_t nq = direct ? (uint32_t) m * 32u : 0u;
         int i = direct ? m : 0;
