@@ -86,6 +86,12 @@ struct fcfcg_ctx {
   size_t d_mock_cap;
   uint32_t *d_mbase;
   size_t d_mbase_cap;
+  fcfcg_prep_cat *h_pcat;        /* the preparation kernels' catalogue table */
+  size_t h_pcat_cap;
+  void *d_pcat;
+  size_t d_pcat_cap;
+  double *d_bpart;               /* per-tile weight sums of a batch */
+  size_t d_bpart_cap;
   double *d_wpart;               /* weight-sum partials; [0] the sum */
   double *d_grad;                /* adjoint: sorted and input-order gradients */
   size_t d_grad_cap;
@@ -195,7 +201,7 @@ void fcfcg_destroy(fcfcg_ctx *c) {
                  c->d_sten, c->d_stenD, c->d_cnt, c->d_wt, c->d_stats,
                  c->d_bbox, c->d_wd, c->d_gfix, c->d_head, c->d_queue, c->d_cnvt,
                  c->d_mock, c->d_mbase, c->d_bout, c->d_bstat, c->d_grad,
-                 c->d_wpart};
+                 c->d_wpart, c->d_pcat, c->d_bpart};
     for (size_t i = 0; i < sizeof p / sizeof p[0]; i++)
       if (p[i]) cudaFree(p[i]);
     if (c->h_pinned) cudaFreeHost(c->h_pinned);
@@ -205,6 +211,7 @@ void fcfcg_destroy(fcfcg_ctx *c) {
   }
   fcfcg_bins_release(&c->bins);
   free(c->h_mock);
+  free(c->h_pcat);
   free(c);
 }
 
@@ -2119,11 +2126,29 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
     free(init);
     BCK(e);
   }
+  /* the catalogue table: inputs, slot offsets, first tiles */
+  if (c->h_pcat_cap < (size_t) na) {
+    free(c->h_pcat);
+    c->h_pcat = malloc(sizeof(fcfcg_prep_cat) * na);
+    c->h_pcat_cap = c->h_pcat ? (size_t) na : 0;
+    if (!c->h_pcat) BFAIL(FCFCG_ERR_MEMORY);
+  }
+  fcfcg_prep_cat *P = c->h_pcat;
+  const size_t tile = fcfcg_batch_tile();
+  uint32_t ntile = 0;
   for (int a = 0; a < na; a++) {
     const fcfcg_job *J = jobs + acc[a];
     const size_t o = base[a], n = J->n;
-    const double *ix = J->x, *iy = J->y, *iz = J->z;
-    const double *iw = withwt ? J->w : NULL;
+    fcfcg_prep_cat *Q = P + a;
+    memset(Q, 0, sizeof *Q);
+    Q->x = J->x;
+    Q->y = J->y;
+    Q->z = J->z;
+    Q->w = withwt ? J->w : NULL;
+    Q->o = o;
+    Q->n = n;
+    Q->tile0 = ntile;
+    ntile += (uint32_t) ((n + tile - 1) / tile);
     if (!on_device && !c->pageable) {
       BCK(cudaMemcpyAsync(S->x + o, J->x, sizeof(double) * n,
                           cudaMemcpyHostToDevice, c->stream));
@@ -2131,22 +2156,23 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
                           cudaMemcpyHostToDevice, c->stream));
       BCK(cudaMemcpyAsync(S->z + o, J->z, sizeof(double) * n,
                           cudaMemcpyHostToDevice, c->stream));
-      if (iw)
+      if (withwt)
         BCK(cudaMemcpyAsync(S->w + o, J->w, sizeof(double) * n,
                             cudaMemcpyHostToDevice, c->stream));
-      ix = S->x + o;
-      iy = S->y + o;
-      iz = S->z + o;
-      iw = iw ? S->w + o : NULL;
+      Q->x = S->x + o;
+      Q->y = S->y + o;
+      Q->z = S->z + o;
+      Q->w = withwt ? S->w + o : NULL;
     }
-    BCKK(fcfcg_k_prep(c->stream, n, ix, iy, iz, iw, b->rescale, 0, S->x + o,
-                      S->y + o, S->z + o, NULL, S->w + o,
-                      c->d_bstat + 8 * a + 6, c->d_wpart,
-                      (double *) (c->d_bstat + 8 * a + 7)));
-    BCKK(fcfcg_k_bbox(c->stream, n, S->x + o, S->y + o, S->z + o,
-                      c->d_bstat + 8 * a));
-    c->launches += iw ? 3 : 2;
   }
+  BGROW(c->d_pcat, c->d_pcat_cap, sizeof(fcfcg_prep_cat) * na);
+  BGROW(c->d_bpart, c->d_bpart_cap, sizeof(double) * ntile);
+  BCK(cudaMemcpyAsync(c->d_pcat, P, sizeof(fcfcg_prep_cat) * na,
+                      cudaMemcpyHostToDevice, c->stream));
+  BCKK(fcfcg_k_prep_batch(c->stream, (const fcfcg_prep_cat *) c->d_pcat, na,
+                          ntile, b->rescale, withwt, S->x, S->y, S->z, S->w,
+                          c->d_bstat, c->d_bpart));
+  c->launches += withwt ? 2 : 1;
   /* 2. per-catalogue range checks, weight scales and sums */
   unsigned long long *hb = malloc(sizeof(unsigned long long) * 8 * na);
   if (!hb) BFAIL(FCFCG_ERR_MEMORY);
@@ -2184,6 +2210,7 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
     int we = (wmax > 0) ? (int) ceil(log2(wmax)) : 0;
     if (ldexp(1.0, we) < wmax) we++;
     wexp[a] = we;
+    P[a].wexp = we;
     if (J->status) continue;
     if (withwt) memcpy(&J->sumw, hb + 8 * a + 7, 8);
     else J->sumw = (double) J->n;
@@ -2251,6 +2278,12 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
       xabs = fmax(xabs, L);
     }
     M->cell_base = (uint32_t) cells;
+    P[a].live = 1;
+    P[a].cell_base = M->cell_base;
+    for (int d = 0; d < 3; d++) {
+      P[a].ncell[d] = M->ncell[d];
+      P[a].cw[d] = M->cw[d];
+    }
     cells += nc;
     if (cells > 0x7FFFFFF0u) {
       free(wexp);
@@ -2323,31 +2356,20 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
   const size_t stl = fcfcg_scan_tmp_len(cells + 1) + 16;
   BGROW(c->scan_tmp, c->scan_cap, sizeof(uint32_t) * stl);
   BCK(cudaMemsetAsync(c->cfill, 0, sizeof(uint32_t) * (cells + 1), c->stream));
-  for (int a = 0; a < na; a++) {
-    const fcfcg_job *J = jobs + acc[a];
-    if (J->status) continue;
-    const fcfcg_mock *M = c->h_mock + a;
-    const size_t o = base[a];
-    BCKK(fcfcg_k_cell_batch(c->stream, J->n, S->x + o, S->y + o, S->z + o,
-                            M->ncell, M->cw, M->cell_base, S->cell_of + o,
-                            c->cfill));
-    c->launches++;
-  }
+  /* the table again, with the grids (the stream is idle: the range checks
+   * synchronised it) */
+  BCK(cudaMemcpyAsync(c->d_pcat, P, sizeof(fcfcg_prep_cat) * na,
+                      cudaMemcpyHostToDevice, c->stream));
+  BCKK(fcfcg_k_cell_batch(c->stream, (const fcfcg_prep_cat *) c->d_pcat, na,
+                          ntile, S->x, S->y, S->z, S->cell_of, c->cfill));
   BCKK(fcfcg_scan(c->stream, c->cfill, cells, S->cstart, c->scan_tmp));
-  c->launches += 3;
   BCK(cudaMemsetAsync(c->cfill, 0, sizeof(uint32_t) * (cells + 1), c->stream));
-  for (int a = 0; a < na; a++) {
-    const fcfcg_job *J = jobs + acc[a];
-    if (J->status) continue;
-    const fcfcg_mock *M = c->h_mock + a;
-    const size_t o = base[a];
-    BCKK(fcfcg_k_scatter_batch(c->stream, J->n, S->x + o, S->y + o, S->z + o,
-                               withwt ? S->w + o : NULL, withwt, wexp[a],
-                               M->ncell, M->cw, M->cell_base, (uint32_t) o,
-                               S->cell_of + o, S->cstart, c->cfill, S->l4,
-                               S->wq, S->sx, S->sy, S->sz, S->sw, S->sid));
-    c->launches++;
-  }
+  BCKK(fcfcg_k_scatter_batch(c->stream, (const fcfcg_prep_cat *) c->d_pcat,
+                             na, ntile, S->x, S->y, S->z,
+                             withwt ? S->w : NULL, withwt, S->cell_of,
+                             S->cstart, c->cfill, S->l4, S->wq, S->sx, S->sy,
+                             S->sz, S->sw, S->sid));
+  c->launches += 5;
   /* 6. per-catalogue histograms and the catalogue table */
   const size_t per = (size_t) b->ntot * (withwt ? 2 : 1);
   BGROW(c->d_bout, c->d_bout_cap, sizeof(unsigned long long) * per * na);

@@ -205,18 +205,41 @@ int fcfcg_k_chunks(void *stream, const uint32_t *cstart, uint32_t ncell,
     uint32_t clen, uint32_t *cchunk, uint32_t *scan_tmp, size_t scan_tmp_len,
     uint32_t *chunks, uint32_t *nchunk_out, const uint32_t *mock_cell_base,
     int nmock);
-/* Batch grid: cells of one catalogue numbered from cell_base into a shared
- * cell-count array (k_cell), and its points scattered into the shared
- * sorted arrays after the global scan (k_scatter); sid = id_base + i. */
-int fcfcg_k_cell_batch(void *stream, size_t n, const double *x,
-    const double *y, const double *z, const int ncell[3], const double cw[3],
-    uint32_t cell_base, uint32_t *cell_of, uint32_t *count);
-int fcfcg_k_scatter_batch(void *stream, size_t n, const double *x,
-    const double *y, const double *z, const double *w, int has_w, int wexp,
-    const int ncell[3], const double cw[3], uint32_t cell_base,
-    uint32_t id_base, const uint32_t *cell_of, const uint32_t *cstart,
-    uint32_t *cfill, float *l4, int *wq, double *sx, double *sy, double *sz,
-    double *sw, uint32_t *sid);
+/* One catalogue of a batch for the preparation kernels: its inputs (device
+ * or GPU-readable host memory), its place o in the batch slot, its first
+ * tile (tiles of fcfcg_batch_tile() points, numbered across the batch) and,
+ * once its range checks pass (live), its grid and weight scale. */
+typedef struct {
+  const double *x, *y, *z, *w;
+  size_t o, n;
+  uint32_t tile0;
+  int live, wexp;
+  int ncell[3];
+  uint32_t cell_base;
+  double cw[3];
+} fcfcg_prep_cat;
+
+size_t fcfcg_batch_tile(void);
+/* Every catalogue rescaled into the slot arrays o*; per catalogue a,
+ * bstat[8a + 0..5] its bounding box (order-preserving keys, min then max;
+ * initialised by the caller to ~0 and 0), bstat[8a + 6] max |w| bits and,
+ * with weights, bstat[8a + 7] the weight sum (a double, in a fixed order;
+ * partial: ntile doubles of scratch). */
+int fcfcg_k_prep_batch(void *stream, const fcfcg_prep_cat *d_cat, int ncat,
+    uint32_t ntile, double rescale, int withwt, double *ox, double *oy,
+    double *oz, double *ow, unsigned long long *bstat, double *partial);
+/* Batch grid: every live catalogue's cells numbered from its cell_base into
+ * a shared cell-count array (k_cell_batch), and its points scattered into
+ * the shared sorted arrays after the global scan (k_scatter_batch); the id
+ * of slot point i is i. */
+int fcfcg_k_cell_batch(void *stream, const fcfcg_prep_cat *d_cat, int ncat,
+    uint32_t ntile, const double *x, const double *y, const double *z,
+    uint32_t *cell_of, uint32_t *count);
+int fcfcg_k_scatter_batch(void *stream, const fcfcg_prep_cat *d_cat,
+    int ncat, uint32_t ntile, const double *x, const double *y,
+    const double *z, const double *w, int has_w, const uint32_t *cell_of,
+    const uint32_t *cstart, uint32_t *cfill, float *l4, int *wq, double *sx,
+    double *sy, double *sz, double *sw, uint32_t *sid);
 /* out[sid[p]] = in[p] for p < n (sorted order back to input order). */
 int fcfcg_k_unsort(void *stream, size_t n, const uint32_t *sid,
     const double *in, double *out);

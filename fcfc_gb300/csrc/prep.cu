@@ -258,6 +258,16 @@ __device__ __forceinline__ int cell_axis(double v, double lo, double cw,
   return c;
 }
 
+/* The global cell of a point (cells of one grid numbered from cell_base). */
+__device__ __forceinline__ uint32_t cell_of_point(double a, double b,
+    double d, int nx, int ny, int nz, double cwx, double cwy, double cwz,
+    double lox, double loy, double loz, uint32_t cell_base) {
+  int cx = cell_axis(a, lox, cwx, nx);
+  int cy = cell_axis(b, loy, cwy, ny);
+  int cz = cell_axis(d, loz, cwz, nz);
+  return cell_base + ((uint32_t) cz * ny + cy) * nx + cx;
+}
+
 __global__ void k_cell(size_t n, const double *__restrict__ x,
     const double *__restrict__ y, const double *__restrict__ z, int nx,
     int ny, int nz, double cwx, double cwy, double cwz, double lox,
@@ -265,13 +275,45 @@ __global__ void k_cell(size_t n, const double *__restrict__ x,
     uint32_t *__restrict__ count) {
   for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n;
        i += (size_t) gridDim.x * blockDim.x) {
-    int cx = cell_axis(x[i], lox, cwx, nx);
-    int cy = cell_axis(y[i], loy, cwy, ny);
-    int cz = cell_axis(z[i], loz, cwz, nz);
-    uint32_t c = cell_base + ((uint32_t) cz * ny + cy) * nx + cx;
+    uint32_t c = cell_of_point(x[i], y[i], z[i], nx, ny, nz, cwx, cwy, cwz,
+                               lox, loy, loz, cell_base);
     cell_of[i] = c;
     atomicAdd(count + c, 1u);
   }
+}
+
+/* Point i (input order) of a grid to its sorted place pos: the FP32
+ * offsets from its cell centre and its weight's scaled high part (l4), the
+ * weight's fixed-point split (wq), FP64 copies and its id. */
+__device__ __forceinline__ void scatter_point(uint32_t c, uint32_t pos,
+    double a, double b, double d, double wv, int wexp, int nx, int ny,
+    double cwx, double cwy, double cwz, double lox, double loy, double loz,
+    uint32_t cell_base, uint32_t id, float4 *__restrict__ l4,
+    int2 *__restrict__ wq, double *__restrict__ sx, double *__restrict__ sy,
+    double *__restrict__ sz, double *__restrict__ sw,
+    uint32_t *__restrict__ sid) {
+  const uint32_t cl = c - cell_base;
+  int cx = (int) (cl % (uint32_t) nx);
+  int cy = (int) ((cl / (uint32_t) nx) % (uint32_t) ny);
+  int cz = (int) (cl / ((uint32_t) nx * (uint32_t) ny));
+  double ccx = lox + (cx + 0.5) * cwx;
+  double ccy = loy + (cy + 0.5) * cwy;
+  double ccz = loz + (cz + 0.5) * cwz;
+  double ws = ldexp(wv, -wexp);            /* |ws| <= 1 */
+  int wi = (int) __double2ll_rn(ws * 1073741824.0);
+  float wr = (float) (ws - (double) wi * (1.0 / 1073741824.0));
+  float4 v;
+  v.x = (float) (a - ccx);
+  v.y = (float) (b - ccy);
+  v.z = (float) (d - ccz);
+  v.w = (float) ws;
+  l4[pos] = v;
+  wq[pos] = make_int2(wi, __float_as_int(wr));
+  sx[pos] = a;
+  sy[pos] = b;
+  sz[pos] = d;
+  sw[pos] = wv;
+  sid[pos] = id;
 }
 
 __global__ void k_scatter(size_t n, const double *__restrict__ x,
@@ -288,31 +330,10 @@ __global__ void k_scatter(size_t n, const double *__restrict__ x,
        i += (size_t) gridDim.x * blockDim.x) {
     uint32_t c = cell_of[i];
     uint32_t pos = cstart[c] + atomicAdd(cfill + c, 1u);
-    const uint32_t cl = c - cell_base;
-    int cx = (int) (cl % (uint32_t) nx);
-    int cy = (int) ((cl / (uint32_t) nx) % (uint32_t) ny);
-    int cz = (int) (cl / ((uint32_t) nx * (uint32_t) ny));
-    double a = x[i], b = y[i], d = z[i];
-    double ccx = lox + (cx + 0.5) * cwx;
-    double ccy = loy + (cy + 0.5) * cwy;
-    double ccz = loz + (cz + 0.5) * cwz;
-    double wv = has_w ? w[i] : 1.0;
-    double ws = ldexp(wv, -wexp);            /* |ws| <= 1 */
-    int wi = (int) __double2ll_rn(ws * 1073741824.0);
-    float wr = (float) (ws - (double) wi * (1.0 / 1073741824.0));
-    float4 v;
-    v.x = (float) (a - ccx);
-    v.y = (float) (b - ccy);
-    v.z = (float) (d - ccz);
-    v.w = (float) ws;
-    l4[pos] = v;
-    wq[pos] = make_int2(wi, __float_as_int(wr));
-    sx[pos] = a;
-    sy[pos] = b;
-    sz[pos] = d;
+    scatter_point(c, pos, x[i], y[i], z[i], has_w ? w[i] : 1.0, wexp, nx, ny,
+                  cwx, cwy, cwz, lox, loy, loz, cell_base,
+                  id_base + (uint32_t) i, l4, wq, sx, sy, sz, sw, sid);
     if (ss) ss[pos] = s[i];
-    sw[pos] = wv;
-    sid[pos] = id_base + (uint32_t) i;
   }
 }
 
@@ -352,29 +373,209 @@ extern "C" int fcfcg_scan(void *stream, const uint32_t *in, size_t n,
   return scan_u32((cudaStream_t) stream, in, n, out, tmp);
 }
 
-extern "C" int fcfcg_k_cell_batch(void *stream, size_t n, const double *x,
-    const double *y, const double *z, const int ncell[3], const double cw[3],
-    uint32_t cell_base, uint32_t *cell_of, uint32_t *count) {
-  if (!n) return 0;
-  k_cell<<<grid_for(n, PREP_THREADS), PREP_THREADS, 0,
-           (cudaStream_t) stream>>>(n, x, y, z, ncell[0], ncell[1], ncell[2],
-                                    cw[0], cw[1], cw[2], 0.0, 0.0, 0.0,
-                                    cell_base, cell_of, count);
+/* ------------------------------------------------------------------------ */
+/* Batches: one launch per stage over every catalogue.  Block t handles tile
+ * t (BATCH_TILE points of one catalogue); the catalogue table lists each
+ * catalogue's first tile, so a block finds its catalogue by bisection. */
+
+#define BATCH_ITEMS 8
+#define BATCH_TILE (PREP_THREADS * BATCH_ITEMS)
+
+extern "C" size_t fcfcg_batch_tile(void) { return BATCH_TILE; }
+
+__device__ __forceinline__ int batch_cat(const fcfcg_prep_cat *__restrict__ cat,
+    int ncat, uint32_t t) {
+  int lo = 0, hi = ncat;          /* the last lo with cat[lo].tile0 <= t */
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (cat[mid].tile0 <= t) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+/* Rescale every catalogue into the batch slot (as k_prep), with each
+ * catalogue's bounding box (order-preserving keys, bstat[8a + 0..5]), max
+ * |w| bits (bstat[8a + 6]) and this tile's weight sum in a fixed order
+ * (partial[t]). */
+__global__ void __launch_bounds__(PREP_THREADS) k_prep_batch(
+    const fcfcg_prep_cat *__restrict__ cat, int ncat, double rescale,
+    int withwt, double *ox, double *oy, double *oz, double *ow,
+    unsigned long long *bstat, double *__restrict__ partial) {
+  __shared__ double sh_sum[PREP_THREADS];
+  const uint32_t t = blockIdx.x;
+  const int a = batch_cat(cat, ncat, t);
+  const fcfcg_prep_cat *C = cat + a;
+  const double *x = C->x, *y = C->y, *z = C->z, *w = withwt ? C->w : NULL;
+  const size_t o = C->o, n = C->n;
+  const size_t i0 = (size_t) (t - C->tile0) * BATCH_TILE;
+  const size_t i1 = (i0 + BATCH_TILE < n) ? i0 + BATCH_TILE : n;
+  unsigned long long lo[3] = {~0ull, ~0ull, ~0ull}, hi[3] = {0, 0, 0};
+  unsigned long long wm = 0;
+  double ws = 0;
+  for (size_t i = i0 + threadIdx.x; i < i1; i += PREP_THREADS) {
+    double v[3] = {x[i], y[i], z[i]};
+    if (rescale != 1)
+      for (int k = 0; k < 3; k++) v[k] = __dmul_rn(v[k], rescale);
+    ox[o + i] = v[0];
+    oy[o + i] = v[1];
+    oz[o + i] = v[2];
+    for (int k = 0; k < 3; k++) {
+      const unsigned long long q = dkey(v[k]);
+      lo[k] = q < lo[k] ? q : lo[k];
+      hi[k] = q > hi[k] ? q : hi[k];
+    }
+    if (w) {
+      const double u = w[i];
+      ow[o + i] = u;
+      ws = __dadd_rn(ws, u);
+      const unsigned long long bits =
+          (unsigned long long) __double_as_longlong(fabs(u));
+      wm = bits > wm ? bits : wm;
+    }
+  }
+  unsigned long long *B = bstat + 8 * (size_t) a;
+  for (int k = 0; k < 3; k++) {
+    for (int s = 16; s > 0; s >>= 1) {
+      const unsigned long long p = __shfl_xor_sync(0xffffffffu, lo[k], s);
+      const unsigned long long q = __shfl_xor_sync(0xffffffffu, hi[k], s);
+      lo[k] = p < lo[k] ? p : lo[k];
+      hi[k] = q > hi[k] ? q : hi[k];
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(B + k, lo[k]);
+      atomicMax(B + 3 + k, hi[k]);
+    }
+  }
+  if (!withwt) return;
+  for (int s = 16; s > 0; s >>= 1) {
+    const unsigned long long p = __shfl_xor_sync(0xffffffffu, wm, s);
+    wm = p > wm ? p : wm;
+  }
+  if ((threadIdx.x & 31) == 0 && wm) atomicMax(B + 6, wm);
+  sh_sum[threadIdx.x] = ws;
+  __syncthreads();
+  for (int s = PREP_THREADS / 2; s > 0; s >>= 1) {
+    if ((int) threadIdx.x < s)
+      sh_sum[threadIdx.x] = __dadd_rn(sh_sum[threadIdx.x],
+                                      sh_sum[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[t] = sh_sum[0];
+}
+
+/* Block a: catalogue a's weight sum from its tiles' sums, in a fixed order,
+ * into bstat[8a + 7] (as a double). */
+__global__ void __launch_bounds__(PREP_THREADS) k_sum_batch(
+    const fcfcg_prep_cat *__restrict__ cat, int ncat, uint32_t ntile,
+    const double *__restrict__ partial, unsigned long long *bstat) {
+  __shared__ double sh[PREP_THREADS];
+  const int a = blockIdx.x;
+  const uint32_t t0 = cat[a].tile0;
+  const uint32_t t1 = (a + 1 < ncat) ? cat[a + 1].tile0 : ntile;
+  double v = 0;
+  for (uint32_t t = t0 + threadIdx.x; t < t1; t += PREP_THREADS)
+    v = __dadd_rn(v, partial[t]);
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = PREP_THREADS / 2; s > 0; s >>= 1) {
+    if ((int) threadIdx.x < s)
+      sh[threadIdx.x] = __dadd_rn(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    bstat[8 * (size_t) a + 7] =
+        (unsigned long long) __double_as_longlong(sh[0]);
+}
+
+extern "C" int fcfcg_k_prep_batch(void *stream, const fcfcg_prep_cat *d_cat,
+    int ncat, uint32_t ntile, double rescale, int withwt, double *ox,
+    double *oy, double *oz, double *ow, unsigned long long *bstat,
+    double *partial) {
+  if (!ncat || !ntile) return 0;
+  cudaStream_t st = (cudaStream_t) stream;
+  k_prep_batch<<<ntile, PREP_THREADS, 0, st>>>(d_cat, ncat, rescale, withwt,
+                                               ox, oy, oz, ow, bstat,
+                                               partial);
+  cudaError_t e = cudaGetLastError();
+  if (e || !withwt) return (int) e;
+  k_sum_batch<<<ncat, PREP_THREADS, 0, st>>>(d_cat, ncat, ntile, partial,
+                                             bstat);
   return (int) cudaGetLastError();
 }
 
-extern "C" int fcfcg_k_scatter_batch(void *stream, size_t n, const double *x,
-    const double *y, const double *z, const double *w, int has_w, int wexp,
-    const int ncell[3], const double cw[3], uint32_t cell_base,
-    uint32_t id_base, const uint32_t *cell_of, const uint32_t *cstart,
-    uint32_t *cfill, float *l4, int *wq, double *sx, double *sy, double *sz,
-    double *sw, uint32_t *sid) {
-  if (!n) return 0;
-  k_scatter<<<grid_for(n, PREP_THREADS), PREP_THREADS, 0,
-              (cudaStream_t) stream>>>(
-      n, x, y, z, NULL, w, has_w, wexp, ncell[0], ncell[1], cw[0], cw[1],
-      cw[2], 0.0, 0.0, 0.0, cell_base, id_base, cell_of, cstart, cfill,
-      (float4 *) l4, (int2 *) wq, sx, sy, sz, NULL, sw, sid);
+/* Cells of every live catalogue's points (slot arrays x, y, z), numbered
+ * from the catalogue's cell_base into the shared count array. */
+__global__ void __launch_bounds__(PREP_THREADS) k_cell_batch(
+    const fcfcg_prep_cat *__restrict__ cat, int ncat,
+    const double *__restrict__ x, const double *__restrict__ y,
+    const double *__restrict__ z, uint32_t *__restrict__ cell_of,
+    uint32_t *__restrict__ count) {
+  const uint32_t t = blockIdx.x;
+  const fcfcg_prep_cat *C = cat + batch_cat(cat, ncat, t);
+  if (!C->live) return;
+  const size_t o = C->o, n = C->n;
+  const size_t i0 = (size_t) (t - C->tile0) * BATCH_TILE;
+  const size_t i1 = (i0 + BATCH_TILE < n) ? i0 + BATCH_TILE : n;
+  const int nx = C->ncell[0], ny = C->ncell[1], nz = C->ncell[2];
+  const double cwx = C->cw[0], cwy = C->cw[1], cwz = C->cw[2];
+  const uint32_t base = C->cell_base;
+  for (size_t i = o + i0 + threadIdx.x; i < o + i1; i += PREP_THREADS) {
+    const uint32_t c = cell_of_point(x[i], y[i], z[i], nx, ny, nz, cwx, cwy,
+                                     cwz, 0.0, 0.0, 0.0, base);
+    cell_of[i] = c;
+    atomicAdd(count + c, 1u);
+  }
+}
+
+/* Every live catalogue's points to their sorted places (as k_scatter); the
+ * id of point i of the slot is i. */
+__global__ void __launch_bounds__(PREP_THREADS) k_scatter_batch(
+    const fcfcg_prep_cat *__restrict__ cat, int ncat,
+    const double *__restrict__ x, const double *__restrict__ y,
+    const double *__restrict__ z, const double *__restrict__ w, int has_w,
+    const uint32_t *__restrict__ cell_of,
+    const uint32_t *__restrict__ cstart, uint32_t *__restrict__ cfill,
+    float4 *__restrict__ l4, int2 *__restrict__ wq, double *__restrict__ sx,
+    double *__restrict__ sy, double *__restrict__ sz, double *__restrict__ sw,
+    uint32_t *__restrict__ sid) {
+  const uint32_t t = blockIdx.x;
+  const fcfcg_prep_cat *C = cat + batch_cat(cat, ncat, t);
+  if (!C->live) return;
+  const size_t o = C->o, n = C->n;
+  const size_t i0 = (size_t) (t - C->tile0) * BATCH_TILE;
+  const size_t i1 = (i0 + BATCH_TILE < n) ? i0 + BATCH_TILE : n;
+  const int nx = C->ncell[0], ny = C->ncell[1], wexp = C->wexp;
+  const double cwx = C->cw[0], cwy = C->cw[1], cwz = C->cw[2];
+  const uint32_t base = C->cell_base;
+  for (size_t i = o + i0 + threadIdx.x; i < o + i1; i += PREP_THREADS) {
+    const uint32_t c = cell_of[i];
+    const uint32_t pos = cstart[c] + atomicAdd(cfill + c, 1u);
+    scatter_point(c, pos, x[i], y[i], z[i], has_w ? w[i] : 1.0, wexp, nx, ny,
+                  cwx, cwy, cwz, 0.0, 0.0, 0.0, base, (uint32_t) i, l4, wq,
+                  sx, sy, sz, sw, sid);
+  }
+}
+
+extern "C" int fcfcg_k_cell_batch(void *stream, const fcfcg_prep_cat *d_cat,
+    int ncat, uint32_t ntile, const double *x, const double *y,
+    const double *z, uint32_t *cell_of, uint32_t *count) {
+  if (!ncat || !ntile) return 0;
+  k_cell_batch<<<ntile, PREP_THREADS, 0, (cudaStream_t) stream>>>(
+      d_cat, ncat, x, y, z, cell_of, count);
+  return (int) cudaGetLastError();
+}
+
+extern "C" int fcfcg_k_scatter_batch(void *stream,
+    const fcfcg_prep_cat *d_cat, int ncat, uint32_t ntile, const double *x,
+    const double *y, const double *z, const double *w, int has_w,
+    const uint32_t *cell_of, const uint32_t *cstart, uint32_t *cfill,
+    float *l4, int *wq, double *sx, double *sy, double *sz, double *sw,
+    uint32_t *sid) {
+  if (!ncat || !ntile) return 0;
+  k_scatter_batch<<<ntile, PREP_THREADS, 0, (cudaStream_t) stream>>>(
+      d_cat, ncat, x, y, z, w, has_w, cell_of, cstart, cfill, (float4 *) l4,
+      (int2 *) wq, sx, sy, sz, sw, sid);
   return (int) cudaGetLastError();
 }
 
