@@ -206,6 +206,34 @@ __device__ __forceinline__ bool candidate(const fcfcg_launch &L, float4 pa,
   return v < L.s_lim;
 }
 
+/* candidate() for chunk points 2k and 2k + 1 at once (pxy = (x, x', y, y'),
+ * pz = (z, z')): packed FP32 operations round each component as the scalar
+ * ones do, so c0 and c1 are candidate()'s answers bit for bit. */
+template <int GEOM, int BIN>
+__device__ __forceinline__ void candidate2(const fcfcg_launch &L, float4 pxy,
+    float2 pz, float bx, float by, float bz, float ux, float uy, float uz,
+    float lh, float lP, bool &c0, bool &c1) {
+  const float2 dx = __fadd2_rn(make_float2(pxy.x, pxy.y), make_float2(-bx, -bx));
+  const float2 dy = __fadd2_rn(make_float2(pxy.z, pxy.w), make_float2(-by, -by));
+  const float2 dz = __fadd2_rn(pz, make_float2(-bz, -bz));
+  if (IS_SPI(BIN) && GEOM == FCFCG_GEOM_BOX) {
+    const float2 v = __ffma2_rn(dy, dy, __fmul2_rn(dx, dx));
+    c0 = (fabsf(dz.x) < L.p_lim) & (v.x < L.s_lim);
+    c1 = (fabsf(dz.y) < L.p_lim) & (v.y < L.s_lim);
+  } else if (LOSCUT(GEOM, BIN)) {
+    const float2 v = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+    const float2 t = __ffma2_rn(dz, make_float2(uz, uz),
+        __ffma2_rn(dy, make_float2(uy, uy), __fmul2_rn(dx, make_float2(ux, ux))));
+    const float2 r = __ffma2_rn(v, make_float2(lh, lh), make_float2(lP, lP));
+    c0 = (v.x < L.s_lim) & (fabsf(t.x) < r.x);
+    c1 = (v.y < L.s_lim) & (fabsf(t.y) < r.y);
+  } else {
+    const float2 v = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+    c0 = v.x < L.s_lim;
+    c1 = v.y < L.s_lim;
+  }
+}
+
 /* Compare a neighbour point (one per lane) with chunk points [i0, i1):
  * bit i - i0 of the result marks a candidate inside the outer range.  For
  * survey (s_perp, pi) counts (u, lh, lP) is the lane's line-of-sight
@@ -291,6 +319,10 @@ k_count32(const fcfcg_launch L) {
     unsigned char *b = smem + soff;
     S.a = (float4 *) b;
     b += (size_t) FCHUNK * 16;
+    S.pxy = (float4 *) b;
+    b += (size_t) FCHUNK * 8;
+    S.pz = (float2 *) b;
+    b += (size_t) FCHUNK * 4;
     S.aw = (int2 *) b;
     b += WT ? (size_t) FCHUNK * 8 : 0;
     S.pre = (uint32_t *) b;
@@ -399,9 +431,13 @@ k_count32(const fcfcg_launch L) {
     if (warp == 1) {
       float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX};
       float hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+      float *pxy = (float *) S.pxy, *pz = (float *) S.pz;
       for (int k = lane; k < m; k += 32) {
         const float4 v = ((const float4 *) L.A.l4)[first + k];
         S.a[k] = v;
+        pxy[(k >> 1) * 4 + (k & 1)] = v.x;
+        pxy[(k >> 1) * 4 + 2 + (k & 1)] = v.y;
+        pz[k] = v.z;
         lo[0] = fminf(lo[0], v.x);
         lo[1] = fminf(lo[1], v.y);
         lo[2] = fminf(lo[2], v.z);
@@ -416,11 +452,19 @@ k_count32(const fcfcg_launch L) {
           lo[d] = fminf(lo[d], __shfl_xor_sync(FULLMASK, lo[d], o));
           hi[d] = fmaxf(hi[d], __shfl_xor_sync(FULLMASK, hi[d], o));
         }
-      if (lane == 0)
+      if (lane == 0) {
         for (int d = 0; d < 3; d++) {
           sh_box[d] = lo[d];
           sh_box[3 + d] = hi[d];
         }
+        if (m & 1) {
+          /* the odd chunk's last pair: a partner no test passes (its
+           * squared separation overflows, its |dz| exceeds any pi_max) */
+          pxy[(m >> 1) * 4 + 1] = 1e30f;
+          pxy[(m >> 1) * 4 + 3] = 1e30f;
+          pz[m] = 1e30f;
+        }
+      }
     } else if (warp == 0) {
       /* neighbour cells of this chunk, laid end to end */
       uint32_t run = 0;
@@ -592,13 +636,19 @@ k_count32(const fcfcg_launch L) {
           /* scan from chunk point i until the next one could overflow the
            * queue (the binning below is the only copy of that code) */
           if (all_lim) {
-#pragma unroll 2
-            for (; i < m && nq <= L.qwarp - 32u; i++) {
-              const bool inr = candidate<GEOM, BIN>(L, S.a[i], bx, by, bz, ux,
-                                                    uy, uz, lh, lP);
-              const uint32_t bal = __ballot_sync(FULLMASK, inr);
-              if (inr) S.q[nq + __popc(bal & lt)] = (uint16_t) (i | (lane << 6));
-              nq += __popc(bal);
+            /* two chunk points per step (i even), each of their tests
+             * rounded as the scalar test is */
+            for (; i < m && nq <= L.qwarp - 64u; i += 2) {
+              bool c0, c1;
+              candidate2<GEOM, BIN>(L, S.pxy[i >> 1], S.pz[i >> 1], bx, by, bz,
+                                    ux, uy, uz, lh, lP, c0, c1);
+              const uint32_t b0 = __ballot_sync(FULLMASK, c0);
+              const uint32_t b1 = __ballot_sync(FULLMASK, c1);
+              if (c0) S.q[nq + __popc(b0 & lt)] = (uint16_t) (i | (lane << 6));
+              nq += __popc(b0);
+              if (c1)
+                S.q[nq + __popc(b1 & lt)] = (uint16_t) ((i + 1) | (lane << 6));
+              nq += __popc(b1);
             }
           } else {
             /* the chunk's own cell in an auto count (j > i only), or lanes

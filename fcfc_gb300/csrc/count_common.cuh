@@ -555,6 +555,10 @@ __device__ __forceinline__ void hist_flush(const fcfcg_launch &L,
  * block's in-range pairs (chunk point | lane << 6). */
 struct Stage {
   float4 *a;        /* FCHUNK: chunk point local x y z, scaled weight */
+  /* FCHUNK / 2: chunk points 2k and 2k + 1 side by side, for the packed
+   * FP32 candidate test: (x, x', y, y') and (z, z') */
+  float4 *pxy;
+  float2 *pz;
   int2 *aw;         /* FCHUNK: chunk point integer weight, remainder bits */
   uint32_t *pre;    /* nsten + 1: prefix of neighbour sizes */
   uint32_t *bst;    /* nsten: first sorted index of each neighbour */
@@ -572,7 +576,8 @@ struct Stage {
 
 /* wt: 0 unweighted, 1 weighted, 2 adjoint (weighted + FP64 gradients) */
 __host__ __device__ __forceinline__ size_t stage_cta_bytes(int nsten, int wt) {
-  size_t n = (size_t) FCHUNK * 16 + (wt ? (size_t) FCHUNK * 8 : 0);
+  size_t n = (size_t) FCHUNK * 16 + (size_t) FCHUNK * 12 +
+             (wt ? (size_t) FCHUNK * 8 : 0);
   n += (((size_t) nsten + 1) * 4 + 15) & ~(size_t) 15;
   n += (((size_t) nsten) * 4 + 15) & ~(size_t) 15;
   if (wt == 2) n += (size_t) FCHUNK * 16;
