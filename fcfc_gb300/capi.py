@@ -150,6 +150,7 @@ PROTOTYPES = {
     "fcfcg_graph_destroy": (None, [P]),
     "fcfcg_set_cells_per_smax": (C.c_int, [P, C.c_int]),
     "fcfcg_set_queue_capacity": (C.c_int, [P, C.c_size_t]),
+    "fcfcg_set_hist_handover": (C.c_int, [P, C.c_ulonglong]),
     "fcfcg_set_warp_queue": (C.c_int, [P, C.c_int]),
     "fcfcg_probe_smem_atomics": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
     "fcfcg_autotune": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_int,

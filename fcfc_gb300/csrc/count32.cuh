@@ -50,7 +50,7 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
     int cy, int cz,
     float c2x, float c2y, float c2z, const uint16_t *fs, const uint16_t *fp,
     const float *fse, const float *fpe, uint32_t *h, uint32_t &n_in,
-    uint32_t &n_q, unsigned long long &n_inline, long long &gbv) {
+    uint32_t &n_q, unsigned long long &n_inline, long long &gbv, bool hs) {
   const int i = (int) (ent & 63u), src = (int) (ent >> 6);
   const float4 pa = S.a[i];
   const float4 pb = S.b[src];
@@ -163,7 +163,7 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
       code = nb_code(BATCH ? ms->nc : L.ncell, cx, cy, cz,
                      __ldg((const int4 *) L.sten + S.bt[src]));
     if (ADJ) enqueue_adj(L, ai, bj, code, n_inline, n_in);
-    else enqueue<WT, BATCH>(L, ms, ai, bj, code, h, n_inline, n_in);
+    else enqueue<WT, BATCH>(L, ms, ai, bj, code, h, n_inline, n_in, hs);
     return;
   }
   n_in++;
@@ -183,7 +183,7 @@ __device__ __forceinline__ void bin_pair(const fcfcg_launch &L,
     w = fix_prod(wa.x, __int_as_float(wa.y), pa.w, __float_as_int(bw.y), bw.z,
                  bw.x);
   }
-  hist_add<WT, BATCH>(L, ms, h, bin, w);
+  hist_add<WT, BATCH>(L, ms, h, bin, w, hs);
 }
 
 /* Is chunk point pa a candidate for the lane's neighbour (bx, by, bz):
@@ -303,6 +303,11 @@ k_count32(const fcfcg_launch L) {
   __shared__ uint32_t sh_blk;   /* next neighbour block of the chunk */
   __shared__ MockSh sh_mock;   /* batched launch: the current catalogue */
   __shared__ float sh_box[6];  /* the chunk points' bounding box (lo, hi) */
+  /* unweighted shared histogram: pairs added at most since the CTA last
+   * handed its bins to the global counters, and this chunk's mode (0 add,
+   * 1 hand over first, 2 count in global memory) */
+  __shared__ unsigned long long sh_hs_added;
+  __shared__ int sh_hs_mode;
   int cur = -1;
   uint16_t *fs = (uint16_t *) smem;
   uint16_t *fp = fs + L.nfs;
@@ -371,6 +376,7 @@ k_count32(const fcfcg_launch L) {
   const int4 *__restrict__ sten = (const int4 *) L.sten;
   const float4 *__restrict__ stD = (const float4 *) L.stenD;
   unsigned long long n_cand = 0, n_in64 = 0, n_q64 = 0, n_inline = 0;
+  if (threadIdx.x == 0) sh_hs_added = 0;
   const uint32_t nchunk = L.nchunk_dev ? __ldg(L.nchunk_dev) : L.nchunk;
 
   for (;;) {
@@ -402,6 +408,7 @@ k_count32(const fcfcg_launch L) {
             sh_mock.box[k] = M->box[k];
           }
           sh_mock.base = M->cell_base;
+          sh_hs_added = 0;
           sh_mock.g = WT ? M->gwt : M->gcnt;
           sh_mock.id = (uint32_t) mk;
         }
@@ -502,7 +509,27 @@ k_count32(const fcfcg_launch L) {
         }
         run += __shfl_sync(FULLMASK, inc, 31);
       }
-      if (lane == 0) S.pre[L.nsten] = run;
+      if (lane == 0) {
+        S.pre[L.nsten] = run;
+        /* the chunk adds at most m x total pairs to the u32 shared bins:
+         * hand them over first if the sum since the last hand-over could
+         * pass hs_limit (<= 2^32 - 1), or count in global memory if the
+         * chunk alone could */
+        if (!WT && !ADJ && L.hist_smem) {
+          const unsigned long long add = (unsigned long long) m * run;
+          int mode = 0;
+          if (add > L.hs_limit) {
+            mode = 2;
+          } else {
+            if (sh_hs_added + add > L.hs_limit) {
+              mode = 1;
+              sh_hs_added = 0;
+            }
+            sh_hs_added += add;
+          }
+          sh_hs_mode = mode;
+        }
+      }
     }
     __syncthreads();
     const uint32_t total = S.pre[L.nsten];
@@ -511,6 +538,15 @@ k_count32(const fcfcg_launch L) {
     const uint32_t pin = S.pre[L.nin];
     if (warp == 0 && lane == 0) n_cand += (unsigned long long) m * total;
     uint32_t n_in = 0, n_q = 0;
+    bool hs = L.hist_smem;
+    if (!WT && !ADJ && L.hist_smem) {
+      const int mode = sh_hs_mode;
+      if (mode == 1) {
+        hist_flush<WT>(L, h, BATCH ? sh_mock.g : L.gcnt);
+        __syncthreads();
+      }
+      hs = (mode != 2);
+    }
 
     /* the warps take the chunk's blocks of 32 neighbour points as they
      * become free (their work varies), so they reach the next chunk's
@@ -673,7 +709,7 @@ k_count32(const fcfcg_launch L) {
               bin_pair<GEOM, BIN, WT, BATCH, ADJ>(L, &sh_mock, S, ent, first,
                                                   cx, cy, cz, c2x, c2y, c2z,
                                                   fs, fp, fse, fpe, h, n_in,
-                                                  n_q, n_inline, gbv);
+                                                  n_q, n_inline, gbv, hs);
             }
           }
           __syncwarp();
@@ -745,7 +781,7 @@ k_count32(const fcfcg_launch L) {
             bin_pair<GEOM, BIN, WT, BATCH, ADJ>(L, &sh_mock, S, ent, first,
                                                 cx, cy, cz, c2x, c2y, c2z, fs,
                                                 fp, fse, fpe, h, n_in, n_q,
-                                                n_inline, gbv);
+                                                n_inline, gbv, hs);
           }
           if (ADJ) {
             /* the pass's entries run in neighbour order: sum each run of

@@ -324,18 +324,24 @@ __device__ __forceinline__ unsigned ftab_bin(const uint16_t *tab, int off,
 __device__ __forceinline__ int lin_bin(const fcfcg_launch &L, float s,
     bool &amb) {
   const float t = fmaf(s, L.lin_inv, L.lin_off);
-  const int k = __float2int_rd(t);
-  const float fr = t - (float) k;
   const float W = fmaf(L.lin_A, s, L.lin_B);
-  amb |= ((fr < W) & (k > L.lin_k0)) | (fr + W > 1.f);
+  /* an edge k > lin_k0 in [t - W, t + W]: the two ends fall in different
+   * bins (the window carries the rounding of t -+ W) */
+  const int lo = max(__float2int_rd(t - W), L.lin_k0);
+  const int k = __float2int_rd(t + W);
+  amb |= (lo != k);
   return k;
 }
 
-/* Integer bin of q = nmu * mu with error Eq; edges at every integer >= 1. */
+/* Integer bin of q = nmu * mu >= 0 with error Eq < 1/2; edges at every
+ * integer >= 1: one lies in [q - Eq, q + Eq] when the two ends truncate
+ * differently (the window carries the rounding of q -+ Eq; q - Eq > -1
+ * truncates to 0, so 0 is no edge).  q is finite: pairs with s^2 < tiny,
+ * the only ones whose q could be NaN, are ambiguous already. */
 __device__ __forceinline__ int mu_bin(float q, float Eq, bool &amb) {
-  int qi = __float2int_rz(q);
-  float fq = q - (float) qi;
-  amb |= ((qi > 0) & (fq <= Eq)) | (fq >= 1.f - Eq) | !(fq == fq);
+  const int lo = __float2int_rz(q - Eq);
+  const int qi = __float2int_rz(q + Eq);
+  amb |= (lo != qi);
   return qi;
 }
 
@@ -424,17 +430,21 @@ struct MockSh {
 };
 
 /* Histogram of the FP32 kernel in shared memory: ntot u32 counts, or
- * ntot u32 low words followed by ntot s32 high words for weighted sums.
- * Overflow goes to the global histogram of the current catalogue. */
+ * ntot u32 low words followed by ntot s32 high words for weighted sums
+ * (their overflow goes to the global histogram of the current catalogue).
+ * hs: the shared histogram takes the add.  Unweighted shared bins take it
+ * unchecked: the kernel hands them to the global counters before the adds
+ * since the last hand-over could pass 2^32 - 1, and a chunk that alone
+ * could (m x total pairs) counts in global memory (hs false). */
 template <int WT, int BATCH>
 __device__ __forceinline__ void hist_add(const fcfcg_launch &L,
-    const MockSh *ms, uint32_t *h, int bin, long long w) {
+    const MockSh *ms, uint32_t *h, int bin, long long w, bool hs) {
   unsigned long long *g = BATCH ? ms->g : (WT ? L.gwt : L.gcnt);
   if (WT) {
     if (L.hist_smem) hist_add_fix32(h, (int *) (h + L.ntot), g, bin, w);
     else add128(g + 2 * bin, w);
   } else {
-    if (L.hist_smem) hist_add_count(h, g, bin);
+    if (hs) atomicAdd(h + bin, 1u);
     else atomicAdd(g + bin, 1ull);
   }
 }
@@ -446,7 +456,7 @@ __device__ __forceinline__ void hist_add(const fcfcg_launch &L,
 template <int WT, int BATCH>
 __device__ __forceinline__ void enqueue(const fcfcg_launch &L,
     const MockSh *ms, uint32_t a, uint32_t b, uint32_t code, uint32_t *h,
-    unsigned long long &n_inline, uint32_t &n_in) {
+    unsigned long long &n_inline, uint32_t &n_in, bool hs) {
   const unsigned long long slot = atomicAdd(L.qcount, 1ull);
   if (slot < L.qcap) {
     *((uint4 *) L.queue + slot) = make_uint4(a, b, code, BATCH ? ms->id : 0u);
@@ -456,7 +466,7 @@ __device__ __forceinline__ void enqueue(const fcfcg_launch &L,
   int bin = ref_bin_pair(L, a, b, code, BATCH ? ms->box : L.box);
   if (bin < 0) return;
   n_in++;
-  hist_add<WT, BATCH>(L, ms, h, bin, WT ? fix_prod_pair(L, a, b) : 0);
+  hist_add<WT, BATCH>(L, ms, h, bin, WT ? fix_prod_pair(L, a, b) : 0, hs);
 }
 
 /*

@@ -73,6 +73,8 @@ struct fcfcg_ctx {
   /* FP32 kernel's warp queue: forced (fcfcg_set_warp_queue), or autotuned
    * for a key and weighting, else the launcher's choice; the last used */
   uint32_t qwarp_force, tuned_q, last_qwarp;
+  /* hand-over threshold of the unweighted shared histogram (0: 2^32 - 1) */
+  unsigned long long hs_limit;
   int tuned_q_key, tuned_q_wt;
   /* RA/Dec/z conversion scratch */
   void *d_cnvt;
@@ -349,6 +351,12 @@ int fcfcg_set_warp_queue(fcfcg_ctx *c, int entries) {
               entries == 1024))
     return FCFCG_ERR_ARG;
   c->qwarp_force = (uint32_t) entries;
+  return FCFCG_OK;
+}
+
+int fcfcg_set_hist_handover(fcfcg_ctx *c, unsigned long long pairs) {
+  if (!c || pairs > 0xFFFFFFFFull) return FCFCG_ERR_ARG;
+  c->hs_limit = pairs;
   return FCFCG_OK;
 }
 
@@ -954,10 +962,11 @@ static double ftab_cell_value(long c, int sh) {
  *    nmu dc / s, the root of s2 against s2_ref contributes q E / (2 s^2) =
  *    q (K2'/2 + K1 / (2 s) + K0' / (2 s^2)), q <= nmu.  So
  *      Eq = Q1 / s + Q2 q + Q0, Q1 = 1.25 nmu (dc + K1 / 2),
- *      Q2 = 1.25 (K2' / 2 + 2^-21 + 2 v), Q0 = 1e-6,
- *    the last covering nmu K0' / (2 s^2) <= 5e-7 (pairs with s^2 < tiny =
- *    1e6 K0' nmu are rechecked whatever their value) and the rounding of
- *    1 - Eq.
+ *      Q2 = 1.25 (K2' / 2 + 2^-21 + 2 v + 2 u), Q0 = 1e-6 + u,
+ *    the 1e-6 covering nmu K0' / (2 s^2) <= 5e-7 (pairs with s^2 < tiny =
+ *    1e6 K0' nmu are rechecked whatever their value); the kernel tests
+ *    the window's ends fl(q -+ Eq), each within u (q + Eq) of q -+ Eq
+ *    (Eq < 1/2): the 2 u of Q2 and the u of Q0.
  * 4. Survey mu and pi^2 use the line of sight m = x_a + x_b.  The kernel
  *    forms m = fl(fl(2 b + c2) + d) with b the neighbour's offset from the
  *    chunk cell's centre c and c2 = fl32(2 c) (the centre in FP64, rounded
@@ -974,8 +983,8 @@ static double ftab_cell_value(long c, int sh) {
  *    (dm 3u absolute, mm, the product, rsqrtf, two products: 8u relative)
  *    and the reference's (6 v nmu sabs / (2 R s), 4 v sabs / |m|^2):
  *      Q1 = 1.25 nmu (sqrt(3) dc + K1 / 2 + 3 v sabs / R),
- *      Q2 = 1.25 (K2' / 2 + 8 u + v sabs / R^2 + 2 v),
- *      Q0 = 1.25 nmu (3 u + 2 dmr) + 1e-6.
+ *      Q2 = 1.25 (K2' / 2 + 8 u + v sabs / R^2 + 2 v + 2 u),
+ *      Q0 = 1.25 nmu (3 u + 2 dmr) + 1e-6 + u (the ends, as in a box).
  *    pi^2 = (d.m)^2 / |m|^2: |d pi| <= sqrt(3) dc + s (2 dmr + 3u), so
  *      Ep = P2 s^2 + P1 s + P0, P1 = 1.25 (2 sqrt(3) dc + 6 v sabs / R),
  *      P2 = 1.25 (4 dmr + 14 u + 2 v sabs / R^2 + 2 v + u) (dm^2, mm and
@@ -1020,12 +1029,13 @@ static int fp32_bounds(const fcfcg_ctx *c, const grid_t *g, double dmax,
   L->m2min = box ? 0.f : (float) (2.01 * R * 2.01 * R);
   if (box) {
     L->Q1 = (float) (1.25 * nmu * (dc + 0.5 * K1));
-    L->Q2 = (float) (1.25 * (0.5 * K2a + ldexp(1.0, -21) + 2 * v));
-    L->Q0 = 1e-6f;
+    L->Q2 = (float) (1.25 * (0.5 * K2a + ldexp(1.0, -21) + 2 * v + 2 * u));
+    L->Q0 = (float) (1e-6 + u);
   } else {
     L->Q1 = (float) (1.25 * nmu * (s3 * dc + 0.5 * K1 + 3 * v * sabs / R));
-    L->Q2 = (float) (1.25 * (0.5 * K2a + 8 * u + v * sabs / (R * R) + 2 * v));
-    L->Q0 = (float) (1.25 * nmu * (3 * u + 2 * dmr) + 1e-6);
+    L->Q2 = (float) (1.25 * (0.5 * K2a + 8 * u + v * sabs / (R * R) + 2 * v +
+                             2 * u));
+    L->Q0 = (float) (1.25 * nmu * (3 * u + 2 * dmr) + 1e-6 + u);
   }
   double tiny = 1e6 * K0a * (nmu > 1 ? nmu : 1);
   if (tiny < 1e-20) tiny = 1e-20;
@@ -1042,9 +1052,10 @@ static int fp32_bounds(const fcfcg_ctx *c, const grid_t *g, double dmax,
    *   K2 s^2 + K1 s + K0 the bound on |s2_32 - s2_ref| above, and
    *   sqrt(s2_32) >= s_32 / (1 + eta), K0 / s <= K0 / sqrt(tiny);
    *   t = fl(fma(s, fl(1 / d), fl(-a / d))) adds u (s + a) / d + u |t|,
-   *   |t| <= ns + 1 where the window matters; fr = t - floor(t) adds u
-   *   (t < 0), and the tests fr < W and fr + W > 1 another u each.  The
-   *   factor 1.01 covers W's own FP32 evaluation.
+   *   |t| <= ns + 1 where the window matters; the kernel tests the ends
+   *   fl(t -+ W), each within u (|t| + W) <= u (ns + 2) of t -+ W (W <
+   *   0.45), plus 3 u of slack.  The factor 1.01 covers W's own FP32
+   *   evaluation.
    */
   L->slin = 0;
   if (b->bintype != FCFCG_BIN_SPI && b->s.tabtype == FCFCG_TAB_INT &&
@@ -1065,7 +1076,8 @@ static int fp32_bounds(const fcfcg_ctx *c, const grid_t *g, double dmax,
                                + uu) / d;
       const double Bw = 1.01 * (((double) L->K1 + (double) L->K0 /
                                  sqrt((double) L->tiny)) * (1 + eta) / d +
-                                uu * a / d + uu * (b->s.nbin + 1) + 3 * uu);
+                                uu * a / d + uu * (b->s.nbin + 1) +
+                                uu * (b->s.nbin + 2) + 3 * uu);
       const double smax = a + d * b->s.nbin;
       if (A * (smax + d) + Bw < 0.45) {
         L->slin = 1;
@@ -1374,6 +1386,7 @@ static int count_plan_make(fcfcg_ctx *c, slot_t *A, slot_t *B, int isauto,
     stage = 0;
   }
   L->hist_smem = (tabbytes + stage + hbytes <= 200 * 1024);
+  L->hs_limit = c->hs_limit ? c->hs_limit : 0xFFFFFFFFull;
   L->qwarp = c->qwarp_force ? c->qwarp_force
       : ((c->tuned_q && c->tuned_q_key == g->key && c->tuned_q_wt == withwt)
              ? c->tuned_q : 0);
@@ -2424,6 +2437,7 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
   }
   const size_t hbytes = (size_t) b->ntot * (withwt ? 8 : 4);
   L.hist_smem = (tabbytes + stage + hbytes <= 200 * 1024);
+  L.hs_limit = c->hs_limit ? c->hs_limit : 0xFFFFFFFFull;
   L.nsten = nsten;
   L.nin = nin;
   L.tzero = -1;

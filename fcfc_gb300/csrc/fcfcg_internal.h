@@ -171,6 +171,9 @@ typedef struct {
   unsigned long long *stats;   /* [0] candidates [1] in-range [2] recheck
                                   [3] inline rechecks */
   int hist_smem;               /* histogram in shared memory */
+  /* unweighted shared histogram: pairs a CTA adds between hand-overs to
+   * the global counters, at most 2^32 - 1 (u32 bins) */
+  unsigned long long hs_limit;
   /* batch of catalogues (NULL: one catalogue pair): chunk .w is the
    * catalogue, queue entries carry it too */
   const fcfcg_mock *mocks;

@@ -197,6 +197,11 @@ class PairCounter:
         1024; 0 automatic)."""
         self._check(self.lib.fcfcg_set_warp_queue(self.h, int(entries)))
 
+    def set_hist_handover(self, pairs: int):
+        """Hand-over threshold of the FP32 kernel's unweighted shared
+        histogram (1..2^32 - 1; 0 default); the counts do not change."""
+        self._check(self.lib.fcfcg_set_hist_handover(self.h, int(pairs)))
+
     def set_queue_capacity(self, cap: int):
         """Limit the FP64 recheck queue (pairs beyond are binned inside the
         counting kernel; the counts do not change)."""

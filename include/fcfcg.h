@@ -368,6 +368,15 @@ int fcfcg_set_warp_queue(fcfcg_ctx *ctx, int entries);
  * tests of that overflow path. */
 int fcfcg_set_queue_capacity(fcfcg_ctx *ctx, size_t cap);
 
+/* Unweighted counts in the FP32 kernel: a CTA's shared-memory bins are 32
+ * bits wide and take their adds unchecked, so the CTA hands them to the
+ * global 64-bit counters before the pairs it may have added since the last
+ * hand-over (a chunk of m points with t neighbour points adds at most m t)
+ * could pass this threshold, and counts a chunk that alone could pass it
+ * in global memory.  1..2^32 - 1, or 0 (default) for 2^32 - 1.  The counts
+ * do not depend on it; meant for tests of those two paths. */
+int fcfcg_set_hist_handover(fcfcg_ctx *ctx, unsigned long long pairs);
+
 /*
  * Autotune the grid refinement and the kernel's tile for this binning and
  * catalogue pair: times the FP32 count at 1..8 cells per maximum

@@ -131,3 +131,35 @@ def test_warp_queue_sizes(weighted):
     pc.autotune(0, weighted=weighted)
     pc.count_pairs(0, weighted=weighted)
     assert pc.stats()["warp_queue"] in (256, 512, 1024)
+
+
+def test_shared_histogram_handover():
+    """Unweighted FP32 counts: a CTA's 32-bit shared bins take their adds
+    unchecked and are handed to the global counters before the pairs added
+    since the last hand-over could pass the threshold
+    (fcfcg_set_hist_handover, default 2^32 - 1); a chunk that alone could
+    pass it counts in global memory.  Small thresholds force both paths --
+    every chunk global (1), a mix (5000), frequent hand-overs (10^6) --
+    for one catalogue and for a batch: the counts never change."""
+    import fcfc_gb300 as fg
+    from fcfc_gb300 import synth
+    x = synth.neyman_scott(40, 200.0, 300, 1.5, seed=93)
+    pc = fg.PairCounter("box", fg.BIN_SMU, box=200.0, smin=0, smax=30, ds=1,
+                        nmu=30)
+    pc.load(0, x)
+    want = fo.Bins(False, 1, ns=30, smin=0, ds=1, nmu=30,
+                   box=200.0).count(x, mode=1)
+    np.testing.assert_array_equal(pc.count_pairs(0), want)
+    cats = [synth.neyman_scott(30, 200.0, 200, 2.0, seed=94 + k)
+            for k in range(3)]
+    ref, status, _ = pc.count_batch(cats, [200.0] * 3)
+    assert list(status) == [0, 0, 0]
+    for limit in (1, 5000, 10 ** 6, 0):
+        pc.set_hist_handover(limit)
+        np.testing.assert_array_equal(pc.count_pairs(0), want)
+        assert pc.stats()["precision_used"] == fg.PREC_FP32_RECHECK
+        got, status, _ = pc.count_batch(cats, [200.0] * 3)
+        for g, r in zip(got, ref):
+            np.testing.assert_array_equal(g, r)
+    with pytest.raises(fg.FCFCGError):
+        pc.set_hist_handover(2 ** 32)
