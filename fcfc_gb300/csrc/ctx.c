@@ -48,6 +48,8 @@ struct fcfcg_ctx {
   /* shared scratch */
   uint32_t *cfill, *scan_tmp, *cchunk, *chunks;
   size_t cfill_cap, scan_cap, cchunk_cap, chunk_cap;
+  uint32_t *fstart;               /* fine (sub-cell) starts of a grid sort */
+  size_t fstart_cap;
   uint16_t *d_fs, *d_fp, *d_rs, *d_rp;
   float *d_fse, *d_fpe;
   double *d_s2edge, *d_pedge;
@@ -197,7 +199,7 @@ void fcfcg_destroy(fcfcg_ctx *c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (int i = 0; i <= FCFCG_MAX_SLOT; i++) slot_free(c->slot + i);
-    void *p[] = {c->cfill, c->scan_tmp, c->cchunk, c->chunks, c->d_fse,
+    void *p[] = {c->cfill, c->fstart, c->scan_tmp, c->cchunk, c->chunks, c->d_fse,
                  c->d_fpe, c->d_fs,
                  c->d_fp, c->d_rs, c->d_rp, c->d_s2edge, c->d_pedge,
                  c->d_sten, c->d_stenD, c->d_cnt, c->d_wt, c->d_stats,
@@ -892,8 +894,10 @@ static int slot_reserve(fcfcg_ctx *c, slot_t *s, const grid_t *g) {
     CK(cudaMalloc((void **) &s->cstart, sizeof(uint32_t) * (nc + 1)));
     s->ccap = nc + 1;
   }
-  GROW(c->cfill, c->cfill_cap, sizeof(uint32_t) * (nc + 1));
-  size_t st = fcfcg_scan_tmp_len(nc + 1) + 16;
+  const size_t nf = nc << fcfcg_grid_sub_bits(nc, n);
+  GROW(c->cfill, c->cfill_cap, sizeof(uint32_t) * (nf + 1));
+  GROW(c->fstart, c->fstart_cap, sizeof(uint32_t) * (nf + 1));
+  size_t st = fcfcg_scan_tmp_len(nf + 1) + 16;
   GROW(c->scan_tmp, c->scan_cap, sizeof(uint32_t) * st);
   return FCFCG_OK;
 }
@@ -902,14 +906,15 @@ static int slot_reserve(fcfcg_ctx *c, slot_t *s, const grid_t *g) {
 static int slot_sort(fcfcg_ctx *c, slot_t *s, const grid_t *g) {
   const size_t nc = (size_t) g->n[0] * g->n[1] * g->n[2];
   const size_t n = s->n;
-  size_t st = fcfcg_scan_tmp_len(nc + 1) + 16;
+  const int sb = fcfcg_grid_sub_bits(nc, n);
+  size_t st = fcfcg_scan_tmp_len((nc << sb) + 1) + 16;
   const int survey = (c->bins.geometry == FCFCG_GEOM_SURVEY);
   CKK(fcfcg_k_grid(c->stream, n, s->x, s->y, s->z, survey ? s->s : NULL,
-                   s->w, s->has_w, s->wexp, g->n, g->cw, g->lo, s->cell_of,
-                   s->cstart, c->cfill, c->scan_tmp, st, s->l4, s->wq,
-                   s->sx, s->sy, s->sz, survey ? s->ss : NULL, s->sw,
-                   s->sid));
-  c->launches += n ? 5 : 3;
+                   s->w, s->has_w, s->wexp, g->n, g->cw, g->lo, sb,
+                   s->cell_of, s->cstart, c->fstart, c->cfill, c->scan_tmp,
+                   st, s->l4, s->wq, s->sx, s->sy, s->sz,
+                   survey ? s->ss : NULL, s->sw, s->sid));
+  c->launches += n ? 6 : 4;
   return FCFCG_OK;
 }
 
@@ -2365,24 +2370,30 @@ int fcfcg_count_batch(fcfcg_ctx *c, fcfcg_job *jobs, int njobs, int withwt,
     }
     S->ccap = cells + 1;
   }
-  BGROW(c->cfill, c->cfill_cap, sizeof(uint32_t) * (cells + 1));
-  const size_t stl = fcfcg_scan_tmp_len(cells + 1) + 16;
+  /* fine counters: cells x sub-cells (the points of a cell grouped by
+   * sub-cell in the sorted arrays) */
+  const int sb = fcfcg_grid_sub_bits(cells, N);
+  const size_t nf = cells << sb;
+  BGROW(c->cfill, c->cfill_cap, sizeof(uint32_t) * (nf + 1));
+  BGROW(c->fstart, c->fstart_cap, sizeof(uint32_t) * (nf + 1));
+  const size_t stl = fcfcg_scan_tmp_len(nf + 1) + 16;
   BGROW(c->scan_tmp, c->scan_cap, sizeof(uint32_t) * stl);
-  BCK(cudaMemsetAsync(c->cfill, 0, sizeof(uint32_t) * (cells + 1), c->stream));
+  BCK(cudaMemsetAsync(c->cfill, 0, sizeof(uint32_t) * (nf + 1), c->stream));
   /* the table again, with the grids (the stream is idle: the range checks
    * synchronised it) */
   BCK(cudaMemcpyAsync(c->d_pcat, P, sizeof(fcfcg_prep_cat) * na,
                       cudaMemcpyHostToDevice, c->stream));
   BCKK(fcfcg_k_cell_batch(c->stream, (const fcfcg_prep_cat *) c->d_pcat, na,
-                          ntile, S->x, S->y, S->z, S->cell_of, c->cfill));
-  BCKK(fcfcg_scan(c->stream, c->cfill, cells, S->cstart, c->scan_tmp));
-  BCK(cudaMemsetAsync(c->cfill, 0, sizeof(uint32_t) * (cells + 1), c->stream));
+                          ntile, sb, S->x, S->y, S->z, S->cell_of, c->cfill));
+  BCKK(fcfcg_scan(c->stream, c->cfill, nf, c->fstart, c->scan_tmp));
+  BCKK(fcfcg_k_cstart(c->stream, cells, sb, c->fstart, S->cstart));
+  BCK(cudaMemsetAsync(c->cfill, 0, sizeof(uint32_t) * (nf + 1), c->stream));
   BCKK(fcfcg_k_scatter_batch(c->stream, (const fcfcg_prep_cat *) c->d_pcat,
-                             na, ntile, S->x, S->y, S->z,
+                             na, ntile, sb, S->x, S->y, S->z,
                              withwt ? S->w : NULL, withwt, S->cell_of,
-                             S->cstart, c->cfill, S->l4, S->wq, S->sx, S->sy,
+                             c->fstart, c->cfill, S->l4, S->wq, S->sx, S->sy,
                              S->sz, S->sw, S->sid));
-  c->launches += 5;
+  c->launches += 6;
   /* 6. per-catalogue histograms and the catalogue table */
   const size_t per = (size_t) b->ntot * (withwt ? 2 : 1);
   BGROW(c->d_bout, c->d_bout_cap, sizeof(unsigned long long) * per * na);

@@ -198,12 +198,23 @@ int fcfcg_k_prep(void *stream, size_t n, const double *x, const double *y,
     double *ox, double *oy, double *oz, double *os, double *ow,
     unsigned long long *wmax_bits, double *partial, double *wsum);
 size_t fcfcg_prep_partials(void);
+/* Sub-cell bits of a grid of ncell cells holding npoint points: 6 (4 x 4
+ * x 4 sub-cells in Morton order within a cell), 3 (2 x 2 x 2) or 0; the
+ * sort then uses (ncell << sb) fine counters. */
+int fcfcg_grid_sub_bits(size_t ncell, size_t npoint);
+/* Counting sort into the grid, cells in order and, within a cell, by
+ * sub-cell (sb bits); cstart[0..nc] the cells' first sorted points.
+ * Scratch: cell_of (n), fstart and cfill ((nc << sb) + 1 each), scan_tmp
+ * (fcfcg_scan_tmp_len((nc << sb) + 1)). */
 int fcfcg_k_grid(void *stream, size_t n, const double *x, const double *y,
     const double *z, const double *s, const double *w, int has_w, int wexp,
-    const int ncell[3], const double cw[3], const double lo[3],
-    uint32_t *cell_of, uint32_t *cstart, uint32_t *cfill, uint32_t *scan_tmp,
-    size_t scan_tmp_len, float *l4, int *wq, double *sx, double *sy,
-    double *sz, double *ss, double *sw, uint32_t *sid);
+    const int ncell[3], const double cw[3], const double lo[3], int sb,
+    uint32_t *cell_of, uint32_t *cstart, uint32_t *fstart, uint32_t *cfill,
+    uint32_t *scan_tmp, size_t scan_tmp_len, float *l4, int *wq, double *sx,
+    double *sy, double *sz, double *ss, double *sw, uint32_t *sid);
+/* cstart[c] = fstart[c << sb] for c = 0..nc. */
+int fcfcg_k_cstart(void *stream, size_t nc, int sb, const uint32_t *fstart,
+    uint32_t *cstart);
 int fcfcg_k_chunks(void *stream, const uint32_t *cstart, uint32_t ncell,
     uint32_t clen, uint32_t *cchunk, uint32_t *scan_tmp, size_t scan_tmp_len,
     uint32_t *chunks, uint32_t *nchunk_out, const uint32_t *mock_cell_base,
@@ -231,17 +242,18 @@ size_t fcfcg_batch_tile(void);
 int fcfcg_k_prep_batch(void *stream, const fcfcg_prep_cat *d_cat, int ncat,
     uint32_t ntile, double rescale, int withwt, double *ox, double *oy,
     double *oz, double *ow, unsigned long long *bstat, double *partial);
-/* Batch grid: every live catalogue's cells numbered from its cell_base into
- * a shared cell-count array (k_cell_batch), and its points scattered into
- * the shared sorted arrays after the global scan (k_scatter_batch); the id
- * of slot point i is i. */
+/* Batch grid: every live catalogue's fine indices (cell numbered from its
+ * cell_base, shifted by sb, with the sub-cell) counted into a shared array
+ * (k_cell_batch), and its points scattered into the shared sorted arrays
+ * after the global scan of the fine counts (k_scatter_batch); the id of
+ * slot point i is i. */
 int fcfcg_k_cell_batch(void *stream, const fcfcg_prep_cat *d_cat, int ncat,
-    uint32_t ntile, const double *x, const double *y, const double *z,
-    uint32_t *cell_of, uint32_t *count);
+    uint32_t ntile, int sb, const double *x, const double *y,
+    const double *z, uint32_t *cell_of, uint32_t *count);
 int fcfcg_k_scatter_batch(void *stream, const fcfcg_prep_cat *d_cat,
-    int ncat, uint32_t ntile, const double *x, const double *y,
+    int ncat, uint32_t ntile, int sb, const double *x, const double *y,
     const double *z, const double *w, int has_w, const uint32_t *cell_of,
-    const uint32_t *cstart, uint32_t *cfill, float *l4, int *wq, double *sx,
+    const uint32_t *fstart, uint32_t *cfill, float *l4, int *wq, double *sx,
     double *sy, double *sz, double *sw, uint32_t *sid);
 /* out[sid[p]] = in[p] for p < n (sorted order back to input order). */
 int fcfcg_k_unsort(void *stream, size_t n, const uint32_t *sid,

@@ -251,32 +251,49 @@ static int scan_u32(cudaStream_t s, const uint32_t *in, size_t n,
 /* ------------------------------------------------------------------------ */
 /* Cell grid.                                                               */
 
-__device__ __forceinline__ int cell_axis(double v, double lo, double cw,
-    int n) {
-  double t = floor((v - lo) / cw);
-  int c = (t < 0) ? 0 : (t >= n ? n - 1 : (int) t);
-  return c;
-}
-
-/* The global cell of a point (cells of one grid numbered from cell_base). */
-__device__ __forceinline__ uint32_t cell_of_point(double a, double b,
+/*
+ * The fine index of a point: its global cell (cells of one grid numbered
+ * from cell_base), shifted left by sb, and with sb = 3 or 6 its sub-cell
+ * (2 or 4 per axis) in Morton order.  Sorting by the fine index keeps each
+ * cell's points contiguous and, within the cell, groups them by sub-cell,
+ * so that runs of 32 or 64 consecutive points (the count kernel's
+ * neighbour blocks and chunks) are compact.  The cell of an axis is
+ * floor((v - lo) / cw) clamped to [0, n).
+ */
+__device__ __forceinline__ uint32_t fine_of_point(double a, double b,
     double d, int nx, int ny, int nz, double cwx, double cwy, double cwz,
-    double lox, double loy, double loz, uint32_t cell_base) {
-  int cx = cell_axis(a, lox, cwx, nx);
-  int cy = cell_axis(b, loy, cwy, ny);
-  int cz = cell_axis(d, loz, cwz, nz);
-  return cell_base + ((uint32_t) cz * ny + cy) * nx + cx;
+    double lox, double loy, double loz, uint32_t cell_base, int sb) {
+  const double v[3] = {a, b, d}, lo[3] = {lox, loy, loz},
+               cw[3] = {cwx, cwy, cwz};
+  const int n[3] = {nx, ny, nz};
+  const int r = sb / 3;                   /* bits per axis */
+  int c[3];
+  uint32_t m = 0;
+  for (int k = 0; k < 3; k++) {
+    const double q = (v[k] - lo[k]) / cw[k];
+    const double t = floor(q);
+    c[k] = (t < 0) ? 0 : (t >= n[k] ? n[k] - 1 : (int) t);
+    if (r) {
+      const int lim = (1 << r) - 1;
+      int s = (int) floor((q - (double) c[k]) * (double) (1 << r));
+      s = s < 0 ? 0 : (s > lim ? lim : s);
+      for (int bit = 0; bit < r; bit++)
+        m |= (uint32_t) ((s >> bit) & 1) << (3 * bit + k);
+    }
+  }
+  const uint32_t cell = cell_base + ((uint32_t) c[2] * ny + c[1]) * nx + c[0];
+  return (cell << sb) | m;
 }
 
 __global__ void k_cell(size_t n, const double *__restrict__ x,
     const double *__restrict__ y, const double *__restrict__ z, int nx,
     int ny, int nz, double cwx, double cwy, double cwz, double lox,
-    double loy, double loz, uint32_t cell_base, uint32_t *__restrict__ cell_of,
-    uint32_t *__restrict__ count) {
+    double loy, double loz, uint32_t cell_base, int sb,
+    uint32_t *__restrict__ cell_of, uint32_t *__restrict__ count) {
   for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n;
        i += (size_t) gridDim.x * blockDim.x) {
-    uint32_t c = cell_of_point(x[i], y[i], z[i], nx, ny, nz, cwx, cwy, cwz,
-                               lox, loy, loz, cell_base);
+    uint32_t c = fine_of_point(x[i], y[i], z[i], nx, ny, nz, cwx, cwy, cwz,
+                               lox, loy, loz, cell_base, sb);
     cell_of[i] = c;
     atomicAdd(count + c, 1u);
   }
@@ -320,52 +337,82 @@ __global__ void k_scatter(size_t n, const double *__restrict__ x,
     const double *__restrict__ y, const double *__restrict__ z,
     const double *__restrict__ s, const double *__restrict__ w, int has_w,
     int wexp, int nx, int ny, double cwx, double cwy, double cwz, double lox,
-    double loy, double loz, uint32_t cell_base, uint32_t id_base,
+    double loy, double loz, uint32_t cell_base, uint32_t id_base, int sb,
     const uint32_t *__restrict__ cell_of,
-    const uint32_t *__restrict__ cstart, uint32_t *__restrict__ cfill,
+    const uint32_t *__restrict__ fstart, uint32_t *__restrict__ cfill,
     float4 *__restrict__ l4, int2 *__restrict__ wq, double *__restrict__ sx,
     double *__restrict__ sy, double *__restrict__ sz, double *__restrict__ ss,
     double *__restrict__ sw, uint32_t *__restrict__ sid) {
   for (size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n;
        i += (size_t) gridDim.x * blockDim.x) {
-    uint32_t c = cell_of[i];
-    uint32_t pos = cstart[c] + atomicAdd(cfill + c, 1u);
-    scatter_point(c, pos, x[i], y[i], z[i], has_w ? w[i] : 1.0, wexp, nx, ny,
+    const uint32_t f = cell_of[i];
+    uint32_t pos = fstart[f] + atomicAdd(cfill + f, 1u);
+    scatter_point(f >> sb, pos, x[i], y[i], z[i], has_w ? w[i] : 1.0, wexp, nx, ny,
                   cwx, cwy, cwz, lox, loy, loz, cell_base,
                   id_base + (uint32_t) i, l4, wq, sx, sy, sz, sw, sid);
     if (ss) ss[pos] = s[i];
   }
 }
 
+/* cstart[c] = fstart[c << sb], c = 0..nc: the cells' first sorted points
+ * from the fine (sub-cell) starts. */
+__global__ void k_cstart(size_t nc, int sb, const uint32_t *__restrict__ fstart,
+    uint32_t *__restrict__ cstart) {
+  for (size_t c = blockIdx.x * (size_t) blockDim.x + threadIdx.x; c <= nc;
+       c += (size_t) gridDim.x * blockDim.x)
+    cstart[c] = fstart[c << sb];
+}
+
+extern "C" int fcfcg_grid_sub_bits(size_t ncell, size_t npoint) {
+  /* sub-cells where cells hold many points on average, with the fine
+   * counters at most ~4 per point (and 32-bit fine indices) */
+  const size_t lim = npoint * 4 > ((size_t) 1 << 22) ? npoint * 4
+                                                   : ((size_t) 1 << 22);
+  if (ncell << 6 <= lim && (ncell << 6) < 0xFFFFFFF0u) return 6;
+  if (ncell << 3 <= lim && (ncell << 3) < 0xFFFFFFF0u) return 3;
+  return 0;
+}
+
 extern "C" int fcfcg_k_grid(void *stream, size_t n, const double *x,
     const double *y, const double *z, const double *s, const double *w,
     int has_w, int wexp, const int ncell[3], const double cw[3],
-    const double lo[3], uint32_t *cell_of, uint32_t *cstart, uint32_t *cfill,
-    uint32_t *scan_tmp, size_t scan_tmp_len, float *l4, int *wq,
-    double *sx, double *sy, double *sz, double *ss, double *sw,
-    uint32_t *sid) {
+    const double lo[3], int sb, uint32_t *cell_of, uint32_t *cstart,
+    uint32_t *fstart, uint32_t *cfill, uint32_t *scan_tmp,
+    size_t scan_tmp_len, float *l4, int *wq, double *sx, double *sy,
+    double *sz, double *ss, double *sw, uint32_t *sid) {
   cudaStream_t st = (cudaStream_t) stream;
-  size_t nc = (size_t) ncell[0] * ncell[1] * ncell[2];
+  const size_t nc = (size_t) ncell[0] * ncell[1] * ncell[2];
+  const size_t nf = nc << sb;
   (void) scan_tmp_len;
-  cudaError_t e = cudaMemsetAsync(cfill, 0, sizeof(uint32_t) * nc, st);
+  cudaError_t e = cudaMemsetAsync(cfill, 0, sizeof(uint32_t) * nf, st);
   if (e) return (int) e;
   if (n) {
     k_cell<<<grid_for(n, PREP_THREADS), PREP_THREADS, 0, st>>>(
         n, x, y, z, ncell[0], ncell[1], ncell[2], cw[0], cw[1], cw[2], lo[0],
-        lo[1], lo[2], 0u, cell_of, cfill);
+        lo[1], lo[2], 0u, sb, cell_of, cfill);
     if ((e = cudaGetLastError())) return (int) e;
   }
-  int r = scan_u32(st, cfill, nc, cstart, scan_tmp);
+  int r = scan_u32(st, cfill, nf, fstart, scan_tmp);
   if (r) return r;
-  if ((e = cudaMemsetAsync(cfill, 0, sizeof(uint32_t) * nc, st))) return (int) e;
+  k_cstart<<<grid_for(nc + 1, PREP_THREADS), PREP_THREADS, 0, st>>>(
+      nc, sb, fstart, cstart);
+  if ((e = cudaGetLastError())) return (int) e;
+  if ((e = cudaMemsetAsync(cfill, 0, sizeof(uint32_t) * nf, st))) return (int) e;
   if (n) {
     k_scatter<<<grid_for(n, PREP_THREADS), PREP_THREADS, 0, st>>>(
         n, x, y, z, s, w, has_w, wexp, ncell[0], ncell[1], cw[0], cw[1],
-        cw[2], lo[0], lo[1], lo[2], 0u, 0u, cell_of, cstart, cfill,
+        cw[2], lo[0], lo[1], lo[2], 0u, 0u, sb, cell_of, fstart, cfill,
         (float4 *) l4, (int2 *) wq, sx, sy, sz, ss, sw, sid);
     if ((e = cudaGetLastError())) return (int) e;
   }
   return 0;
+}
+
+extern "C" int fcfcg_k_cstart(void *stream, size_t nc, int sb,
+    const uint32_t *fstart, uint32_t *cstart) {
+  k_cstart<<<grid_for(nc + 1, PREP_THREADS), PREP_THREADS, 0,
+             (cudaStream_t) stream>>>(nc, sb, fstart, cstart);
+  return (int) cudaGetLastError();
 }
 
 extern "C" int fcfcg_scan(void *stream, const uint32_t *in, size_t n,
@@ -507,7 +554,7 @@ extern "C" int fcfcg_k_prep_batch(void *stream, const fcfcg_prep_cat *d_cat,
 /* Cells of every live catalogue's points (slot arrays x, y, z), numbered
  * from the catalogue's cell_base into the shared count array. */
 __global__ void __launch_bounds__(PREP_THREADS) k_cell_batch(
-    const fcfcg_prep_cat *__restrict__ cat, int ncat,
+    const fcfcg_prep_cat *__restrict__ cat, int ncat, int sb,
     const double *__restrict__ x, const double *__restrict__ y,
     const double *__restrict__ z, uint32_t *__restrict__ cell_of,
     uint32_t *__restrict__ count) {
@@ -521,8 +568,8 @@ __global__ void __launch_bounds__(PREP_THREADS) k_cell_batch(
   const double cwx = C->cw[0], cwy = C->cw[1], cwz = C->cw[2];
   const uint32_t base = C->cell_base;
   for (size_t i = o + i0 + threadIdx.x; i < o + i1; i += PREP_THREADS) {
-    const uint32_t c = cell_of_point(x[i], y[i], z[i], nx, ny, nz, cwx, cwy,
-                                     cwz, 0.0, 0.0, 0.0, base);
+    const uint32_t c = fine_of_point(x[i], y[i], z[i], nx, ny, nz, cwx, cwy,
+                                     cwz, 0.0, 0.0, 0.0, base, sb);
     cell_of[i] = c;
     atomicAdd(count + c, 1u);
   }
@@ -531,11 +578,11 @@ __global__ void __launch_bounds__(PREP_THREADS) k_cell_batch(
 /* Every live catalogue's points to their sorted places (as k_scatter); the
  * id of point i of the slot is i. */
 __global__ void __launch_bounds__(PREP_THREADS) k_scatter_batch(
-    const fcfcg_prep_cat *__restrict__ cat, int ncat,
+    const fcfcg_prep_cat *__restrict__ cat, int ncat, int sb,
     const double *__restrict__ x, const double *__restrict__ y,
     const double *__restrict__ z, const double *__restrict__ w, int has_w,
     const uint32_t *__restrict__ cell_of,
-    const uint32_t *__restrict__ cstart, uint32_t *__restrict__ cfill,
+    const uint32_t *__restrict__ fstart, uint32_t *__restrict__ cfill,
     float4 *__restrict__ l4, int2 *__restrict__ wq, double *__restrict__ sx,
     double *__restrict__ sy, double *__restrict__ sz, double *__restrict__ sw,
     uint32_t *__restrict__ sid) {
@@ -549,32 +596,32 @@ __global__ void __launch_bounds__(PREP_THREADS) k_scatter_batch(
   const double cwx = C->cw[0], cwy = C->cw[1], cwz = C->cw[2];
   const uint32_t base = C->cell_base;
   for (size_t i = o + i0 + threadIdx.x; i < o + i1; i += PREP_THREADS) {
-    const uint32_t c = cell_of[i];
-    const uint32_t pos = cstart[c] + atomicAdd(cfill + c, 1u);
-    scatter_point(c, pos, x[i], y[i], z[i], has_w ? w[i] : 1.0, wexp, nx, ny,
+    const uint32_t f = cell_of[i];
+    const uint32_t pos = fstart[f] + atomicAdd(cfill + f, 1u);
+    scatter_point(f >> sb, pos, x[i], y[i], z[i], has_w ? w[i] : 1.0, wexp, nx, ny,
                   cwx, cwy, cwz, 0.0, 0.0, 0.0, base, (uint32_t) i, l4, wq,
                   sx, sy, sz, sw, sid);
   }
 }
 
 extern "C" int fcfcg_k_cell_batch(void *stream, const fcfcg_prep_cat *d_cat,
-    int ncat, uint32_t ntile, const double *x, const double *y,
+    int ncat, uint32_t ntile, int sb, const double *x, const double *y,
     const double *z, uint32_t *cell_of, uint32_t *count) {
   if (!ncat || !ntile) return 0;
   k_cell_batch<<<ntile, PREP_THREADS, 0, (cudaStream_t) stream>>>(
-      d_cat, ncat, x, y, z, cell_of, count);
+      d_cat, ncat, sb, x, y, z, cell_of, count);
   return (int) cudaGetLastError();
 }
 
 extern "C" int fcfcg_k_scatter_batch(void *stream,
-    const fcfcg_prep_cat *d_cat, int ncat, uint32_t ntile, const double *x,
-    const double *y, const double *z, const double *w, int has_w,
-    const uint32_t *cell_of, const uint32_t *cstart, uint32_t *cfill,
-    float *l4, int *wq, double *sx, double *sy, double *sz, double *sw,
-    uint32_t *sid) {
+    const fcfcg_prep_cat *d_cat, int ncat, uint32_t ntile, int sb,
+    const double *x, const double *y, const double *z, const double *w,
+    int has_w, const uint32_t *cell_of, const uint32_t *fstart,
+    uint32_t *cfill, float *l4, int *wq, double *sx, double *sy, double *sz,
+    double *sw, uint32_t *sid) {
   if (!ncat || !ntile) return 0;
   k_scatter_batch<<<ntile, PREP_THREADS, 0, (cudaStream_t) stream>>>(
-      d_cat, ncat, x, y, z, w, has_w, cell_of, cstart, cfill, (float4 *) l4,
+      d_cat, ncat, sb, x, y, z, w, has_w, cell_of, fstart, cfill, (float4 *) l4,
       (int2 *) wq, sx, sy, sz, sw, sid);
   return (int) cudaGetLastError();
 }
