@@ -234,6 +234,93 @@ __device__ __forceinline__ void candidate2(const fcfcg_launch &L, float4 pxy,
   }
 }
 
+/* Binnings whose direct blocks (every pair a candidate) take the packed
+ * path below: boxes with linear s bins. */
+#define PACKED_DIRECT(G, B) ((G) == FCFCG_GEOM_BOX && LINS(B))
+
+/*
+ * A direct block of a box with linear s bins: the lane's neighbour (bx, by,
+ * bz; sorted index bj) against every chunk point, two chunk points per step
+ * (pxy = (x, x', y, y'), pz = (z, z')).  Packed FP32 operations round each
+ * component as bin_pair's scalar ones do (q - Eq and t - W are formed as
+ * fma(-1, Eq, q) and fma(-1, W, t), fl(q |dz| ...) as |fl(q dz ...)|: the
+ * same roundings), so every pair gets bin_pair's bin and ambiguity bit for
+ * bit; the neighbour's point, weight and index stay in the lane's
+ * registers.
+ */
+template <int BIN, int WT, int BATCH>
+__device__ __forceinline__ void bin_direct2(const fcfcg_launch &L,
+    const MockSh *ms, const Stage &S, int m, uint32_t first, int cx, int cy,
+    int cz, float bx, float by, float bz, uint32_t bj, int lane, uint32_t *h,
+    uint32_t &n_in, uint32_t &n_q, unsigned long long &n_inline, bool hs) {
+  const float2 nbx = make_float2(-bx, -bx), nby = make_float2(-by, -by),
+               nbz = make_float2(-bz, -bz);
+  const float2 m1 = make_float2(-1.f, -1.f);
+  float4 bw = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (WT) bw = S.bw[lane];
+  for (int k = 0; k < m; k += 2) {
+    const float4 pxy = S.pxy[k >> 1];
+    const float2 dx = __fadd2_rn(make_float2(pxy.x, pxy.y), nbx);
+    const float2 dy = __fadd2_rn(make_float2(pxy.z, pxy.w), nby);
+    const float2 dz = __fadd2_rn(S.pz[k >> 1], nbz);
+    const float2 s2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+    const float2 rs = make_float2(rsqrtf(s2.x), rsqrtf(s2.y));
+    const float2 s = __fmul2_rn(s2, rs);
+    int qi[2] = {0, 0}, kb[2], klo[2];
+    bool amb[2] = {!(s2.x >= L.tiny), !(s2.y >= L.tiny)};
+    if (IS_SMU(BIN)) {
+      float2 q = __fmul2_rn(__fmul2_rn(make_float2(L.fnmu, L.fnmu), dz), rs);
+      q = make_float2(fabsf(q.x), fabsf(q.y));
+      const float2 Eq = __ffma2_rn(make_float2(L.Q1, L.Q1), rs,
+          __ffma2_rn(make_float2(L.Q2, L.Q2), q, make_float2(L.Q0, L.Q0)));
+      const float2 qlo = __ffma2_rn(m1, Eq, q);
+      const float2 qhi = __fadd2_rn(q, Eq);
+      qi[0] = __float2int_rz(qhi.x);
+      qi[1] = __float2int_rz(qhi.y);
+      amb[0] |= (__float2int_rz(qlo.x) != qi[0]);
+      amb[1] |= (__float2int_rz(qlo.y) != qi[1]);
+    }
+    const float2 t = __ffma2_rn(s, make_float2(L.lin_inv, L.lin_inv),
+                                make_float2(L.lin_off, L.lin_off));
+    const float2 W = __ffma2_rn(make_float2(L.lin_A, L.lin_A), s,
+                                make_float2(L.lin_B, L.lin_B));
+    const float2 tlo = __ffma2_rn(m1, W, t);
+    const float2 thi = __fadd2_rn(t, W);
+    kb[0] = __float2int_rd(thi.x);
+    kb[1] = __float2int_rd(thi.y);
+    klo[0] = max(__float2int_rd(tlo.x), L.lin_k0);
+    klo[1] = max(__float2int_rd(tlo.y), L.lin_k0);
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      if (k + e >= m) break;
+      const bool a = amb[e] | (klo[e] != kb[e]);
+      const uint32_t ai = first + (uint32_t) (k + e);
+      if (a) {
+        n_q++;
+        const uint32_t code = nb_code(BATCH ? ms->nc : L.ncell, cx, cy, cz,
+            __ldg((const int4 *) L.sten + S.bt[lane]));
+        enqueue<WT, BATCH>(L, ms, ai, bj, code, h, n_inline, n_in, hs);
+        continue;
+      }
+      int q = qi[e];
+      if (IS_SMU(BIN) && q >= L.nmu) {
+        if (!L.mu_one) continue;
+        q = L.nmu - 1;
+      }
+      if ((unsigned) kb[e] >= (unsigned) L.ns) continue;
+      n_in++;
+      long long w = 0;
+      if (WT) {
+        const int2 wa = S.aw[k + e];
+        w = fix_prod(wa.x, __int_as_float(wa.y), S.a[k + e].w,
+                     __float_as_int(bw.y), bw.z, bw.x);
+      }
+      hist_add<WT, BATCH>(L, ms, h, kb[e] + (IS_SMU(BIN) ? q * L.ns : 0), w,
+                          hs);
+    }
+  }
+}
+
 /* Compare a neighbour point (one per lane) with chunk points [i0, i1):
  * bit i - i0 of the result marks a candidate inside the outer range.  For
  * survey (s_perp, pi) counts (u, lh, lP) is the lane's line-of-sight
@@ -294,9 +381,13 @@ __device__ __forceinline__ uint32_t scan_chunk(const fcfcg_launch &L,
  * time, every lane busy.
  */
 /* (s, mu) binning keeps more values live: 3 CTAs per SM (85 registers)
- * measure faster there, 4 CTAs (64 registers) for the other binnings. */
+ * measure faster there, 4 CTAs (64 registers) for the other binnings and
+ * for weighted (s, mu) boxes (whose packed direct path would take 70
+ * registers and lose the fourth CTA: 40.6 ms against 35.4 ms with a 4-byte
+ * spill at 64). */
 template <int GEOM, int BIN, int WT, int BATCH, int ADJ>
-__global__ void __launch_bounds__(CT32_THREADS, IS_SMU(BIN) ? 3 : 4)
+__global__ void __launch_bounds__(CT32_THREADS,
+    (IS_SMU(BIN) && !(WT && GEOM == FCFCG_GEOM_BOX)) ? 3 : 4)
 k_count32(const fcfcg_launch L) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t sh_chunk;
@@ -665,6 +756,12 @@ k_count32(const fcfcg_launch L) {
          */
         const bool all_lim = __all_sync(FULLMASK, ilim >= m);
         const bool direct = !LOSCUT(GEOM, BIN) && all_lim && near_all;
+        if (PACKED_DIRECT(GEOM, BIN) && direct) {
+          bin_direct2<BIN, WT, BATCH>(L, &sh_mock, S, m, first, cx, cy, cz, bx,
+                                      by, bz, bjl, lane, h, n_in, n_q,
+                                      n_inline, hs);
+          continue;
+        }
         const uint32_t lt = (1u << lane) - 1u;
         uint32_t nq = direct ? (uint32_t) m * 32u : 0u;
         int i = direct ? m : 0;
