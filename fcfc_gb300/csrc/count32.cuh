@@ -234,8 +234,13 @@ __device__ __forceinline__ void candidate2(const fcfcg_launch &L, float4 pxy,
   }
 }
 
-/* Binnings whose direct blocks (every pair a candidate) take the packed
- * path below: boxes with linear s bins. */
+/* Binnings whose direct blocks take the packed path below: boxes with
+ * linear s bins.  Their direct blocks are those with a point within range
+ * of the whole chunk (the others: every pair a candidate); the binning
+ * drops the pairs beyond s_max (those whose mu window holds an edge go to
+ * the recheck, which drops them: dropping them here, when the s window lies
+ * beyond s_max, took two registers and measured 1 % slower than the 6 %
+ * more rechecks). */
 #define PACKED_DIRECT(G, B) ((G) == FCFCG_GEOM_BOX && LINS(B))
 
 /*
@@ -380,14 +385,14 @@ __device__ __forceinline__ uint32_t scan_chunk(const fcfcg_launch &L,
  * in-range pairs are then compacted into the warp queue and binned 32 at a
  * time, every lane busy.
  */
-/* (s, mu) binning keeps more values live: 3 CTAs per SM (85 registers)
- * measure faster there, 4 CTAs (64 registers) for the other binnings and
- * for weighted (s, mu) boxes (whose packed direct path would take 70
- * registers and lose the fourth CTA: 40.6 ms against 35.4 ms with a 4-byte
- * spill at 64). */
+/* Survey (s, mu) binning keeps more values live: 3 CTAs per SM (85
+ * registers) measure faster there, 4 CTAs (64 registers) for the other
+ * binnings and for (s, mu) boxes (whose packed direct path would take 66-70
+ * registers and lose the fourth CTA: weighted 40.6 ms against 35.4 ms with
+ * a 4-byte spill at 64). */
 template <int GEOM, int BIN, int WT, int BATCH, int ADJ>
 __global__ void __launch_bounds__(CT32_THREADS,
-    (IS_SMU(BIN) && !(WT && GEOM == FCFCG_GEOM_BOX)) ? 3 : 4)
+    (IS_SMU(BIN) && GEOM != FCFCG_GEOM_BOX) ? 3 : 4)
 k_count32(const fcfcg_launch L) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t sh_chunk;
@@ -719,7 +724,8 @@ k_count32(const fcfcg_launch L) {
        * exceeds that of any pair of the block */
       /* and a block all of whose points are within the outer range of
        * the whole box (its farthest corner, rounded the same way) is binned
-       * without the test, as a block of cells wholly in range */
+       * without the test, as a block of cells wholly in range (with the
+       * packed binning, a block with one such point) */
       bool near_all = base + 32u <= pin;
       if (!near_all) {
         bool far = true, near = false;
@@ -742,7 +748,13 @@ k_count32(const fcfcg_launch L) {
           }
         }
         if (__all_sync(FULLMASK, far)) continue;
-        near_all = __all_sync(FULLMASK, near);
+        /* the packed direct binning costs less per pair than the test, the
+         * queue and the scalar binning as soon as about a third of a
+         * block's pairs are in range: it takes every block with a point
+         * within range of the whole chunk (measured: one such point 333
+         * ms, eight 340, all 32 374 on 48 large mocks) */
+        near_all = PACKED_DIRECT(GEOM, BIN) ? __any_sync(FULLMASK, near)
+                                            : __all_sync(FULLMASK, near);
       }
       if (!ADJ) {
         /*
