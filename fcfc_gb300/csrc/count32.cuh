@@ -234,33 +234,43 @@ __device__ __forceinline__ void candidate2(const fcfcg_launch &L, float4 pxy,
   }
 }
 
-/* Binnings whose direct blocks take the packed path below: boxes with
- * linear s bins.  Their direct blocks are those with a point within range
+/* Binnings whose direct blocks take the packed path below: linear s bins
+ * (s or (s, mu); boxes and surveys).  Their direct blocks are those with a point within range
  * of the whole chunk (the others: every pair a candidate); the binning
  * drops the pairs beyond s_max (those whose mu window holds an edge go to
  * the recheck, which drops them: dropping them here, when the s window lies
  * beyond s_max, took two registers and measured 1 % slower than the 6 %
  * more rechecks). */
-#define PACKED_DIRECT(G, B) ((G) == FCFCG_GEOM_BOX && LINS(B))
+#define PACKED_DIRECT(G, B) LINS(B)
 
 /*
- * A direct block of a box with linear s bins: the lane's neighbour (bx, by,
- * bz; sorted index bj) against every chunk point, two chunk points per step
+ * A direct block with linear s bins: the lane's neighbour (bx, by, bz;
+ * sorted index bj) against every chunk point, two chunk points per step
  * (pxy = (x, x', y, y'), pz = (z, z')).  Packed FP32 operations round each
  * component as bin_pair's scalar ones do (q - Eq and t - W are formed as
  * fma(-1, Eq, q) and fma(-1, W, t), fl(q |dz| ...) as |fl(q dz ...)|: the
  * same roundings), so every pair gets bin_pair's bin and ambiguity bit for
  * bit; the neighbour's point, weight and index stay in the lane's
- * registers.
+ * registers.  Surveys: the line of sight m = (2 l_b + c2) + d with the
+ * lane's part formed once, as bin_pair forms it.
  */
-template <int BIN, int WT, int BATCH>
+template <int GEOM, int BIN, int WT, int BATCH>
 __device__ __forceinline__ void bin_direct2(const fcfcg_launch &L,
     const MockSh *ms, const Stage &S, int m, uint32_t first, int cx, int cy,
-    int cz, float bx, float by, float bz, uint32_t bj, int lane, uint32_t *h,
-    uint32_t &n_in, uint32_t &n_q, unsigned long long &n_inline, bool hs) {
+    int cz, float c2x, float c2y, float c2z, float bx, float by, float bz,
+    uint32_t bj, int lane, uint32_t *h, uint32_t &n_in, uint32_t &n_q,
+    unsigned long long &n_inline, bool hs) {
   const float2 nbx = make_float2(-bx, -bx), nby = make_float2(-by, -by),
                nbz = make_float2(-bz, -bz);
   const float2 m1 = make_float2(-1.f, -1.f);
+  float2 mbx, mby, mbz;                      /* survey: 2 l_b + c2 */
+  if (GEOM == FCFCG_GEOM_SURVEY) {
+    const float vx = fmaf(2.f, bx, c2x), vy = fmaf(2.f, by, c2y),
+                vz = fmaf(2.f, bz, c2z);
+    mbx = make_float2(vx, vx);
+    mby = make_float2(vy, vy);
+    mbz = make_float2(vz, vz);
+  }
   float4 bw = make_float4(0.f, 0.f, 0.f, 0.f);
   if (WT) bw = S.bw[lane];
   for (int k = 0; k < m; k += 2) {
@@ -274,7 +284,20 @@ __device__ __forceinline__ void bin_direct2(const fcfcg_launch &L,
     int qi[2] = {0, 0}, kb[2], klo[2];
     bool amb[2] = {!(s2.x >= L.tiny), !(s2.y >= L.tiny)};
     if (IS_SMU(BIN)) {
-      float2 q = __fmul2_rn(__fmul2_rn(make_float2(L.fnmu, L.fnmu), dz), rs);
+      float2 q;
+      if (GEOM == FCFCG_GEOM_BOX) {
+        q = __fmul2_rn(__fmul2_rn(make_float2(L.fnmu, L.fnmu), dz), rs);
+      } else {
+        const float2 mx = __fadd2_rn(mbx, dx), my = __fadd2_rn(mby, dy),
+                     mz = __fadd2_rn(mbz, dz);
+        const float2 dm = __ffma2_rn(dz, mz, __ffma2_rn(dy, my, __fmul2_rn(dx, mx)));
+        const float2 mm = __ffma2_rn(mz, mz, __ffma2_rn(my, my, __fmul2_rn(mx, mx)));
+        amb[0] |= !(mm.x >= L.m2min);
+        amb[1] |= !(mm.y >= L.m2min);
+        const float2 p = __fmul2_rn(mm, s2);
+        q = __fmul2_rn(__fmul2_rn(make_float2(L.fnmu, L.fnmu), dm),
+                       make_float2(rsqrtf(p.x), rsqrtf(p.y)));
+      }
       q = make_float2(fabsf(q.x), fabsf(q.y));
       const float2 Eq = __ffma2_rn(make_float2(L.Q1, L.Q1), rs,
           __ffma2_rn(make_float2(L.Q2, L.Q2), q, make_float2(L.Q0, L.Q0)));
@@ -302,8 +325,10 @@ __device__ __forceinline__ void bin_direct2(const fcfcg_launch &L,
       const uint32_t ai = first + (uint32_t) (k + e);
       if (a) {
         n_q++;
-        const uint32_t code = nb_code(BATCH ? ms->nc : L.ncell, cx, cy, cz,
-            __ldg((const int4 *) L.sten + S.bt[lane]));
+        const uint32_t code = (GEOM == FCFCG_GEOM_BOX)
+            ? nb_code(BATCH ? ms->nc : L.ncell, cx, cy, cz,
+                      __ldg((const int4 *) L.sten + S.bt[lane]))
+            : 0u;
         enqueue<WT, BATCH>(L, ms, ai, bj, code, h, n_inline, n_in, hs);
         continue;
       }
@@ -769,9 +794,9 @@ k_count32(const fcfcg_launch L) {
         const bool all_lim = __all_sync(FULLMASK, ilim >= m);
         const bool direct = !LOSCUT(GEOM, BIN) && all_lim && near_all;
         if (PACKED_DIRECT(GEOM, BIN) && direct) {
-          bin_direct2<BIN, WT, BATCH>(L, &sh_mock, S, m, first, cx, cy, cz, bx,
-                                      by, bz, bjl, lane, h, n_in, n_q,
-                                      n_inline, hs);
+          bin_direct2<GEOM, BIN, WT, BATCH>(L, &sh_mock, S, m, first, cx, cy,
+                                            cz, c2x, c2y, c2z, bx, by, bz, bjl,
+                                            lane, h, n_in, n_q, n_inline, hs);
           continue;
         }
         const uint32_t lt = (1u << lane) - 1u;
