@@ -254,12 +254,12 @@ __device__ __forceinline__ void candidate2(const fcfcg_launch &L, float4 pxy,
  * registers.  Surveys: the line of sight m = (2 l_b + c2) + d with the
  * lane's part formed once, as bin_pair forms it.
  */
-template <int GEOM, int BIN, int WT, int BATCH>
+template <int GEOM, int BIN, int WT, int BATCH, int ADJ>
 __device__ __forceinline__ void bin_direct2(const fcfcg_launch &L,
     const MockSh *ms, const Stage &S, int m, uint32_t first, int cx, int cy,
     int cz, float c2x, float c2y, float c2z, float bx, float by, float bz,
     uint32_t bj, int lane, uint32_t *h, uint32_t &n_in, uint32_t &n_q,
-    unsigned long long &n_inline, bool hs) {
+    unsigned long long &n_inline, bool hs, long long &gsum) {
   const float2 nbx = make_float2(-bx, -bx), nby = make_float2(-by, -by),
                nbz = make_float2(-bz, -bz);
   const float2 m1 = make_float2(-1.f, -1.f);
@@ -272,7 +272,9 @@ __device__ __forceinline__ void bin_direct2(const fcfcg_launch &L,
     mbz = make_float2(vz, vz);
   }
   float4 bw = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (WT) bw = S.bw[lane];
+  if (WT && !ADJ) bw = S.bw[lane];
+  double wbl = 0;                 /* adjoint: the neighbour's FP64 weight */
+  if (ADJ) wbl = S.wb[lane];
   for (int k = 0; k < m; k += 2) {
     const float4 pxy = S.pxy[k >> 1];
     const float2 dx = __fadd2_rn(make_float2(pxy.x, pxy.y), nbx);
@@ -329,7 +331,8 @@ __device__ __forceinline__ void bin_direct2(const fcfcg_launch &L,
             ? nb_code(BATCH ? ms->nc : L.ncell, cx, cy, cz,
                       __ldg((const int4 *) L.sten + S.bt[lane]))
             : 0u;
-        enqueue<WT, BATCH>(L, ms, ai, bj, code, h, n_inline, n_in, hs);
+        if (ADJ) enqueue_adj(L, ai, bj, code, n_inline, n_in);
+        else enqueue<WT, BATCH>(L, ms, ai, bj, code, h, n_inline, n_in, hs);
         continue;
       }
       int q = qi[e];
@@ -339,14 +342,24 @@ __device__ __forceinline__ void bin_direct2(const fcfcg_launch &L,
       }
       if ((unsigned) kb[e] >= (unsigned) L.ns) continue;
       n_in++;
+      const int bin = kb[e] + (IS_SMU(BIN) ? q * L.ns : 0);
+      if (ADJ) {
+        /* as bin_pair: the chunk point's term to its accumulator, the
+         * neighbour's summed in the lane (at most 64 terms below 2^50) */
+        const double g = L.hist_smem ? ((const double *) h)[bin]
+                                     : __ldg(L.gfix + bin);
+        adj_acc((uint32_t *) S.ga + (k + e), (int *) S.ga + FCHUNK + (k + e),
+                adj_term(wbl, g), L.dA + ai, L.gunit);
+        gsum += adj_term(S.wa[k + e], g);
+        continue;
+      }
       long long w = 0;
       if (WT) {
         const int2 wa = S.aw[k + e];
         w = fix_prod(wa.x, __int_as_float(wa.y), S.a[k + e].w,
                      __float_as_int(bw.y), bw.z, bw.x);
       }
-      hist_add<WT, BATCH>(L, ms, h, kb[e] + (IS_SMU(BIN) ? q * L.ns : 0), w,
-                          hs);
+      hist_add<WT, BATCH>(L, ms, h, bin, w, hs);
     }
   }
 }
@@ -794,9 +807,11 @@ k_count32(const fcfcg_launch L) {
         const bool all_lim = __all_sync(FULLMASK, ilim >= m);
         const bool direct = !LOSCUT(GEOM, BIN) && all_lim && near_all;
         if (PACKED_DIRECT(GEOM, BIN) && direct) {
-          bin_direct2<GEOM, BIN, WT, BATCH>(L, &sh_mock, S, m, first, cx, cy,
-                                            cz, c2x, c2y, c2z, bx, by, bz, bjl,
-                                            lane, h, n_in, n_q, n_inline, hs);
+          long long gsum = 0;
+          bin_direct2<GEOM, BIN, WT, BATCH, 0>(L, &sh_mock, S, m, first, cx,
+                                               cy, cz, c2x, c2y, c2z, bx, by,
+                                               bz, bjl, lane, h, n_in, n_q,
+                                               n_inline, hs, gsum);
           continue;
         }
         const uint32_t lt = (1u << lane) - 1u;
@@ -852,87 +867,100 @@ k_count32(const fcfcg_launch L) {
         }
         continue;
       }
-      /* compare with every chunk point (two 32-point halves); in weighted
-       * counts a block wholly in cells within range takes every chunk point
-       * (below ilim) without a test -- the binning checks each pair anyway
-       * (measured: 1-2 % faster weighted; the unweighted kernel's code runs
-       * 6 % slower with the branch, so it keeps the test) */
-      uint32_t m0, m1;
-      if (WT && !LOSCUT(GEOM, BIN) && base + 32u <= pin) {
-        const int lim = min(ilim, m);
-        m0 = (lim <= 0) ? 0u : (lim >= 32 ? ~0u : (1u << lim) - 1u);
-        m1 = (lim <= 32) ? 0u
-                         : (lim >= 64 ? ~0u : (1u << (lim - 32)) - 1u);
+      /* the adjoint's direct blocks (linear s bins): the packed binning,
+       * the lane's neighbour terms summed in a register */
+      if (PACKED_DIRECT(GEOM, BIN) && near_all &&
+          __all_sync(FULLMASK, ilim >= m)) {
+        long long gsum = 0;
+        bin_direct2<GEOM, BIN, WT, BATCH, ADJ>(L, &sh_mock, S, m, first, cx,
+                                               cy, cz, c2x, c2y, c2z, bx, by,
+                                               bz, bjl, lane, h, n_in, n_q,
+                                               n_inline, hs, gsum);
+        S.gb[lane] += gsum;
+        __syncwarp();
       } else {
-        m0 = scan_chunk<GEOM, BIN>(L, S.a, 0, min(m, 32), ilim, bx, by, bz,
-                                   ux, uy, uz, lh, lP);
-        m1 = (m > 32) ? scan_chunk<GEOM, BIN>(L, S.a, 32, m, ilim, bx, by,
-                                              bz, ux, uy, uz, lh, lP)
-                      : 0u;
-      }
-      /* compact the block's in-range pairs into the queue, qwarp per round */
-      const uint32_t cnt = __popc(m0) + __popc(m1);
-      uint32_t inc = cnt;
-      for (int s = 1; s < 32; s <<= 1) {
-        uint32_t u = __shfl_up_sync(FULLMASK, inc, s);
-        if (lane >= s) inc += u;
-      }
-      const uint32_t tot = __shfl_sync(FULLMASK, inc, 31);
-      const uint32_t excl = inc - cnt;
-      for (uint32_t r0 = 0; r0 < tot; r0 += L.qwarp) {
-        /* this lane's entries with positions in [r0, r0 + qwarp) */
-        uint32_t lo = excl > r0 ? excl : r0;
-        uint32_t hi = excl + cnt < r0 + L.qwarp ? excl + cnt : r0 + L.qwarp;
-        if (lo < hi) {
-          uint32_t b0 = m0, b1 = m1;
-          for (uint32_t sk = lo - excl; sk > 0; sk--) {
-            if (b0) b0 &= b0 - 1;
-            else b1 &= b1 - 1;
-          }
-          for (uint32_t pos = lo; pos < hi; pos++) {
-            uint32_t i;
-            if (b0) {
-              i = (uint32_t) (__ffs(b0) - 1);
-              b0 &= b0 - 1;
-            } else {
-              i = 32u + (uint32_t) (__ffs(b1) - 1);
-              b1 &= b1 - 1;
-            }
-            S.q[pos - r0] = (uint16_t) (i | ((uint32_t) lane << 6));
-          }
+        /* compare with every chunk point (two 32-point halves); in weighted
+         * counts a block wholly in cells within range takes every chunk point
+         * (below ilim) without a test -- the binning checks each pair anyway
+         * (measured: 1-2 % faster weighted; the unweighted kernel's code runs
+         * 6 % slower with the branch, so it keeps the test) */
+        uint32_t m0, m1;
+        if (WT && !LOSCUT(GEOM, BIN) && base + 32u <= pin) {
+          const int lim = min(ilim, m);
+          m0 = (lim <= 0) ? 0u : (lim >= 32 ? ~0u : (1u << lim) - 1u);
+          m1 = (lim <= 32) ? 0u
+                           : (lim >= 64 ? ~0u : (1u << (lim - 32)) - 1u);
+        } else {
+          m0 = scan_chunk<GEOM, BIN>(L, S.a, 0, min(m, 32), ilim, bx, by, bz,
+                                     ux, uy, uz, lh, lP);
+          m1 = (m > 32) ? scan_chunk<GEOM, BIN>(L, S.a, 32, m, ilim, bx, by,
+                                                bz, ux, uy, uz, lh, lP)
+                        : 0u;
         }
-        __syncwarp();
-        const uint32_t nr = (tot - r0 < L.qwarp) ? tot - r0 : L.qwarp;
-        /* pass k: lane l takes entry 32 k + l */
-        const uint32_t np = (nr + 31) >> 5;
-        for (uint32_t k = 0; k < np; k++) {
-          const uint32_t e = k * 32u + (uint32_t) lane;
-          long long gbv = 0;
-          int key = -1;
-          if (e < nr) {
-            const uint32_t ent = S.q[e];
-            key = (int) (ent >> 6);
-            bin_pair<GEOM, BIN, WT, BATCH, ADJ>(L, &sh_mock, S, ent, first,
-                                                cx, cy, cz, c2x, c2y, c2z, fs,
-                                                fp, fse, fpe, h, n_in, n_q,
-                                                n_inline, gbv, hs);
-          }
-          if (ADJ) {
-            /* the pass's entries run in neighbour order: sum each run of
-             * equal neighbours across the lanes (suffix sums within a run)
-             * and let the run's first lane add it -- the neighbour block is
-             * this warp's own, so no atomic is needed */
-            for (int o = 1; o < 32; o <<= 1) {
-              const long long t = __shfl_down_sync(FULLMASK, gbv, o);
-              const int k2 = __shfl_down_sync(FULLMASK, key, o);
-              if (lane + o < 32 && k2 == key) gbv += t;
-            }
-            const int kp = __shfl_up_sync(FULLMASK, key, 1);
-            if (key >= 0 && (lane == 0 || kp != key)) S.gb[key] += gbv;
-            __syncwarp();
-          }
+        /* compact the block's in-range pairs into the queue, qwarp per round */
+        const uint32_t cnt = __popc(m0) + __popc(m1);
+        uint32_t inc = cnt;
+        for (int s = 1; s < 32; s <<= 1) {
+          uint32_t u = __shfl_up_sync(FULLMASK, inc, s);
+          if (lane >= s) inc += u;
         }
-        __syncwarp();
+        const uint32_t tot = __shfl_sync(FULLMASK, inc, 31);
+        const uint32_t excl = inc - cnt;
+        for (uint32_t r0 = 0; r0 < tot; r0 += L.qwarp) {
+          /* this lane's entries with positions in [r0, r0 + qwarp) */
+          uint32_t lo = excl > r0 ? excl : r0;
+          uint32_t hi = excl + cnt < r0 + L.qwarp ? excl + cnt : r0 + L.qwarp;
+          if (lo < hi) {
+            uint32_t b0 = m0, b1 = m1;
+            for (uint32_t sk = lo - excl; sk > 0; sk--) {
+              if (b0) b0 &= b0 - 1;
+              else b1 &= b1 - 1;
+            }
+            for (uint32_t pos = lo; pos < hi; pos++) {
+              uint32_t i;
+              if (b0) {
+                i = (uint32_t) (__ffs(b0) - 1);
+                b0 &= b0 - 1;
+              } else {
+                i = 32u + (uint32_t) (__ffs(b1) - 1);
+                b1 &= b1 - 1;
+              }
+              S.q[pos - r0] = (uint16_t) (i | ((uint32_t) lane << 6));
+            }
+          }
+          __syncwarp();
+          const uint32_t nr = (tot - r0 < L.qwarp) ? tot - r0 : L.qwarp;
+          /* pass k: lane l takes entry 32 k + l */
+          const uint32_t np = (nr + 31) >> 5;
+          for (uint32_t k = 0; k < np; k++) {
+            const uint32_t e = k * 32u + (uint32_t) lane;
+            long long gbv = 0;
+            int key = -1;
+            if (e < nr) {
+              const uint32_t ent = S.q[e];
+              key = (int) (ent >> 6);
+              bin_pair<GEOM, BIN, WT, BATCH, ADJ>(L, &sh_mock, S, ent, first,
+                                                  cx, cy, cz, c2x, c2y, c2z, fs,
+                                                  fp, fse, fpe, h, n_in, n_q,
+                                                  n_inline, gbv, hs);
+            }
+            if (ADJ) {
+              /* the pass's entries run in neighbour order: sum each run of
+               * equal neighbours across the lanes (suffix sums within a run)
+               * and let the run's first lane add it -- the neighbour block is
+               * this warp's own, so no atomic is needed */
+              for (int o = 1; o < 32; o <<= 1) {
+                const long long t = __shfl_down_sync(FULLMASK, gbv, o);
+                const int k2 = __shfl_down_sync(FULLMASK, key, o);
+                if (lane + o < 32 && k2 == key) gbv += t;
+              }
+              const int kp = __shfl_up_sync(FULLMASK, key, 1);
+              if (key >= 0 && (lane == 0 || kp != key)) S.gb[key] += gbv;
+              __syncwarp();
+            }
+          }
+          __syncwarp();
+        }
       }
       if (ADJ) {
         /* the block's neighbour points are done: their gradients out */
