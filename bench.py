@@ -151,10 +151,11 @@ def fp32_peak_tflops(dev):
     return 2.0 * n ** 3 / (best * 1e-3) / 1e12
 
 
-def profile_value(key):
-    """A figure of the committed ncu summary of the dominant kernel (DRAM
-    bytes per launch, warp instructions per in-range pair), if present."""
-    p = os.path.join(ROOT, "profiles", "k_count32_box_smu_wt_ns_box.txt")
+def profile_value(key, name="k_count32_box_smu_wt_ns_box.txt"):
+    """A figure of a committed ncu summary (DRAM bytes per launch, warp
+    instructions per in-range pair), if present; by default the summary of
+    the box workload's dominant kernel."""
+    p = os.path.join(ROOT, "profiles", name)
     try:
         for line in open(p):
             if line.startswith(key + ":"):
@@ -168,12 +169,12 @@ def profile_traffic():
     return profile_value("traffic_bytes_per_launch_full_workload")
 
 
-def issue_bound(pairs_per_s, clocks):
+def issue_bound(pairs_per_s, clocks, name="k_count32_box_smu_wt_ns_box.txt"):
     """The bound the count kernel actually meets: instruction issue.  Warp
     instructions per in-range pair (ncu, committed summary) x pairs/s over
     the issue rate of the GPU (SMs x 4 schedulers x the SM clock sampled
     during the run)."""
-    ipp = profile_value("warp_instructions_per_in_range_pair")
+    ipp = profile_value("warp_instructions_per_in_range_pair", name)
     mhz = (clocks or {}).get("sm_mhz") or 2070.0
     if ipp is None:
         return None
@@ -671,12 +672,21 @@ def run_survey(args, rank, world, local, dist):
                 "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": 2 * (nd + nr) * 32,
                 "d2h_bytes_per_step": 3 * (p1.ntot + p2.ntot) * 8},
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "issue", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
                      "kernel": "k_count32<survey,smu,weighted> (RR)",
                      "kernel_ms": k_rr,
                      "peak_source": "measured cuBLAS SGEMM (TF32 off) on this GPU",
-                     "flops_per_pair": FLOPS_PER_PAIR["smu"]},
+                     "flops_per_pair": FLOPS_PER_PAIR["smu"],
+                     "issue": issue_bound(
+                         pairs[("smu", "RR")] / (k_rr * 1e-3), clocks,
+                         "k_count32_survey_smu_wt_rr.txt"),
+                     "from_profile": {
+                         "file": "profiles/k_count32_survey_smu_wt_rr.txt",
+                         "keys": ["issue.warp_instructions_per_pair"],
+                         "captured_on_current_source": (profile_info(
+                             "k_count32_survey_smu_wt_rr.txt") or {}).get(
+                                 "source_matches")}},
         "counters": {"kernel_ms_%s_%s" % k: v for k, v in kt.items()},
         "clocks": clocks,
         "gpu_launches": int(launches),
@@ -1068,7 +1078,7 @@ def main():
         "e2e": {"value": pairs_per_step / (e2e_ms * 1e-3), "unit": UNIT,
                 "ms_per_step": e2e_ms, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "issue", "achieved": achieved, "peak": peak,
                      "unit": "TFLOP/s", "frac": achieved / peak,
                      "traffic": traffic,
                      "kernel": "k_count32<box,smu,weighted>",
