@@ -320,46 +320,65 @@ __device__ __forceinline__ void bin_direct2(const fcfcg_launch &L,
     kb[1] = __float2int_rd(thi.y);
     klo[0] = max(__float2int_rd(tlo.x), L.lin_k0);
     klo[1] = max(__float2int_rd(tlo.y), L.lin_k0);
+    /* per pair, without branches: ambiguous (a), binned (ok), its bin;
+     * the second pair of an odd chunk's last step is neither */
+    bool a[2], ok[2];
+    int bin[2];
 #pragma unroll
     for (int e = 0; e < 2; e++) {
-      if (k + e >= m) break;
-      const bool a = amb[e] | (klo[e] != kb[e]);
-      const uint32_t ai = first + (uint32_t) (k + e);
-      if (a) {
+      const bool valid = (e == 0) || (k + 1 < m);
+      a[e] = valid && (amb[e] | (klo[e] != kb[e]));
+      int q = qi[e];
+      bool in = valid && !a[e] && (unsigned) kb[e] < (unsigned) L.ns;
+      if (IS_SMU(BIN)) {
+        in = in && (q < L.nmu || L.mu_one);
+        q = min(q, L.nmu - 1);
+      }
+      ok[e] = in;
+      bin[e] = kb[e] + (IS_SMU(BIN) ? q * L.ns : 0);
+    }
+    n_in += (uint32_t) ok[0] + (uint32_t) ok[1];
+    if (!WT && !ADJ && hs) {
+      if (ok[0]) atomicAdd(h + bin[0], 1u);
+      if (ok[1]) atomicAdd(h + bin[1], 1u);
+    } else {
+#pragma unroll
+      for (int e = 0; e < 2; e++) {
+        if (!ok[e]) continue;
+        if (ADJ) {
+          /* as bin_pair: the chunk point's term to its accumulator, the
+           * neighbour's summed in the lane (at most 64 terms below 2^50) */
+          const double g = L.hist_smem ? ((const double *) h)[bin[e]]
+                                       : __ldg(L.gfix + bin[e]);
+          adj_acc((uint32_t *) S.ga + (k + e), (int *) S.ga + FCHUNK + (k + e),
+                  adj_term(wbl, g), L.dA + first + (uint32_t) (k + e),
+                  L.gunit);
+          gsum += adj_term(S.wa[k + e], g);
+          continue;
+        }
+        long long w = 0;
+        if (WT) {
+          const int2 wa = S.aw[k + e];
+          w = fix_prod(wa.x, __int_as_float(wa.y), S.a[k + e].w,
+                       __float_as_int(bw.y), bw.z, bw.x);
+        }
+        hist_add<WT, BATCH>(L, ms, h, bin[e], w, hs);
+      }
+    }
+    /* the rare ambiguous pairs: to the FP64 recheck */
+    if (__any_sync(FULLMASK, a[0] | a[1])) {
+#pragma unroll
+      for (int e = 0; e < 2; e++) {
+        if (!a[e]) continue;
         n_q++;
         const uint32_t code = (GEOM == FCFCG_GEOM_BOX)
             ? nb_code(BATCH ? ms->nc : L.ncell, cx, cy, cz,
                       __ldg((const int4 *) L.sten + S.bt[lane]))
             : 0u;
+        const uint32_t ai = first + (uint32_t) (k + e);
         if (ADJ) enqueue_adj(L, ai, bj, code, n_inline, n_in);
         else enqueue<WT, BATCH>(L, ms, ai, bj, code, h, n_inline, n_in, hs);
-        continue;
       }
-      int q = qi[e];
-      if (IS_SMU(BIN) && q >= L.nmu) {
-        if (!L.mu_one) continue;
-        q = L.nmu - 1;
-      }
-      if ((unsigned) kb[e] >= (unsigned) L.ns) continue;
-      n_in++;
-      const int bin = kb[e] + (IS_SMU(BIN) ? q * L.ns : 0);
-      if (ADJ) {
-        /* as bin_pair: the chunk point's term to its accumulator, the
-         * neighbour's summed in the lane (at most 64 terms below 2^50) */
-        const double g = L.hist_smem ? ((const double *) h)[bin]
-                                     : __ldg(L.gfix + bin);
-        adj_acc((uint32_t *) S.ga + (k + e), (int *) S.ga + FCHUNK + (k + e),
-                adj_term(wbl, g), L.dA + ai, L.gunit);
-        gsum += adj_term(S.wa[k + e], g);
-        continue;
-      }
-      long long w = 0;
-      if (WT) {
-        const int2 wa = S.aw[k + e];
-        w = fix_prod(wa.x, __int_as_float(wa.y), S.a[k + e].w,
-                     __float_as_int(bw.y), bw.z, bw.x);
-      }
-      hist_add<WT, BATCH>(L, ms, h, bin, w, hs);
     }
   }
 }
@@ -423,14 +442,14 @@ __device__ __forceinline__ uint32_t scan_chunk(const fcfcg_launch &L,
  * in-range pairs are then compacted into the warp queue and binned 32 at a
  * time, every lane busy.
  */
-/* Survey (s, mu) binning keeps more values live: 3 CTAs per SM (85
- * registers) measure faster there, 4 CTAs (64 registers) for the other
- * binnings and for (s, mu) boxes (whose packed direct path would take 66-70
- * registers and lose the fourth CTA: weighted 40.6 ms against 35.4 ms with
- * a 4-byte spill at 64). */
+/* 4 CTAs per SM (64 registers) measure fastest for the counts: the packed
+ * direct path would take 66-70 registers and lose the fourth CTA (weighted
+ * box (s, mu) 40.6 ms against 35.4 ms with a 4-byte spill at 64, survey
+ * (s, mu) RR 93.9 against 84.4 ms).  The survey (s, mu) adjoint keeps 3
+ * (78 registers). */
 template <int GEOM, int BIN, int WT, int BATCH, int ADJ>
 __global__ void __launch_bounds__(CT32_THREADS,
-    (IS_SMU(BIN) && GEOM != FCFCG_GEOM_BOX) ? 3 : 4)
+    (IS_SMU(BIN) && GEOM != FCFCG_GEOM_BOX && ADJ) ? 3 : 4)
 k_count32(const fcfcg_launch L) {
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ uint32_t sh_chunk;
