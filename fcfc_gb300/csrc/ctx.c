@@ -664,10 +664,12 @@ static double box_volume(const double v[3]) { return v[0] * v[1] * v[2]; }
  * objects, the fastest refinement held 15 to 50 objects per cell.) */
 /* Default refinement: about `per_cell` objects per cell at the given
  * density (timed over k = 1..8: boxes 24 objects of the chunk catalogue;
- * surveys 130 at the geometric mean of the two catalogues' densities in
- * their occupied volumes -- on 1e6 data and 1e7 randoms with the packed
- * direct binning, RR fastest at k = 6 (2046 ms, 2324 at the old 8), DR at
- * k = 4 (427 ms, 495 at the old 5)). */
+ * survey s and (s, mu) counts 130 at the geometric mean of the two
+ * catalogues' densities in their occupied volumes -- on 1e6 data and 1e7
+ * randoms with the packed direct binning, RR fastest at k = 6 (2046 ms,
+ * 2324 at the old 8), DR at k = 4 (427 ms, 495 at the old 5); survey
+ * (s_perp, pi) counts, which keep the candidate test, 30 of the chunk
+ * catalogue: RR at k = 5 (430 ms), DR and DD at k = 2 (100, 5.6 ms)). */
 static int pick_k(double density, double reach, double per_cell) {
   const int k = (int) floor(reach * cbrt(density / per_cell) + 0.5);
   return k < 1 ? 1 : (k > 8 ? 8 : k);
@@ -721,7 +723,8 @@ static int grid_setup(fcfcg_ctx *c, grid_t *g, const slot_t *A,
   const double vbox = vol;
   if (!box && A->vol > 0 && A->vol < vol) vol = A->vol;
   double density = (double) A->n / (vol > 0 ? vol : 1);
-  if (!box && B != A) {
+  const int spi = (b->bintype == FCFCG_BIN_SPI);
+  if (!box && !spi && B != A) {
     double vb = vbox;
     if (B->vol > 0 && B->vol < vb) vb = B->vol;
     density = sqrt(density * ((double) B->n / (vb > 0 ? vb : 1)));
@@ -729,7 +732,8 @@ static int grid_setup(fcfcg_ctx *c, grid_t *g, const slot_t *A,
   g->key = tune_key(density, g->reach);
   int k = c->kcell;
   if (!k) k = (c->tuned_k && c->tuned_key == g->key)
-                  ? c->tuned_k : pick_k(density, r3, box ? 24.0 : 130.0);
+                  ? c->tuned_k
+                  : pick_k(density, r3, box ? 24.0 : (spi ? 30.0 : 130.0));
   g->k = k;
   const double maxcells = 16.0 * 1024 * 1024;
   double scale = 1;
