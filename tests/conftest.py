@@ -15,5 +15,5 @@ def pytest_configure(config):
 
 def pytest_collection_modifyitems(config, items):
     # GPU tests fail loudly when selected without a GPU; nothing is skipped
-    # silently on a GPU machine.
+    # silently on a machine that has one.
     pass
