@@ -211,3 +211,28 @@ def test_fp32_table_kind():
             # edges a factor 1.23 apart: 16 cells per octave resolve them
             assert 16 <= cpo <= 1 << 15
         pc.close()
+
+
+def test_grid_sub_bits_bounds():
+    """The grid sort's sub-cell choice (prep.cu:fcfcg_grid_sub_bits): 4x4x4
+    sub-cells where cells hold many objects, 2x2x2 or none as they thin out,
+    the fine counters at most ~4 per object (or 2^22), and the fine index
+    (cell << bits | sub-cell) always within 32 bits."""
+    import fcfc_gb300 as fg
+    lib = fg.load_library()
+    f = lib.fcfcg_grid_sub_bits
+    f.restype = C.c_int
+    f.argtypes = [C.c_size_t, C.c_size_t]
+    assert f(64000, 2000000) == 6            # ~31 objects per cell
+    assert f(1800000, 55000000) == 6
+    assert f(2000000, 4000000) == 3          # ~2 objects per cell
+    assert f(2000000, 2000000) == 0          # ~1: no sub-cells
+    assert f(40000000, 2000000) == 0
+    assert f(1000, 0) == 6                   # small grids: 2^22 counters
+    for nc in (1, 10 ** 3, 10 ** 5, 6 * 10 ** 7, 10 ** 8, 2 ** 31):
+        for n in (0, 10 ** 4, 10 ** 6, 10 ** 8, 4 * 10 ** 9):
+            sb = f(nc, n)
+            assert sb in (0, 3, 6)
+            if sb:
+                assert (nc << sb) < 0xFFFFFFF0
+                assert (nc << sb) <= max(4 * n, 1 << 22)
