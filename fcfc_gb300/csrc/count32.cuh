@@ -235,13 +235,14 @@ __device__ __forceinline__ void candidate2(const fcfcg_launch &L, float4 pxy,
 }
 
 /* Binnings whose direct blocks take the packed path below: linear s bins
- * (s or (s, mu); boxes and surveys).  Their direct blocks are those with a point within range
+ * (s or (s, mu); boxes and surveys) and box (s_perp, pi) (FP32 tables).  Their direct blocks are those with a point within range
  * of the whole chunk (the others: every pair a candidate); the binning
  * drops the pairs beyond s_max (those whose mu window holds an edge go to
  * the recheck, which drops them: dropping them here, when the s window lies
  * beyond s_max, took two registers and measured 1 % slower than the 6 %
  * more rechecks). */
-#define PACKED_DIRECT(G, B) LINS(B)
+#define PACKED_DIRECT(G, B) \
+  (LINS(B) || ((G) == FCFCG_GEOM_BOX && IS_SPI(B)))
 
 /*
  * A direct block with linear s bins: the lane's neighbour (bx, by, bz;
@@ -258,8 +259,9 @@ template <int GEOM, int BIN, int WT, int BATCH, int ADJ>
 __device__ __forceinline__ void bin_direct2(const fcfcg_launch &L,
     const MockSh *ms, const Stage &S, int m, uint32_t first, int cx, int cy,
     int cz, float c2x, float c2y, float c2z, float bx, float by, float bz,
-    uint32_t bj, int lane, uint32_t *h, uint32_t &n_in, uint32_t &n_q,
-    unsigned long long &n_inline, bool hs, long long &gsum) {
+    uint32_t bj, int lane, const uint16_t *fs, const uint16_t *fp,
+    const float *fse, const float *fpe, uint32_t *h, uint32_t &n_in,
+    uint32_t &n_q, unsigned long long &n_inline, bool hs, long long &gsum) {
   const float2 nbx = make_float2(-bx, -bx), nby = make_float2(-by, -by),
                nbz = make_float2(-bz, -bz);
   const float2 m1 = make_float2(-1.f, -1.f);
@@ -280,62 +282,84 @@ __device__ __forceinline__ void bin_direct2(const fcfcg_launch &L,
     const float2 dx = __fadd2_rn(make_float2(pxy.x, pxy.y), nbx);
     const float2 dy = __fadd2_rn(make_float2(pxy.z, pxy.w), nby);
     const float2 dz = __fadd2_rn(S.pz[k >> 1], nbz);
-    const float2 s2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
-    const float2 rs = make_float2(rsqrtf(s2.x), rsqrtf(s2.y));
-    const float2 s = __fmul2_rn(s2, rs);
-    int qi[2] = {0, 0}, kb[2], klo[2];
-    bool amb[2] = {!(s2.x >= L.tiny), !(s2.y >= L.tiny)};
-    if (IS_SMU(BIN)) {
-      float2 q;
-      if (GEOM == FCFCG_GEOM_BOX) {
-        q = __fmul2_rn(__fmul2_rn(make_float2(L.fnmu, L.fnmu), dz), rs);
-      } else {
-        const float2 mx = __fadd2_rn(mbx, dx), my = __fadd2_rn(mby, dy),
-                     mz = __fadd2_rn(mbz, dz);
-        const float2 dm = __ffma2_rn(dz, mz, __ffma2_rn(dy, my, __fmul2_rn(dx, mx)));
-        const float2 mm = __ffma2_rn(mz, mz, __ffma2_rn(my, my, __fmul2_rn(mx, mx)));
-        amb[0] |= !(mm.x >= L.m2min);
-        amb[1] |= !(mm.y >= L.m2min);
-        const float2 p = __fmul2_rn(mm, s2);
-        q = __fmul2_rn(__fmul2_rn(make_float2(L.fnmu, L.fnmu), dm),
-                       make_float2(rsqrtf(p.x), rsqrtf(p.y)));
-      }
-      q = make_float2(fabsf(q.x), fabsf(q.y));
-      const float2 Eq = __ffma2_rn(make_float2(L.Q1, L.Q1), rs,
-          __ffma2_rn(make_float2(L.Q2, L.Q2), q, make_float2(L.Q0, L.Q0)));
-      const float2 qlo = __ffma2_rn(m1, Eq, q);
-      const float2 qhi = __fadd2_rn(q, Eq);
-      qi[0] = __float2int_rz(qhi.x);
-      qi[1] = __float2int_rz(qhi.y);
-      amb[0] |= (__float2int_rz(qlo.x) != qi[0]);
-      amb[1] |= (__float2int_rz(qlo.y) != qi[1]);
-    }
-    const float2 t = __ffma2_rn(s, make_float2(L.lin_inv, L.lin_inv),
-                                make_float2(L.lin_off, L.lin_off));
-    const float2 W = __ffma2_rn(make_float2(L.lin_A, L.lin_A), s,
-                                make_float2(L.lin_B, L.lin_B));
-    const float2 tlo = __ffma2_rn(m1, W, t);
-    const float2 thi = __fadd2_rn(t, W);
-    kb[0] = __float2int_rd(thi.x);
-    kb[1] = __float2int_rd(thi.y);
-    klo[0] = max(__float2int_rd(tlo.x), L.lin_k0);
-    klo[1] = max(__float2int_rd(tlo.y), L.lin_k0);
-    /* per pair, without branches: ambiguous (a), binned (ok), its bin;
-     * the second pair of an odd chunk's last step is neither */
     bool a[2], ok[2];
     int bin[2];
+    if (IS_SPI(BIN)) {
+      /* box (s_perp, pi): bin_pair's table lookups, per pair */
+      const float2 sp2 = __ffma2_rn(dy, dy, __fmul2_rn(dx, dx));
 #pragma unroll
-    for (int e = 0; e < 2; e++) {
-      const bool valid = (e == 0) || (k + 1 < m);
-      a[e] = valid && (amb[e] | (klo[e] != kb[e]));
-      int q = qi[e];
-      bool in = valid && !a[e] && (unsigned) kb[e] < (unsigned) L.ns;
-      if (IS_SMU(BIN)) {
-        in = in && (q < L.nmu || L.mu_one);
-        q = min(q, L.nmu - 1);
+      for (int e = 0; e < 2; e++) {
+        const float v = e ? sp2.y : sp2.x;
+        const float pi = fabsf(e ? dz.y : dz.x);
+        bool am = !(v >= L.tiny);
+        const float Es = LOGTAB(BIN)
+            ? fmaf(L.K2, v, fmaf(L.K1, v * rsqrtf(v), L.K0)) : L.Emax;
+        const unsigned sb = ftab_bin<false, LOGTAB(BIN)>(fs, L.fsoff, L.nfs,
+            L.fsinv, fse, L.nsb, v, Es, am, L.fslog, L.fsamb);
+        const unsigned pbn = ftab_bin<false, false>(fp, L.fpoff, L.nfp,
+            L.fpinv, fpe, L.npb, pi, L.P0, am, L.fplog, L.fpamb);
+        const bool valid = (e == 0) || (k + 1 < m);
+        a[e] = valid && am;
+        ok[e] = valid && !am && sb != FCFCG_FTAB_BIN_MASK &&
+                pbn != FCFCG_FTAB_BIN_MASK;
+        bin[e] = (int) sb + (int) pbn * L.ns;
       }
-      ok[e] = in;
-      bin[e] = kb[e] + (IS_SMU(BIN) ? q * L.ns : 0);
+    } else {
+      const float2 s2 = __ffma2_rn(dz, dz, __ffma2_rn(dy, dy, __fmul2_rn(dx, dx)));
+      const float2 rs = make_float2(rsqrtf(s2.x), rsqrtf(s2.y));
+      const float2 s = __fmul2_rn(s2, rs);
+      int qi[2] = {0, 0}, kb[2], klo[2];
+      bool amb[2] = {!(s2.x >= L.tiny), !(s2.y >= L.tiny)};
+      if (IS_SMU(BIN)) {
+        float2 q;
+        if (GEOM == FCFCG_GEOM_BOX) {
+          q = __fmul2_rn(__fmul2_rn(make_float2(L.fnmu, L.fnmu), dz), rs);
+        } else {
+          const float2 mx = __fadd2_rn(mbx, dx), my = __fadd2_rn(mby, dy),
+                       mz = __fadd2_rn(mbz, dz);
+          const float2 dm = __ffma2_rn(dz, mz, __ffma2_rn(dy, my, __fmul2_rn(dx, mx)));
+          const float2 mm = __ffma2_rn(mz, mz, __ffma2_rn(my, my, __fmul2_rn(mx, mx)));
+          amb[0] |= !(mm.x >= L.m2min);
+          amb[1] |= !(mm.y >= L.m2min);
+          const float2 p = __fmul2_rn(mm, s2);
+          q = __fmul2_rn(__fmul2_rn(make_float2(L.fnmu, L.fnmu), dm),
+                         make_float2(rsqrtf(p.x), rsqrtf(p.y)));
+        }
+        q = make_float2(fabsf(q.x), fabsf(q.y));
+        const float2 Eq = __ffma2_rn(make_float2(L.Q1, L.Q1), rs,
+            __ffma2_rn(make_float2(L.Q2, L.Q2), q, make_float2(L.Q0, L.Q0)));
+        const float2 qlo = __ffma2_rn(m1, Eq, q);
+        const float2 qhi = __fadd2_rn(q, Eq);
+        qi[0] = __float2int_rz(qhi.x);
+        qi[1] = __float2int_rz(qhi.y);
+        amb[0] |= (__float2int_rz(qlo.x) != qi[0]);
+        amb[1] |= (__float2int_rz(qlo.y) != qi[1]);
+      }
+      const float2 t = __ffma2_rn(s, make_float2(L.lin_inv, L.lin_inv),
+                                  make_float2(L.lin_off, L.lin_off));
+      const float2 W = __ffma2_rn(make_float2(L.lin_A, L.lin_A), s,
+                                  make_float2(L.lin_B, L.lin_B));
+      const float2 tlo = __ffma2_rn(m1, W, t);
+      const float2 thi = __fadd2_rn(t, W);
+      kb[0] = __float2int_rd(thi.x);
+      kb[1] = __float2int_rd(thi.y);
+      klo[0] = max(__float2int_rd(tlo.x), L.lin_k0);
+      klo[1] = max(__float2int_rd(tlo.y), L.lin_k0);
+      /* per pair, without branches: ambiguous (a), binned (ok), its bin;
+       * the second pair of an odd chunk's last step is neither */
+#pragma unroll
+      for (int e = 0; e < 2; e++) {
+        const bool valid = (e == 0) || (k + 1 < m);
+        a[e] = valid && (amb[e] | (klo[e] != kb[e]));
+        int q = qi[e];
+        bool in = valid && !a[e] && (unsigned) kb[e] < (unsigned) L.ns;
+        if (IS_SMU(BIN)) {
+          in = in && (q < L.nmu || L.mu_one);
+          q = min(q, L.nmu - 1);
+        }
+        ok[e] = in;
+        bin[e] = kb[e] + (IS_SMU(BIN) ? q * L.ns : 0);
+      }
     }
     n_in += (uint32_t) ok[0] + (uint32_t) ok[1];
     if (!WT && !ADJ && hs) {
@@ -829,8 +853,9 @@ k_count32(const fcfcg_launch L) {
           long long gsum = 0;
           bin_direct2<GEOM, BIN, WT, BATCH, 0>(L, &sh_mock, S, m, first, cx,
                                                cy, cz, c2x, c2y, c2z, bx, by,
-                                               bz, bjl, lane, h, n_in, n_q,
-                                               n_inline, hs, gsum);
+                                               bz, bjl, lane, fs, fp, fse, fpe,
+                                               h, n_in, n_q, n_inline, hs,
+                                               gsum);
           continue;
         }
         const uint32_t lt = (1u << lane) - 1u;
@@ -893,8 +918,9 @@ k_count32(const fcfcg_launch L) {
         long long gsum = 0;
         bin_direct2<GEOM, BIN, WT, BATCH, ADJ>(L, &sh_mock, S, m, first, cx,
                                                cy, cz, c2x, c2y, c2z, bx, by,
-                                               bz, bjl, lane, h, n_in, n_q,
-                                               n_inline, hs, gsum);
+                                               bz, bjl, lane, fs, fp, fse, fpe,
+                                               h, n_in, n_q, n_inline, hs,
+                                               gsum);
         S.gb[lane] += gsum;
         __syncwarp();
       } else {
